@@ -1,0 +1,144 @@
+/*
+ * poisson_solver_gb300.h -- C ABI of the GB300-native Green's-function FFT
+ * Poisson solver (solves lap(A) = -B on 3D unbounded, periodic and mixed
+ * unbounded/periodic domains, optionally returning grad, div or curl of A).
+ *
+ * The entry points replace the public C++ interface of the reference solver
+ * (mmhej/poissonsolver, c++/source/poisson_solver.hpp:107-122); each one names
+ * the member it stands for. include/poisson_solver.hpp re-creates that class
+ * on top of this ABI so existing client code compiles unchanged.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only. Real fields are double arrays of
+ *     Nx*Ny*Nz values laid out [Nz][Ny][Nx] (x fastest), index (k*Ny + j)*Nx + i,
+ *     exactly as the reference's push/pull take them.
+ *   - Boundary conditions per axis: 0 = unbounded (free space), 1 = periodic.
+ *     Supported combinations, as in the reference: (0,0,0), (1,1,1),
+ *     (1,1,0) and (0,0,1).
+ *   - Every call returns a PS_* status; ps_last_error() gives the message of
+ *     the last failure on a handle. No call exits the process.
+ *   - A handle is not thread-safe; use one handle per host thread.
+ *   - All GPU work runs on the handle's stream (default: the legacy stream).
+ */
+#ifndef POISSON_SOLVER_GB300_H
+#define POISSON_SOLVER_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ps_solver ps_solver;
+
+/* Status codes. */
+enum {
+    PS_OK = 0,
+    PS_ERR_ARGUMENT = 1,    /* bad pointer, size or option value */
+    PS_ERR_BOUNDARY = 2,    /* unsupported boundary-condition combination */
+    PS_ERR_COMPONENTS = 3,  /* pushed components do not fit the output option */
+    PS_ERR_MEMORY = 4,      /* device or host allocation failed */
+    PS_ERR_CUDA = 5,        /* a CUDA call failed */
+    PS_ERR_STATE = 6,       /* call out of order (e.g. solve before setup/push) */
+    PS_ERR_UNSUPPORTED = 7  /* outside what this build implements (e.g. 2D) */
+};
+
+/* Options for ps_set_option. */
+enum {
+    PS_OPT_GRAD = 0,       /* value 0/1: return grad A   (set_return_grad, settings.cpp:9)  */
+    PS_OPT_DIV = 1,        /* value 0/1: return div A    (set_return_div, settings.cpp:15)  */
+    PS_OPT_CURL = 2,       /* value 0/1: return curl A   (set_return_curl, settings.cpp:21) */
+    PS_OPT_REPROJECT = 3,  /* value 0/1: reproject the returned B (set_reprojection, settings.cpp:26) */
+    PS_OPT_PRECISION = 4   /* PS_PREC_FP64 (default) or PS_PREC_FP32 transforms */
+};
+
+enum {
+    PS_PREC_FP64 = 0,  /* all transforms and the spectral operation in FP64 */
+    PS_PREC_FP32 = 1   /* FP64 kernel build, FP32 transforms, FP64 field I/O */
+};
+
+/* Constructor / destructor: poisson_solver::poisson_solver / ~poisson_solver
+ * (poisson_solver.hpp:107-108). ps_create binds the handle to the current
+ * CUDA device. */
+int ps_create(ps_solver **out);
+int ps_destroy(ps_solver *h);
+
+/* poisson_solver::setup3d(int ncell[3], int bc[3], double dx[3], int reg_order)
+ * (poisson_solver.hpp:111, setup3d.cpp:8-71): grid of ncell cells of size dx,
+ * boundary conditions bc, regularisation order reg_order (0 = none; odd orders
+ * round up to the next even one). Builds the spectral kernel on the GPU. */
+int ps_setup3d(ps_solver *h, const int ncell[3], const int bc[3], const double dx[3], int reg_order);
+
+/* set_return_grad / set_return_div / set_return_curl / set_reprojection
+ * (poisson_solver.hpp:113-116), plus the transform precision. */
+int ps_set_option(ps_solver *h, int option, int value);
+int ps_get_option(const ps_solver *h, int option, int *value);
+
+/* poisson_solver::push(double*, double*, double*) (poisson_solver.hpp:121,
+ * push.cpp:9-397): copy the right-hand side B from HOST arrays; a NULL
+ * pointer means the component is absent. */
+int ps_push(ps_solver *h, const double *bx, const double *by, const double *bz);
+
+/* poisson_solver::solve3d() (poisson_solver.hpp:119, solve3d.cpp:8-635).
+ * Fails with PS_ERR_COMPONENTS where the reference prints its "rhs fields
+ * have not been pushed correctly" error: grad needs B_x, div and curl need all
+ * three components. grad with fewer than three components differentiates
+ * B_x along the missing directions (the reference dereferences NULL there). */
+int ps_solve3d(ps_solver *h);
+
+/* poisson_solver::pull(Ax, Ay, Az, Bx, By, Bz) (poisson_solver.hpp:122,
+ * pull.cpp:8-469): copy the solution (A, or its grad/div/curl) and,
+ * when Bx/By/Bz are non-NULL, the right-hand side as the solve used it
+ * (regularised and, if enabled, reprojected) into HOST arrays. Arrays of
+ * components the last solve did not produce are left untouched. */
+int ps_pull(ps_solver *h, double *ax, double *ay, double *az, double *bx, double *by, double *bz);
+
+/* Device-pointer forms of push and pull (same semantics; pointers are CUDA
+ * device memory of the handle's device). */
+int ps_push_device(ps_solver *h, const double *bx, const double *by, const double *bz);
+int ps_pull_device(ps_solver *h, double *ax, double *ay, double *az, double *bx, double *by, double *bz);
+
+/* Device-resident solve in one call: B in device memory -> A in device
+ * memory, no copies through the handle's own field buffers. NULL B pointers
+ * are absent components; NULL A pointers are outputs not written. Equivalent
+ * to push_device + solve3d + pull_device of A. */
+int ps_solve3d_device(ps_solver *h, const double *bx, const double *by, const double *bz,
+                      double *ax, double *ay, double *az);
+
+/* The public member `std::vector<class_partition> partition`
+ * (poisson_solver.hpp:102, class_partition.hpp:29-43): one GPU holds the
+ * whole grid, so there is exactly one partition: ncell = the grid, icell = 0. */
+int ps_partition_count(const ps_solver *h);
+int ps_partition(const ps_solver *h, int index, int ncell[3], int icell[3], double dx[3]);
+
+/* setup2d / solve2d (poisson_solver.hpp:110, 118): the 2D solver is not
+ * part of this build; both return PS_ERR_UNSUPPORTED. */
+int ps_setup2d(ps_solver *h, const int ncell[2], const int bc[2], const double dx[2], int reg_order);
+int ps_solve2d(ps_solver *h);
+
+/* Stream the handle launches on (a cudaStream_t; NULL = legacy default). */
+int ps_set_stream(ps_solver *h, void *stream);
+/* Wait for the handle's stream. */
+int ps_synchronize(ps_solver *h);
+
+/* Message of the last failed call on h ("" when none); static text for a
+ * status code. */
+const char *ps_last_error(const ps_solver *h);
+const char *ps_status_string(int status);
+
+/* Introspection used by tests and benchmarks. */
+enum {
+    PS_INFO_PADDED_X = 0, PS_INFO_PADDED_Y = 1, PS_INFO_PADDED_Z = 2, /* transform lengths */
+    PS_INFO_LAUNCHES_PER_SOLVE = 3,  /* kernels one solve launches */
+    PS_INFO_DEVICE_BYTES = 4,        /* device memory the handle holds */
+    PS_INFO_KERNEL_OCTANT = 5        /* elements of the stored kernel octant */
+};
+int ps_get_info(const ps_solver *h, int what, double *value);
+
+/* Copy the FP64 kernel octant K = G * zeta / (Px Py Pz), layout
+ * [Pz/2+1][Py/2+1][Px/2+1] (x fastest), to a HOST array. */
+int ps_get_kernel(const ps_solver *h, double *out, long long capacity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

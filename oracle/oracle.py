@@ -1,0 +1,149 @@
+"""ctypes front end for the CPU oracle. TEST INFRASTRUCTURE ONLY.
+
+Two libraries sit behind the same calls:
+
+* ``port``      -- oracle/_build/libps_oracle.so, the plain-C restatement of the
+                   reference solve (oracle/ps_oracle.c). Built anywhere.
+* ``reference`` -- oracle/_ref/libpsref.so, the unmodified reference C++ sources
+                   compiled with a single-rank MPI stand-in (oracle/Makefile).
+                   Only buildable where the reference sources are present.
+
+Only tests, the smoke check and the benchmark's CPU-baseline leg import this
+module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libps_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libpsref.so")
+DEFAULT_REF = "/root/reference"
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_libs: dict[str, ctypes.CDLL] = {}
+
+
+def build(reference_root: str | None = None) -> None:
+    """Compile the port (always) and the reference library (when its sources exist)."""
+    ref = reference_root or os.environ.get("PS_REFERENCE_ROOT", DEFAULT_REF)
+    subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile"), f"REF={ref}", "all"],
+                   check=True, cwd=HERE)
+
+
+def available(kind: str = "port") -> bool:
+    return os.path.exists(PORT_SO if kind == "port" else REF_SO)
+
+
+def _lib(kind: str) -> ctypes.CDLL:
+    if kind in _libs:
+        return _libs[kind]
+    path = PORT_SO if kind == "port" else REF_SO
+    if not os.path.exists(path):
+        if kind == "port":
+            build()
+        else:
+            raise FileNotFoundError(f"{path} not built (reference sources needed)")
+    lib = ctypes.CDLL(path)
+    pre = "oracle_" if kind == "port" else "ref_"
+    f = getattr(lib, pre + "solve3d")
+    f.restype = ctypes.c_int
+    f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 4 + [_dp] * 9
+    f = getattr(lib, pre + "greens3d")
+    f.restype = ctypes.c_int
+    f.argtypes = [_ip, _ip, _dp, ctypes.c_int, _dp, _dp, _dp, _ip]
+    f = getattr(lib, pre + "fft")
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
+    for name in ("sine_int", "bessel_int_J0"):
+        f = getattr(lib, pre + name)
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_double]
+    _libs[kind] = lib
+    return lib
+
+
+def _fn(kind: str, name: str):
+    return getattr(_lib(kind), ("oracle_" if kind == "port" else "ref_") + name)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a):
+    if a is None:
+        return None
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def sine_int(x: float, kind: str = "port") -> float:
+    return _fn(kind, "sine_int")(float(x))
+
+
+def bessel_int_J0(x: float, kind: str = "port") -> float:
+    return _fn(kind, "bessel_int_J0")(float(x))
+
+
+def fft(z: np.ndarray, inverse: bool = False, kind: str = "port") -> np.ndarray:
+    """Unnormalised transform of a complex vector (forward e^{-2 pi i jk/n})."""
+    z = np.ascontiguousarray(z, dtype=np.complex128).copy()
+    buf = z.view(np.float64)
+    st = _fn(kind, "fft")(z.size, 1 if inverse else -1, _ptr(buf))
+    if st:
+        raise RuntimeError(f"oracle fft status {st}")
+    return z
+
+
+def greens3d(ncell, bc, dx, reg: int = 0, kind: str = "port"):
+    """(G complex [Pz][Py][Px], zeta [Pz][Py][Px] or None) as the kernel build makes them."""
+    nc = (ctypes.c_int * 3)(*ncell)
+    b = (ctypes.c_int * 3)(*bc)
+    d = (ctypes.c_double * 3)(*dx)
+    p = [(2 if bc[i] == 0 else 1) * ncell[i] for i in range(3)]
+    n = p[0] * p[1] * p[2]
+    gre = np.zeros(n)
+    gim = np.zeros(n)
+    zeta = np.zeros(n) if reg > 0 else None
+    pext = (ctypes.c_int * 3)()
+    st = _fn(kind, "greens3d")(nc, b, d, int(reg), _ptr(gre), _ptr(gim), _ptr(zeta), pext)
+    if st:
+        raise ValueError(f"oracle greens3d status {st}")
+    shape = (p[2], p[1], p[0])
+    g = (gre + 1j * gim).reshape(shape)
+    return g, (zeta.reshape(shape) if zeta is not None else None)
+
+
+def solve3d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False,
+            reproject=False, want_rhs=False, kind: str = "port"):
+    """Run setup3d/push/solve3d/pull. B: sequence of 3 arrays [Nz][Ny][Nx] or None.
+
+    Returns (A, RB): lists of 3 arrays or None (component not produced).
+    """
+    nx, ny, nz = ncell
+    shape = (nz, ny, nx)
+    Bc = [_f64(b) for b in B]
+    for b in Bc:
+        if b is not None and b.shape != shape:
+            raise ValueError(f"field shape {b.shape} != {shape}")
+    nan = float("nan")
+    A = [np.full(shape, nan) for _ in range(3)]
+    RB = [np.full(shape, nan) for _ in range(3)] if want_rhs else [None] * 3
+    nc = (ctypes.c_int * 3)(*ncell)
+    b = (ctypes.c_int * 3)(*bc)
+    d = (ctypes.c_double * 3)(*dx)
+    st = _fn(kind, "solve3d")(nc, b, d, int(reg), int(grad), int(div), int(curl), int(reproject),
+                              *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
+    if st:
+        raise ValueError(f"oracle solve3d status {st}")
+    # components the solve did not produce stay NaN-filled: report them as None
+    A = [a if not np.isnan(a).all() else None for a in A]
+    RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
+    return A, RB

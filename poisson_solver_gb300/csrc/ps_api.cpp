@@ -1,0 +1,201 @@
+// C ABI (include/poisson_solver_gb300.h) over ps::Solver. Every entry point
+// catches the solver's exceptions and turns them into a status code plus the
+// handle's last-error message; nothing propagates across the ABI.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "poisson_solver_gb300.h"
+#include "ps_solver.hpp"
+
+struct ps_solver {
+    ps::Solver s;
+};
+
+namespace {
+
+template <typename F> int guarded(ps_solver *h, F &&f)
+{
+    if (!h) return PS_ERR_ARGUMENT;
+    try {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != h->s.device) cudaSetDevice(h->s.device);
+        f(h->s);
+        h->s.last_error.clear();
+        return PS_OK;
+    } catch (const ps::Error &e) {
+        h->s.last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        h->s.last_error = "host allocation failed";
+        return PS_ERR_MEMORY;
+    } catch (const std::exception &e) {
+        h->s.last_error = e.what();
+        return PS_ERR_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ps_create(ps_solver **out)
+{
+    if (!out) return PS_ERR_ARGUMENT;
+    *out = nullptr;
+    try {
+        *out = new ps_solver();
+    } catch (const ps::Error &e) {
+        return e.status;
+    } catch (...) {
+        return PS_ERR_MEMORY;
+    }
+    return PS_OK;
+}
+
+int ps_destroy(ps_solver *h)
+{
+    if (!h) return PS_OK;
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != h->s.device) cudaSetDevice(h->s.device);
+    if (h->s.stream) cudaStreamSynchronize(h->s.stream);
+    delete h;
+    return PS_OK;
+}
+
+int ps_setup3d(ps_solver *h, const int ncell[3], const int bc[3], const double dx[3], int reg_order)
+{
+    if (!ncell || !bc || !dx) return h ? (h->s.last_error = "NULL argument", PS_ERR_ARGUMENT) : PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) { s.setup3d(ncell, bc, dx, reg_order); });
+}
+
+int ps_set_option(ps_solver *h, int option, int value)
+{
+    return guarded(h, [&](ps::Solver &s) { s.set_option(option, value); });
+}
+
+int ps_get_option(const ps_solver *h, int option, int *value)
+{
+    if (!value) return PS_ERR_ARGUMENT;
+    return guarded(const_cast<ps_solver *>(h), [&](ps::Solver &s) { *value = s.get_option(option); });
+}
+
+int ps_push(ps_solver *h, const double *bx, const double *by, const double *bz)
+{
+    const double *B[3] = {bx, by, bz};
+    return guarded(h, [&](ps::Solver &s) { s.push(B, cudaMemcpyHostToDevice); });
+}
+
+int ps_push_device(ps_solver *h, const double *bx, const double *by, const double *bz)
+{
+    const double *B[3] = {bx, by, bz};
+    return guarded(h, [&](ps::Solver &s) { s.push(B, cudaMemcpyDeviceToDevice); });
+}
+
+int ps_solve3d(ps_solver *h)
+{
+    return guarded(h, [&](ps::Solver &s) { s.solve_internal(); });
+}
+
+int ps_pull(ps_solver *h, double *ax, double *ay, double *az, double *bx, double *by, double *bz)
+{
+    double *A[3] = {ax, ay, az}, *RB[3] = {bx, by, bz};
+    return guarded(h, [&](ps::Solver &s) { s.pull(A, RB, cudaMemcpyDeviceToHost); });
+}
+
+int ps_pull_device(ps_solver *h, double *ax, double *ay, double *az, double *bx, double *by, double *bz)
+{
+    double *A[3] = {ax, ay, az}, *RB[3] = {bx, by, bz};
+    return guarded(h, [&](ps::Solver &s) { s.pull(A, RB, cudaMemcpyDeviceToDevice); });
+}
+
+int ps_solve3d_device(ps_solver *h, const double *bx, const double *by, const double *bz,
+                      double *ax, double *ay, double *az)
+{
+    const double *B[3] = {bx, by, bz};
+    double *A[3] = {ax, ay, az};
+    return guarded(h, [&](ps::Solver &s) { s.solve(B, A); });
+}
+
+int ps_partition_count(const ps_solver *h) { return (h && h->s.is_setup) ? 1 : 0; }
+
+int ps_partition(const ps_solver *h, int index, int ncell[3], int icell[3], double dx[3])
+{
+    if (!h) return PS_ERR_ARGUMENT;
+    if (!h->s.is_setup) return PS_ERR_STATE;
+    if (index != 0) return PS_ERR_ARGUMENT;
+    for (int d = 0; d < 3; ++d) {
+        if (ncell) ncell[d] = h->s.n[d];
+        if (icell) icell[d] = 0;
+        if (dx) dx[d] = h->s.dx[d];
+    }
+    return PS_OK;
+}
+
+int ps_setup2d(ps_solver *h, const int *, const int *, const double *, int)
+{
+    if (h) h->s.last_error = "the 2D solver is not part of this build";
+    return PS_ERR_UNSUPPORTED;
+}
+
+int ps_solve2d(ps_solver *h)
+{
+    if (h) h->s.last_error = "the 2D solver is not part of this build";
+    return PS_ERR_UNSUPPORTED;
+}
+
+int ps_set_stream(ps_solver *h, void *stream)
+{
+    return guarded(h, [&](ps::Solver &s) { s.stream = (cudaStream_t)stream; });
+}
+
+int ps_synchronize(ps_solver *h)
+{
+    return guarded(h, [&](ps::Solver &s) {
+        cudaError_t e = cudaStreamSynchronize(s.stream);
+        if (e != cudaSuccess) throw ps::Error(PS_ERR_CUDA, cudaGetErrorString(e));
+    });
+}
+
+const char *ps_last_error(const ps_solver *h) { return h ? h->s.last_error.c_str() : "NULL handle"; }
+
+const char *ps_status_string(int status)
+{
+    switch (status) {
+    case PS_OK: return "ok";
+    case PS_ERR_ARGUMENT: return "invalid argument";
+    case PS_ERR_BOUNDARY: return "unsupported boundary conditions";
+    case PS_ERR_COMPONENTS: return "pushed components do not fit the output option";
+    case PS_ERR_MEMORY: return "out of memory";
+    case PS_ERR_CUDA: return "CUDA error";
+    case PS_ERR_STATE: return "call out of order";
+    case PS_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+int ps_get_info(const ps_solver *h, int what, double *value)
+{
+    if (!h || !value) return PS_ERR_ARGUMENT;
+    const ps::Solver &s = h->s;
+    switch (what) {
+    case PS_INFO_PADDED_X: *value = s.P[0]; break;
+    case PS_INFO_PADDED_Y: *value = s.P[1]; break;
+    case PS_INFO_PADDED_Z: *value = s.P[2]; break;
+    case PS_INFO_LAUNCHES_PER_SOLVE: *value = 5; break;
+    case PS_INFO_DEVICE_BYTES: *value = (double)s.device_bytes(); break;
+    case PS_INFO_KERNEL_OCTANT: *value = (double)s.Mx * s.oy * s.oz; break;
+    default: return PS_ERR_ARGUMENT;
+    }
+    return PS_OK;
+}
+
+int ps_get_kernel(const ps_solver *h, double *out, long long capacity)
+{
+    if (!out) return PS_ERR_ARGUMENT;
+    return guarded(const_cast<ps_solver *>(h), [&](ps::Solver &s) { s.copy_kernel(out, capacity); });
+}
+
+}  // extern "C"

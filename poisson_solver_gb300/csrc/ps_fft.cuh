@@ -1,0 +1,327 @@
+// Device FFT core: Stockham autosort stages over lines held in shared memory.
+//
+// A CTA owns B "lines" (independent transforms of length L). Thread
+// tid = t * B + b works on line b; the TPL threads of a line split each
+// stage's L/R butterflies between them. Every stage reads its butterfly
+// inputs into registers, synchronises, and writes the outputs back in
+// place, so one shared buffer per line suffices (prime radices above 7 use a
+// second, scratch buffer). The shared address of element n of line b is
+// n * sn + b * sb: strided passes use sn = B, sb = 1 (a row of B adjacent
+// columns, 128 bytes for the default B); the contiguous x pass uses sn = 1,
+// sb = L + 1 (padded rows, so the B lines of one n fall in distinct banks).
+//
+// Stage s with radix R and sub-transform size m (the product of the radices
+// before it) is the radix-R Stockham step: butterfly q*m + j reads
+// x[q*m + j + r*L/R], multiplies by w_{mR}^{r j}, applies the R-point DFT and
+// writes y[(q*R + r)*m + j]. After the last stage the line is in natural
+// order. Forward uses e^{-2 pi i/N}; INV flips every sign.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ps_types.hpp"
+
+namespace ps {
+
+template <typename T> struct CxT;
+template <> struct CxT<double> { using type = double2; };
+template <> struct CxT<float> { using type = float2; };
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b)
+{
+    return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b)
+{
+    return C{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+template <typename C, typename S> __device__ __forceinline__ C cscale(C a, S s) { return C{a.x * s, a.y * s}; }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, typename C> __device__ __forceinline__ C rot(C a)
+{
+    return INV ? C{-a.y, a.x} : C{a.y, -a.x};
+}
+// multiply by w = (c, -s) forward or (c, s) inverse, i.e. e^{-+ i theta}
+template <bool INV, typename C, typename S> __device__ __forceinline__ C crot(C a, S c, S s)
+{
+    return INV ? C{a.x * c - a.y * s, a.x * s + a.y * c} : C{a.x * c + a.y * s, a.y * c - a.x * s};
+}
+
+// ---------------------------------------------------------------------------
+// Small DFTs on register arrays (forward e^{-2 pi i/R}; INV conjugates).
+
+template <bool INV, typename C> __device__ __forceinline__ void dft2(C &a, C &b)
+{
+    C t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft4(C &x0, C &x1, C &x2, C &x3)
+{
+    C t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = rot<INV>(csub(x1, x3));
+    x0 = cadd(t0, t2);
+    x2 = csub(t0, t2);
+    x1 = cadd(t1, t3);
+    x3 = csub(t1, t3);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft8(C *x)
+{
+    using S = decltype(x[0].x);
+    const S h = (S)0.70710678118654752440;
+    dft4<INV>(x[0], x[2], x[4], x[6]);
+    dft4<INV>(x[1], x[3], x[5], x[7]);
+    // twiddles w8^k on the odd half
+    x[3] = crot<INV>(x[3], h, h);
+    x[5] = rot<INV>(x[5]);
+    x[7] = rot<INV>(crot<INV>(x[7], h, h));
+    C y[8];
+    y[0] = cadd(x[0], x[1]); y[4] = csub(x[0], x[1]);
+    y[1] = cadd(x[2], x[3]); y[5] = csub(x[2], x[3]);
+    y[2] = cadd(x[4], x[5]); y[6] = csub(x[4], x[5]);
+    y[3] = cadd(x[6], x[7]); y[7] = csub(x[6], x[7]);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = y[i];
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft16(C *x)
+{
+    using S = decltype(x[0].x);
+    const S c1 = (S)0.92387953251128675613, s1 = (S)0.38268343236508977173;
+    const S h = (S)0.70710678118654752440;
+    // n = 4 n2 + n1: four 4-point DFTs over n2 for each n1
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) dft4<INV>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
+    // x[n1 + 4 k1] now holds A[n1][k1]; multiply by w16^{n1 k1}
+    x[5] = crot<INV>(x[5], c1, s1);                // w^1
+    x[9] = crot<INV>(x[9], h, h);                  // w^2
+    x[13] = crot<INV>(x[13], s1, c1);              // w^3
+    x[6] = crot<INV>(x[6], h, h);                  // w^2
+    x[10] = rot<INV>(x[10]);                       // w^4
+    x[14] = rot<INV>(crot<INV>(x[14], h, h));      // w^6
+    x[7] = crot<INV>(x[7], s1, c1);                // w^3
+    x[11] = rot<INV>(crot<INV>(x[11], h, h));      // w^6
+    x[15] = cscale(crot<INV>(x[15], c1, s1), (S)-1);  // w^9 = -w^1
+    // X[k1 + 4 k2] = DFT4 over n1 of A[n1][k1]
+    C y[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        C a0 = x[4 * k1], a1 = x[4 * k1 + 1], a2 = x[4 * k1 + 2], a3 = x[4 * k1 + 3];
+        dft4<INV>(a0, a1, a2, a3);
+        y[k1] = a0; y[k1 + 4] = a1; y[k1 + 8] = a2; y[k1 + 12] = a3;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = y[i];
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft3(C *x)
+{
+    using S = decltype(x[0].x);
+    const S s3 = (S)0.86602540378443864676;
+    C t1 = cadd(x[1], x[2]), t2 = cscale(csub(x[1], x[2]), s3);
+    C a = C{x[0].x - (S)0.5 * t1.x, x[0].y - (S)0.5 * t1.y};
+    x[0] = cadd(x[0], t1);
+    C r = rot<INV>(t2);
+    x[1] = cadd(a, r);
+    x[2] = csub(a, r);
+}
+
+// Odd prime R with cosines c[k-1] = cos(2 pi k/R), sines s[k-1] = sin(2 pi k/R):
+// y_k = x0 + sum_n c_{nk}(x_n + x_{R-n}) -/+ i sum_n s_{nk}(x_n - x_{R-n}).
+template <bool INV, int R, typename C, typename S>
+__device__ __forceinline__ void dft_odd(C *x, const S *c, const S *s)
+{
+    constexpr int H = (R - 1) / 2;
+    C p[H], q[H];
+#pragma unroll
+    for (int n = 1; n <= H; ++n) {
+        p[n - 1] = cadd(x[n], x[R - n]);
+        q[n - 1] = csub(x[n], x[R - n]);
+    }
+    C y0 = x[0];
+#pragma unroll
+    for (int n = 0; n < H; ++n) y0 = cadd(y0, p[n]);
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+        C a = x[0], b = C{0, 0};
+#pragma unroll
+        for (int n = 1; n <= H; ++n) {
+            const int e = (n * k) % R;  // cos(2 pi e/R), sin(2 pi e/R)
+            const S cc = e <= H ? c[e - 1] : c[R - e - 1];
+            const S ss = e <= H ? s[e - 1] : -s[R - e - 1];
+            a = C{a.x + cc * p[n - 1].x, a.y + cc * p[n - 1].y};
+            b = C{b.x + ss * q[n - 1].x, b.y + ss * q[n - 1].y};
+        }
+        C r = rot<INV>(b);
+        x[k] = cadd(a, r);
+        x[R - k] = csub(a, r);
+    }
+    x[0] = y0;
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft5(C *x)
+{
+    using S = decltype(x[0].x);
+    const S c[2] = {(S)0.30901699437494742410, (S)-0.80901699437494742410};
+    const S s[2] = {(S)0.95105651629515357212, (S)0.58778525229247312917};
+    dft_odd<INV, 5>(x, c, s);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft7(C *x)
+{
+    using S = decltype(x[0].x);
+    const S c[3] = {(S)0.62348980185873353053, (S)-0.22252093395631440429, (S)-0.90096886790241912624};
+    const S s[3] = {(S)0.78183148246802980871, (S)0.97492791218182360702, (S)0.43388373911755812048};
+    dft_odd<INV, 7>(x, c, s);
+}
+
+template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *x)
+{
+    if constexpr (R == 2) dft2<INV>(x[0], x[1]);
+    else if constexpr (R == 3) dft3<INV>(x);
+    else if constexpr (R == 4) dft4<INV>(x[0], x[1], x[2], x[3]);
+    else if constexpr (R == 5) dft5<INV>(x);
+    else if constexpr (R == 7) dft7<INV>(x);
+    else if constexpr (R == 8) dft8<INV>(x);
+    else if constexpr (R == 16) dft16<INV>(x);
+}
+
+// ---------------------------------------------------------------------------
+// Per-stage descriptors, copied from the plan into shared memory at kernel
+// start (indexing the plan's arrays in the kernel parameters at run time
+// would force a local-memory copy of the whole parameter block).
+struct StageInfo {
+    int4 st[MAX_STAGES];  // radix, m, twiddle offset, generic-table offset
+};
+
+__device__ __forceinline__ void load_stages(StageInfo &si, const FftPlanDev &P)
+{
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < MAX_STAGES; ++i) si.st[i] = make_int4(P.radix[i], P.m[i], P.tw[i], P.gw[i]);
+    }
+}
+
+// One in-place Stockham stage with a compile-time radix.
+template <typename C> struct ElemMax { static constexpr int value = sizeof(C) == 16 ? e_max(PREC_FP64) : e_max(PREC_FP32); };
+
+template <int R, bool INV, typename C>
+__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const FftPlanDev &P, int4 sd)
+{
+    constexpr int U = ElemMax<C>::value / R;
+    const int L = P.L, m = sd.y, nbf = L / R, tpl = P.tpl;
+    const C *tw = reinterpret_cast<const C *>(P.table) + sd.z;
+    C v[U][R];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int bf = t + u * tpl;
+        if (bf < nbf) {
+            const int j = bf % m;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[u][r] = S[(bf + r * nbf) * sn + b * sb];
+            if (m > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    const C w = __ldg(&tw[j * (R - 1) + r - 1]);
+                    v[u][r] = INV ? cmulc(v[u][r], w) : cmul(v[u][r], w);
+                }
+            }
+            dft<R, INV>(v[u]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int bf = t + u * tpl;
+        if (bf < nbf) {
+            const int j = bf % m, q = bf / m;
+            const int base = q * R * m + j;
+#pragma unroll
+            for (int r = 0; r < R; ++r) S[(base + r * m) * sn + b * sb] = v[u][r];
+        }
+    }
+    __syncthreads();
+}
+
+// A stage with a prime radix above 7: out of place into W, then copied back.
+template <bool INV, typename C>
+__device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, int4 sd)
+{
+    const int L = P.L, R = sd.x, m = sd.y, nbf = L / R, tpl = P.tpl;
+    const C *tw = reinterpret_cast<const C *>(P.table) + sd.z;
+    const C *gw = reinterpret_cast<const C *>(P.table) + sd.w;
+    for (int bf = t; bf < nbf; bf += tpl) {
+        const int j = bf % m, q = bf / m;
+        const int base = q * R * m + j;
+        for (int k = 0; k < R; ++k) {
+            C acc = C{0, 0};
+            for (int r = 0; r < R; ++r) {
+                C x = S[(bf + r * nbf) * sn + b * sb];
+                if (m > 1 && r > 0) {
+                    const C w = __ldg(&tw[j * (R - 1) + r - 1]);
+                    x = INV ? cmulc(x, w) : cmul(x, w);
+                }
+                const C g = __ldg(&gw[(r * k) % R]);
+                acc = cadd(acc, INV ? cmulc(x, g) : cmul(x, g));
+            }
+            W[(base + k * m) * sn + b * sb] = acc;
+        }
+    }
+    __syncthreads();
+    for (int bf = t; bf < nbf; bf += tpl) {
+        const int j = bf % m, q = bf / m;
+        const int base = q * R * m + j;
+        for (int k = 0; k < R; ++k) S[(base + k * m) * sn + b * sb] = W[(base + k * m) * sn + b * sb];
+    }
+    __syncthreads();
+}
+
+// Full transform of the CTA's lines. Threads with t >= tpl (never the case
+// with the launch shapes used) would idle through the barriers.
+// Full transform of the CTA's lines, for ncomp line sets cstride elements
+// apart. The plan orders its stages as prime radices above 7, then 7s, 5s,
+// 3s, 16s (FP32 only), 8s, and at most one 4 or 2; each radix runs in its own
+// loop, with the line sets innermost, so that the register arrays of
+// different radices never share a live range (a radix switch inside one
+// stage loop, or the stage loops inside a component loop, made the register
+// allocator keep them all live and spill).
+template <bool INV, typename C>
+__device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+                                          const StageInfo &si, int ncomp = 1, int cstride = 0)
+{
+    const int ns = P.nstages;
+    int s = 0;
+    for (; s < ns && si.st[s].x > 16; ++s)
+        for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, si.st[s]);
+    for (; s < ns && si.st[s].x == 7; ++s)
+        for (int c = 0; c < ncomp; ++c) stage<7, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+    for (; s < ns && si.st[s].x == 5; ++s)
+        for (int c = 0; c < ncomp; ++c) stage<5, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+    for (; s < ns && si.st[s].x == 3; ++s)
+        for (int c = 0; c < ncomp; ++c) stage<3, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+    if constexpr (ElemMax<C>::value >= 16)
+        for (; s < ns && si.st[s].x == 16; ++s)
+            for (int c = 0; c < ncomp; ++c) stage<16, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+    for (; s < ns && si.st[s].x == 8; ++s)
+        for (int c = 0; c < ncomp; ++c) stage<8, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+    if (s < ns && si.st[s].x == 4) {
+        for (int c = 0; c < ncomp; ++c) stage<4, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        ++s;
+    }
+    if (s < ns && si.st[s].x == 2) {
+        for (int c = 0; c < ncomp; ++c) stage<2, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        ++s;
+    }
+}
+
+// Component c of a three-entry parameter array, read with constant indices.
+template <typename T> __device__ __forceinline__ T pick3(const T (&a)[3], int c)
+{
+    return c == 0 ? a[0] : (c == 1 ? a[1] : a[2]);
+}
+
+}  // namespace ps

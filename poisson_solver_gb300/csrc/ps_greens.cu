@@ -1,0 +1,310 @@
+// Green's-kernel construction on the GPU, all in FP64. The solver samples the
+// real-space kernel of the domain on one octant of the padded grid (the
+// kernel is even in every axis), transforms it with the same pass kernels as
+// the solve, and folds the regularisation filter and the inverse-transform
+// normalisation into one real octant K = G zeta / (Px Py Pz).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "ps_types.hpp"
+
+namespace ps {
+
+namespace {
+
+constexpr double PI = 3.1415926535897932;
+constexpr double EULER_GAMMA = 0.5772156649015329;
+
+struct cd { double x, y; };
+__device__ __forceinline__ cd cd_add(cd a, cd b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cd cd_mul(cd a, cd b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+// complex quotient by Smith's method
+__device__ __forceinline__ cd cd_div(cd a, cd b)
+{
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double r = b.y / b.x, den = b.x + b.y * r;
+        return {(a.x + a.y * r) / den, (a.y - a.x * r) / den};
+    }
+    const double r = b.x / b.y, den = b.x * r + b.y;
+    return {(a.x * r + a.y) / den, (a.y * r - a.x) / den};
+}
+
+// Sine integral by the method of Numerical Recipes' cisi (Press et al., 2nd
+// ed.): modified-Lentz continued fraction of E1(it) for t > 2, interleaved
+// Si/Ci power series below, both stopped at relative change 1e-10 (the
+// tolerance and switch point of the reference, special_functions.cpp:238-352,
+// so the kernel carries the same truncation).
+__device__ double sine_int(double x)
+{
+    const double eps = 1.0e-10, fpmin = 1.0e-30, fpmax = 1.0e30, tmin = 2.0;
+    const int maxit = 1000;
+    const double t = fabs(x);
+    double ans;
+    if (t == 0.0) return 0.0;
+    if (t > tmin) {
+        cd b = {1.0, t}, c = {fpmax, 0.0};
+        cd d = cd_div({1.0, 0.0}, b), h = d;
+        double err = 1.0;
+        for (int i = 2; i < maxit && err > eps; ++i) {
+            const double a = -(double)(i - 1) * (double)(i - 1);
+            b.x += 2.0;
+            d = cd_div({1.0, 0.0}, cd_add({a * d.x, a * d.y}, b));
+            c = cd_add(b, cd_div({a, 0.0}, c));
+            const cd del = cd_mul(c, d);
+            h = cd_mul(h, del);
+            err = fabs(del.x - 1.0) + fabs(del.y);
+        }
+        double s, co;
+        sincos(t, &s, &co);
+        h = cd_mul({co, -s}, h);
+        ans = 0.5 * PI + h.y;
+    } else {
+        double sums = 0.0;
+        if (t < sqrt(fpmin)) {
+            sums = t;
+        } else {
+            double sum = 0.0, sumc = 0.0, sign = 1.0, fact = 1.0, err = 1.0;
+            bool odd = true;
+            for (int k = 1; k <= maxit && err > eps; ++k) {
+                fact = fact * t / k;
+                const double term = fact / k;
+                sum = sum + sign * term;
+                err = term / fabs(sum);
+                if (odd) { sign = -sign; sums = sum; sum = sumc; }
+                else { sumc = sum; sum = sums; }
+                odd = !odd;
+            }
+        }
+        ans = sums;
+    }
+    return x < 0.0 ? -ans : ans;
+}
+
+// Integral of (1 - J0(t))/t over [0, x]: Chebyshev expansions of Y. L. Luke,
+// "Mathematical functions and their approximations" (1975), Table 9.3 -- an
+// even series in T_2n(x/8) below 8 and a complex series in T_n(10/x - 1)
+// times the asymptotic phase above (the form special_functions.cpp:115-229
+// evaluates). The coefficients are Luke's published values.
+__constant__ double c_luke_small[18] = {
+    1.35105091918187636388,  0.83791030734868376979, -0.35047963978529462711,
+    0.12777415867753198659, -0.02981035698255560990,  0.00455219841169387328,
+   -0.00048408621967185359,  0.00003780202859916883, -0.00000225886908506771,
+    0.00000010664609068423, -0.00000000408005443149,  0.00000000012909996251,
+   -0.00000000000343577839,  0.00000000000007799552, -0.00000000000000152842,
+    0.00000000000000002612, -0.00000000000000000039,  0.00000000000000000001};
+__constant__ double c_luke_large[39][2] = {
+    { 0.95360150809738558095, -0.13917925930200001236}, {-0.05860838853872331670, -0.12902065726135067062},
+    {-0.01020283575659856676,  0.01103004348109535741}, { 0.00196012704043622581,  0.00051817180856880364},
+    {-0.00009574977697756219, -0.00030928210173975681}, {-0.00003570479477043714,  0.00004647098443047525},
+    { 0.00001169677960430223, -0.00000008198845340928}, {-0.00000164386246452682, -0.00000191888381006925},
+    {-0.00000007415845751760,  0.00000057813667761104}, { 0.00000011434387527717, -0.00000008448997773317},
+    {-0.00000003600903214141, -0.00000000525612161520}, { 0.00000000601257386446,  0.00000000763257790924},
+    { 0.00000000019124656215, -0.00000000268643963177}, {-0.00000000054892028385,  0.00000000054279949860},
+    { 0.00000000022740445656, -0.00000000001744365343}, {-0.00000000005671490865, -0.00000000003975692920},
+    { 0.00000000000607510983,  0.00000000002069683990}, { 0.00000000000252060520, -0.00000000000639623674},
+    {-0.00000000000191255246,  0.00000000000116359235}, { 0.00000000000074056501,  0.00000000000006759603},
+    {-0.00000000000018950214, -0.00000000000016557337}, { 0.00000000000002021389,  0.00000000000008425597},
+    { 0.00000000000001103617, -0.00000000000002824474}, {-0.00000000000000889993,  0.00000000000000607698},
+    { 0.00000000000000388558, -0.00000000000000003171}, {-0.00000000000000119200, -0.00000000000000077237},
+    { 0.00000000000000021456,  0.00000000000000048022}, { 0.00000000000000002915, -0.00000000000000019502},
+    {-0.00000000000000004877,  0.00000000000000005671}, { 0.00000000000000002737, -0.00000000000000000862},
+    {-0.00000000000000001080, -0.00000000000000000269}, { 0.00000000000000000308,  0.00000000000000000309},
+    {-0.00000000000000000042, -0.00000000000000000167}, {-0.00000000000000000020,  0.00000000000000000066},
+    { 0.00000000000000000020, -0.00000000000000000019}, {-0.00000000000000000011,  0.00000000000000000003},
+    { 0.00000000000000000004,  0.00000000000000000001}, {-0.00000000000000000001, -0.00000000000000000001},
+    { 0.00000000000000000000,  0.00000000000000000001}};
+
+__device__ double bessel_int_j0(double x)
+{
+    if (x < 8.0) {
+        const double x8 = 0.125 * x;
+        double t0 = 1.0, t1 = x8, ans = c_luke_small[0];
+        for (int i = 2; i < 36; ++i) {
+            const double t2 = 2.0 * x8 * t1 - t0;
+            if ((i & 1) == 0) ans += c_luke_small[i / 2] * t2;
+            t0 = t1;
+            t1 = t2;
+        }
+        return ans;
+    }
+    const double u = 10.0 / x - 1.0;
+    double t0 = 1.0, t1 = u;
+    double sr = c_luke_large[0][0] + c_luke_large[1][0] * t1;
+    double si = c_luke_large[0][1] + c_luke_large[1][1] * t1;
+    for (int i = 2; i < 39; ++i) {
+        const double t2 = 2.0 * u * t1 - t0;
+        t0 = t1;
+        t1 = t2;
+        sr += c_luke_large[i][0] * t2;
+        si += c_luke_large[i][1] * t2;
+    }
+    const double ph = x + 0.25 * PI;
+    const double fac = cos(ph) * sr - sin(ph) * si;
+    return sqrt(2.0 / (PI * x)) / x * fac + EULER_GAMMA + log(0.5 * x);
+}
+
+// 3D unbounded kernel, spectrally truncated: G(r) = Si(r/sigma)/(2 pi^2 r) dV,
+// sigma = h/pi, h = max dx; 1/(2 pi^2 sigma) dV at the origin
+// (greens3d.cpp:193-225). Octant index i' is the half-swapped grid index, so
+// the sample sits at x = -(P/2) dx + (i' + P/2) dx as the reference forms it.
+__global__ void k_sample_unbounded3d(double *oct, int ox, int oy, int oz, int P0, int P1, int P2,
+                                     double dx0, double dx1, double dx2)
+{
+    const long long n = (long long)ox * oy * oz;
+    const double h = fmax(fmax(dx0, dx1), dx2);
+    const double sigma = h / PI;
+    const double c = 0.5 / (PI * PI);
+    const double xmin0 = -(0.5 * (double)P0) * dx0, xmin1 = -(0.5 * (double)P1) * dx1,
+                 xmin2 = -(0.5 * (double)P2) * dx2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % ox), j = (int)((q / ox) % oy), k = (int)(q / ((long long)ox * oy));
+        const double x = xmin0 + (double)(i + P0 / 2) * dx0;
+        const double y = xmin1 + (double)(j + P1 / 2) * dx1;
+        const double z = xmin2 + (double)(k + P2 / 2) * dx2;
+        const double r = sqrt(x * x + y * y + z * z);
+        double g;
+        if (r > 0.25 * dx0) g = c * sine_int(r / sigma) / r * dx0 * dx1 * dx2;
+        else g = c / sigma * dx0 * dx1 * dx2;
+        oct[q] = g;
+    }
+}
+
+// 2D unbounded kernel -(1/2 pi)(Ji0(r/sigma) + ln(2 sigma) - gamma) dx dy,
+// sigma = max(dx, dy)/pi (greens2d.cpp:157-202).
+__global__ void k_sample_unbounded2d(double *oct, int ox, int oy, int P0, int P1, double dx0, double dx1)
+{
+    const long long n = (long long)ox * oy;
+    const double sigma = fmax(dx0, dx1) / PI;
+    const double C2 = log(2.0 * sigma) - EULER_GAMMA;
+    const double c = 0.5 / PI;
+    const double xmin0 = -(0.5 * (double)P0) * dx0, xmin1 = -(0.5 * (double)P1) * dx1;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % ox), j = (int)(q / ox);
+        const double x = xmin0 + (double)(i + P0 / 2) * dx0;
+        const double y = xmin1 + (double)(j + P1 / 2) * dx1;
+        const double r = sqrt(x * x + y * y);
+        oct[q] = -c * (bessel_int_j0(r / sigma) + C2) * dx0 * dx1;
+    }
+}
+
+// Spectrum of the 1D free-space kernel of the periodic-periodic-unbounded
+// domain, -(sigma/pi)(rho Si(rho) + cos rho) dz with rho = |z|/sigma,
+// sigma = dz/pi (greens3d.cpp:361-373), sampled at z = -(Pz/2) dz + k dz and
+// half-swapped. The samples are even, so the transform is the real cosine sum
+// G1[k] = g0 + (-1)^k g_{P/2} + 2 sum_{0<m<P/2} g_m cos(2 pi k m / P).
+__global__ void k_line_ppf(double *line, int P, double dz)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > P / 2) return;
+    const double sigma = dz / PI, C1 = sigma / PI;
+    const double zmin = -(0.5 * (double)P) * dz;
+    auto g = [&](int m) {
+        const double z = zmin + (double)(m + P / 2) * dz;
+        const double rho = fabs(z) / sigma;
+        return -C1 * (sine_int(rho) * rho + cos(rho)) * dz;
+    };
+    double acc = g(0) + ((k & 1) ? -1.0 : 1.0) * g(P / 2);
+    for (int m = 1; m < P / 2; ++m) {
+        const long long e = ((long long)k * m) % P;
+        acc += 2.0 * g(m) * cospi(2.0 * (double)e / (double)P);
+    }
+    line[k] = acc;
+}
+
+__device__ __forceinline__ double wn(int m, int P, double dx)
+{
+    // signed wavenumber as greens3d.cpp:78-118 forms it: 2 pi m / (P dx), m wrapped at P/2
+    const int mm = (2 * m < P) ? m : m - P;
+    const double dk = 1.0 / ((double)P * dx);
+    return 2.0 * PI * (double)mm * dk;
+}
+
+__global__ void k_kernel_fill(const KernelFillArgs a)
+{
+    const long long n = (long long)a.Mx * a.oy * a.oz;
+    const double h = fmax(fmax(a.dx[0], a.dx[1]), a.dx[2]);
+    const double sigma = 2.0 * h;
+    const int r = (a.reg % 2 != 0) ? a.reg + 1 : a.reg;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int kx = (int)(q % a.Mx), ky = (int)((q / a.Mx) % a.oy), kz = (int)(q / ((long long)a.Mx * a.oy));
+        const double fx = wn(kx, a.P[0], a.dx[0]), fy = wn(ky, a.P[1], a.dx[1]), fz = wn(kz, a.P[2], a.dx[2]);
+        const double k2 = fx * fx + fy * fy + fz * fz;
+        double g = 0.0;
+        if (a.kern) {
+            switch (a.kind) {
+            case 0: g = a.spec[((long long)kz * a.P[1] + ky) * a.Mx + kx].x; break;
+            case 1: g = (kx == 0 && ky == 0) ? a.line[kz] : 1.0 / k2; break;
+            case 2: g = (kz == 0) ? a.plane[(long long)ky * a.Mx + kx].x : 1.0 / k2; break;
+            default: g = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : 1.0 / k2; break;
+            }
+        }
+        // zeta = e^{-a} sum_{n < r/2} a^n / n!, a = sigma^2 |k|^2 / 2 (greens3d.cpp:123-159)
+        double zeta = 1.0;
+        if (a.reg > 0) {
+            const double arg = 0.5 * sigma * sigma * k2;
+            double c = 1.0, p = 1.0, sum = 1.0;
+            for (int m = 1; m <= r / 2 - 1; ++m) {
+                c = c * 1.0 / (double)m;
+                p = p * arg;
+                sum += c * p;
+            }
+            zeta = sum * exp(-arg);
+        }
+        if (a.kern) a.kern[q] = g * zeta / a.norm;
+        if (a.zeta_out) a.zeta_out[q] = zeta / a.norm;
+    }
+}
+
+__global__ void k_to_fp32(const double *in, float *out, size_t n)
+{
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        out[q] = (float)in[q];
+}
+
+unsigned grid_for(long long n, int threads)
+{
+    long long g = (n + threads - 1) / threads;
+    if (g > 152LL * 64) g = 152LL * 64;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+cudaError_t launch_sample_unbounded3d(double *oct, const int oext[3], const int P[3], const double dx[3],
+                                      cudaStream_t st)
+{
+    const long long n = (long long)oext[0] * oext[1] * oext[2];
+    k_sample_unbounded3d<<<grid_for(n, 256), 256, 0, st>>>(oct, oext[0], oext[1], oext[2], P[0], P[1], P[2], dx[0],
+                                                             dx[1], dx[2]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sample_unbounded2d(double *oct, const int oext[2], const int P[2], const double dx[2],
+                                      cudaStream_t st)
+{
+    const long long n = (long long)oext[0] * oext[1];
+    k_sample_unbounded2d<<<grid_for(n, 256), 256, 0, st>>>(oct, oext[0], oext[1], P[0], P[1], dx[0], dx[1]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_line_ppf(double *line, int P, double dz, cudaStream_t st)
+{
+    const int n = P / 2 + 1;
+    k_line_ppf<<<(n + 127) / 128, 128, 0, st>>>(line, P, dz);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st)
+{
+    const long long n = (long long)a.Mx * a.oy * a.oz;
+    k_kernel_fill<<<grid_for(n, 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t st)
+{
+    k_to_fp32<<<grid_for((long long)n, 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace ps

@@ -1,0 +1,404 @@
+// Pass kernels of the 3D solve: x forward (real-to-half-spectrum, zero-pad
+// fused), y column transforms, the fused z pass (forward, spectral kernel and
+// derivative operator, inverse), and x inverse (half-spectrum-to-real, crop
+// fused). Each CTA stages its lines in shared memory and runs the Stockham
+// stages of ps_fft.cuh on them; global traffic is coalesced along x.
+#include <cuda_runtime.h>
+
+#include "ps_fft.cuh"
+#include "ps_types.hpp"
+
+namespace ps {
+
+namespace {
+
+template <typename T> struct Cplx { using type = typename CxT<T>::type; };
+
+__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// x forward. Line l of the CTA carries rows 2l (real part) and 2l+1 (imag
+// part); after the complex transform Z the two half spectra are
+// Xa[k] = (Z[k] + conj Z[L-k]) / 2 and Xb[k] = (Z[k] - conj Z[L-k]) / 2i.
+template <typename T>
+__global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+{
+    using C = typename Cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, L = a.L, ld = L + 1;
+    C *W = a.plan.generic ? S + B * ld : nullptr;
+    __shared__ StageInfo si;
+    load_stages(si, a.plan);
+    const int comp = blockIdx.y;
+    const double *in = pick3(a.in, comp);
+    C *out = reinterpret_cast<C *>(pick3(a.out, comp));
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long row0 = (long long)blockIdx.x * 2 * B;
+
+    // load (zero-fill n >= n_in and rows past the end)
+    T *Sr = reinterpret_cast<T *>(S);
+    for (int idx = tid; idx < 2 * B * L; idx += nt) {
+        const int rl = idx / L, n = idx - rl * L;
+        const long long r = row0 + rl;
+        double v = 0.0;
+        if (n < a.n_in && r < rows) {
+            if (!a.mirror) {
+                v = in[r * a.in_stride + n];
+            } else {
+                const int j = (int)(r % a.rows_y), k = (int)(r / a.rows_y);
+                const int jj = imin(j, a.Py - j), kk = imin(k, a.Pz - k), nn = imin(n, L - n);
+                v = in[((long long)kk * a.oct_y + jj) * a.oct_x + nn];
+            }
+        }
+        Sr[2 * ((rl >> 1) * ld + n) + (rl & 1)] = (T)v;
+    }
+    __syncthreads();
+    fft_lines<false>(S, W, 1, ld, tid % B, tid / B, a.plan, si);
+
+    // separate the two half spectra and store
+    const int Mx = a.Mx;
+    for (int idx = tid; idx < B * Mx; idx += nt) {
+        const int line = idx / Mx, k = idx - line * Mx;
+        const long long ra = row0 + 2 * line, rb = ra + 1;
+        if (ra >= rows) continue;
+        const C z = S[line * ld + k], w = S[line * ld + (k == 0 ? 0 : L - k)];
+        const T h = (T)0.5;
+        const C xa = C{h * (z.x + w.x), h * (z.y - w.y)};
+        const C xb = C{h * (z.y + w.y), h * (w.x - z.x)};
+        {
+            const long long j = ra % a.rows_y, kz = ra / a.rows_y;
+            out[(kz * a.out_y + j) * Mx + k] = xa;
+        }
+        if (rb < rows) {
+            const long long j = rb % a.rows_y, kz = rb / a.rows_y;
+            out[(kz * a.out_y + j) * Mx + k] = xb;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Column transforms along a strided axis, in place: the CTA takes B adjacent
+// columns (one 128-byte row segment per sample for the default B) of one slab.
+template <typename T, bool INV>
+__global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
+{
+    using C = typename Cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, L = a.L;
+    C *W = a.plan.generic ? S + L * B : nullptr;
+    const int lb = __ffs(B) - 1;
+    __shared__ StageInfo si;
+    load_stages(si, a.plan);
+    const int comp = blockIdx.z;
+    const int x0 = blockIdx.x * B;
+    const int nb = imin(B, a.Mx - x0);
+    C *base = reinterpret_cast<C *>(pick3(a.data, comp)) + (long long)blockIdx.y * a.outer_stride + x0;
+    const int nt = blockDim.x, tid = threadIdx.x;
+
+    for (int idx = tid; idx < L * B; idx += nt) {
+        const int n = idx >> lb, b = idx & (B - 1);
+        C v = C{0, 0};
+        if (n < a.n_in && b < nb) v = base[n * a.axis_stride + b];
+        S[idx] = v;
+    }
+    __syncthreads();
+    fft_lines<INV>(S, W, B, 1, tid & (B - 1), tid >> lb, a.plan, si);
+    for (int idx = tid; idx < a.n_out * B; idx += nt) {
+        const int n = idx >> lb, b = idx & (B - 1);
+        if (b < nb) base[n * a.axis_stride + b] = S[idx];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused z pass.
+template <typename T>
+__device__ __forceinline__ T wavenumber(int k, int P, double c, bool derivative)
+{
+    // k in [0, P): signed index wrapped at P/2; the derivative drops the
+    // unpaired Nyquist mode (its Hermitian part vanishes in the real output).
+    const int m = (2 * k < P) ? k : k - P;
+    if (derivative && 2 * k == P) return (T)0;
+    return (T)((double)m * c);
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
+{
+    using C = typename Cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, L = a.L, LB = L * B;
+    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
+    C *W = a.plan.generic ? S + nbuf * LB : nullptr;
+    const int lb = __ffs(B) - 1;
+    const int x0 = blockIdx.x * B;
+    const int ky = a.ky0 + blockIdx.y;
+    const int nb = imin(B, a.Mx - x0);
+    const long long off = (long long)ky * a.row_stride + x0;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const int b = tid & (B - 1), t = tid >> lb;
+    __shared__ StageInfo si;
+    load_stages(si, a.plan);
+
+    for (int c = 0; c < a.nin; ++c) {
+        const C *src = reinterpret_cast<const C *>(pick3(a.in, c)) + off;
+        C *buf = S + c * LB;
+        for (int idx = tid; idx < LB; idx += nt) {
+            const int n = idx >> lb, bb = idx & (B - 1);
+            C v = C{0, 0};
+            if (n < a.n_in && bb < nb) v = src[n * a.axis_stride + bb];
+            buf[idx] = v;
+        }
+    }
+    __syncthreads();
+    fft_lines<false>(S, W, B, 1, b, t, a.plan, si, a.nin, LB);
+
+    if constexpr (OP != OP_FORWARD) {
+        const T *K = reinterpret_cast<const T *>(a.kern);
+        const int oy = imin(ky, a.Py - ky);
+        const T kyv = wavenumber<T>(ky, a.Py, a.kyc, true);
+        for (int idx = tid; idx < LB; idx += nt) {
+            const int n = idx >> lb, bb = idx & (B - 1);
+            const int kx = x0 + bb;
+            if (bb >= nb) continue;
+            const int oz = imin(n, a.Pz - n);
+            const T g = K[((long long)oz * a.oct_y + oy) * a.Mx + kx];
+            const T kxv = wavenumber<T>(kx, a.Px, a.kxc, true);
+            const T kzv = wavenumber<T>(n, a.Pz, a.kzc, true);
+            if constexpr (OP == OP_NONE) {
+                for (int c = 0; c < a.nin; ++c) S[c * LB + idx] = cscale(S[c * LB + idx], g);
+            } else if constexpr (OP == OP_GRAD) {
+                // out_d = i k_d K in_d; in_d falls back to component x
+                const C i0 = S[idx];
+                const C i1 = a.nin > 1 ? S[LB + idx] : i0;
+                const C i2 = a.nin > 2 ? S[2 * LB + idx] : i0;
+                const T gx = g * kxv, gy = g * kyv, gz = g * kzv;
+                S[idx] = C{-gx * i0.y, gx * i0.x};
+                S[LB + idx] = C{-gy * i1.y, gy * i1.x};
+                S[2 * LB + idx] = C{-gz * i2.y, gz * i2.x};
+            } else if constexpr (OP == OP_DIV) {
+                const C i0 = S[idx], i1 = S[LB + idx], i2 = S[2 * LB + idx];
+                const C s = C{kxv * i0.x + kyv * i1.x + kzv * i2.x, kxv * i0.y + kyv * i1.y + kzv * i2.y};
+                S[idx] = C{-g * s.y, g * s.x};
+            } else if constexpr (OP == OP_CURL) {
+                const C i0 = S[idx], i1 = S[LB + idx], i2 = S[2 * LB + idx];
+                const C c0 = C{kyv * i2.x - kzv * i1.x, kyv * i2.y - kzv * i1.y};
+                const C c1 = C{kzv * i0.x - kxv * i2.x, kzv * i0.y - kxv * i2.y};
+                const C c2 = C{kxv * i1.x - kyv * i0.x, kxv * i1.y - kyv * i0.y};
+                S[idx] = C{-g * c0.y, g * c0.x};
+                S[LB + idx] = C{-g * c1.y, g * c1.x};
+                S[2 * LB + idx] = C{-g * c2.y, g * c2.x};
+            } else if constexpr (OP == OP_FILTER) {
+                const T *Z = reinterpret_cast<const T *>(a.zeta);
+                const T z = Z[((long long)oz * a.oct_y + oy) * a.Mx + kx];
+                if (a.reproject && a.nin == 3) {
+                    // r'_c = z r_c - K sum_d k_c k_d r_d. A product k_c k_d is
+                    // even under k -> -k (and survives in the real output)
+                    // unless exactly one of the two axes sits on its Nyquist
+                    // mode, where the unpaired wavenumber makes it odd.
+                    const T kf[3] = {wavenumber<T>(kx, a.Px, a.kxc, false), wavenumber<T>(ky, a.Py, a.kyc, false),
+                                     wavenumber<T>(n, a.Pz, a.kzc, false)};
+                    const bool nq[3] = {2 * kx == a.Px, 2 * ky == a.Py, 2 * n == a.Pz};
+                    const C in3[3] = {S[idx], S[LB + idx], S[2 * LB + idx]};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        C acc = C{0, 0};
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            const T kk = nq[c] == nq[d] ? kf[c] * kf[d] : (T)0;
+                            acc.x += kk * in3[d].x;
+                            acc.y += kk * in3[d].y;
+                        }
+                        S[c * LB + idx] = C{z * in3[c].x - g * acc.x, z * in3[c].y - g * acc.y};
+                    }
+                } else {
+                    for (int c = 0; c < a.nin; ++c) S[c * LB + idx] = cscale(S[c * LB + idx], z);
+                }
+            }
+        }
+        __syncthreads();
+        fft_lines<true>(S, W, B, 1, b, t, a.plan, si, a.nout, LB);
+    }
+
+    for (int c = 0; c < a.nout; ++c) {
+        C *dst0 = reinterpret_cast<C *>(pick3(a.out, c));
+        if (dst0 == nullptr) continue;
+        C *dst = dst0 + off;
+        const C *buf = S + c * LB;
+        for (int idx = tid; idx < a.n_out * B; idx += nt) {
+            const int n = idx >> lb, bb = idx & (B - 1);
+            if (bb < nb) dst[n * a.axis_stride + bb] = buf[idx];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// x inverse. Line l rebuilds Z = Xa + i Xb over the full length from the two
+// half spectra (Z[L-k] = conj Xa[k] + i conj Xb[k]), transforms back and
+// writes Re -> row 2l, Im -> row 2l+1, first n_out samples only.
+template <typename T>
+__global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+{
+    using C = typename Cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, L = a.L, ld = L + 1, Mx = a.Mx;
+    C *W = a.plan.generic ? S + B * ld : nullptr;
+    __shared__ StageInfo si;
+    load_stages(si, a.plan);
+    const int comp = blockIdx.y;
+    const C *in = reinterpret_cast<const C *>(pick3(a.in, comp));
+    double *out = pick3(a.out, comp);
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long row0 = (long long)blockIdx.x * 2 * B;
+
+    for (int idx = tid; idx < B * Mx; idx += nt) {
+        const int line = idx / Mx, k = idx - line * Mx;
+        const long long ra = row0 + 2 * line, rb = ra + 1;
+        C xa = C{0, 0}, xb = C{0, 0};
+        if (ra < rows) xa = in[((ra / a.rows_y) * a.in_y + ra % a.rows_y) * Mx + k];
+        if (rb < rows) xb = in[((rb / a.rows_y) * a.in_y + rb % a.rows_y) * Mx + k];
+        S[line * ld + k] = C{xa.x - xb.y, xa.y + xb.x};
+        if (k >= 1 && k <= L - Mx) S[line * ld + L - k] = C{xa.x + xb.y, xb.x - xa.y};
+    }
+    __syncthreads();
+    fft_lines<true>(S, W, 1, ld, tid % B, tid / B, a.plan, si);
+
+    const T *Sr = reinterpret_cast<const T *>(S);
+    const int no = a.n_out;
+    for (int idx = tid; idx < 2 * B * no; idx += nt) {
+        const int rl = idx / no, n = idx - rl * no;
+        const long long r = row0 + rl;
+        if (r < rows) out[r * a.out_stride + n] = (double)Sr[2 * ((rl >> 1) * ld + n) + (rl & 1)];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+static int threads_for(const FftPlanDev &p, int B) { return B * p.tpl; }
+
+size_t smem_x(int prec, int L, int B, int generic)
+{
+    const size_t c = prec == PREC_FP64 ? 16 : 8;
+    return c * (size_t)B * (L + 1) * (generic ? 2 : 1);
+}
+size_t smem_col(int prec, int L, int B, int generic)
+{
+    const size_t c = prec == PREC_FP64 ? 16 : 8;
+    return c * (size_t)B * L * (generic ? 2 : 1);
+}
+size_t smem_z(int prec, int L, int B, int nbuf, int generic)
+{
+    const size_t c = prec == PREC_FP64 ? 16 : 8;
+    return c * (size_t)B * L * (nbuf + (generic ? 1 : 0));
+}
+
+int max_smem_per_block()
+{
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+template <typename K> static cudaError_t prep(K kernel, size_t smem)
+{
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st)
+{
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long lines = (rows + 1) / 2;
+    dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
+    const int nt = threads_for(a.plan, a.B);
+    const size_t sm = smem_x(prec, a.L, a.B, a.plan.generic);
+    cudaError_t e;
+    if (prec == PREC_FP64) {
+        if ((e = prep(k_xfwd<double>, sm)) != cudaSuccess) return e;
+        k_xfwd<double><<<grid, nt, sm, st>>>(a);
+    } else {
+        if ((e = prep(k_xfwd<float>, sm)) != cudaSuccess) return e;
+        k_xfwd<float><<<grid, nt, sm, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaStream_t st)
+{
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), outer, a.ncomp);
+    const int nt = threads_for(a.plan, a.B);
+    const size_t sm = smem_col(prec, a.L, a.B, a.plan.generic);
+    cudaError_t e;
+#define PS_LAUNCH_COL(T, I)                                         \
+    do {                                                            \
+        if ((e = prep(k_col<T, I>, sm)) != cudaSuccess) return e;   \
+        k_col<T, I><<<grid, nt, sm, st>>>(a);                       \
+    } while (0)
+    if (prec == PREC_FP64) {
+        if (inverse) PS_LAUNCH_COL(double, true); else PS_LAUNCH_COL(double, false);
+    } else {
+        if (inverse) PS_LAUNCH_COL(float, true); else PS_LAUNCH_COL(float, false);
+    }
+#undef PS_LAUNCH_COL
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t launch_z_t(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    cudaError_t e;
+#define PS_LAUNCH_Z(OPV)                                               \
+    case OPV:                                                          \
+        if ((e = prep(k_z<T, OPV>, sm)) != cudaSuccess) return e;      \
+        k_z<T, OPV><<<grid, nt, sm, st>>>(a);                          \
+        break;
+    switch (a.op) {
+        PS_LAUNCH_Z(OP_NONE)
+        PS_LAUNCH_Z(OP_GRAD)
+        PS_LAUNCH_Z(OP_DIV)
+        PS_LAUNCH_Z(OP_CURL)
+        PS_LAUNCH_Z(OP_FILTER)
+        PS_LAUNCH_Z(OP_FORWARD)
+    default: return cudaErrorInvalidValue;
+    }
+#undef PS_LAUNCH_Z
+    return cudaGetLastError();
+}
+
+cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st)
+{
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), ny);
+    const int nt = threads_for(a.plan, a.B);
+    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
+    const size_t sm = smem_z(prec, a.L, a.B, nbuf, a.plan.generic);
+    return prec == PREC_FP64 ? launch_z_t<double>(a, grid, nt, sm, st) : launch_z_t<float>(a, grid, nt, sm, st);
+}
+
+cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
+{
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long lines = (rows + 1) / 2;
+    dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
+    const int nt = threads_for(a.plan, a.B);
+    const size_t sm = smem_x(prec, a.L, a.B, a.plan.generic);
+    cudaError_t e;
+    if (prec == PREC_FP64) {
+        if ((e = prep(k_xinv<double>, sm)) != cudaSuccess) return e;
+        k_xinv<double><<<grid, nt, sm, st>>>(a);
+    } else {
+        if ((e = prep(k_xinv<float>, sm)) != cudaSuccess) return e;
+        k_xinv<float><<<grid, nt, sm, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ps

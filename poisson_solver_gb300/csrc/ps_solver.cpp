@@ -1,0 +1,624 @@
+// Host orchestration of the 3D solve: transform plans, device buffers, the
+// kernel build and the five-launch pipeline
+//   x forward (R2C, zero-pad) -> y forward -> z (forward, kernel x operator,
+//   inverse) -> y inverse -> x inverse (C2R, crop)
+// that replaces the reference's pencil FFTs and MPI remaps (solve3d.cpp:8-635).
+#include "ps_solver.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <functional>
+#include <vector>
+
+#include "poisson_solver_gb300.h"
+
+namespace ps {
+
+#define PS_CK(expr)                                                                                   \
+    do {                                                                                              \
+        cudaError_t e_ = (expr);                                                                      \
+        if (e_ != cudaSuccess) throw Error(PS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+static constexpr long double PI_L = 3.141592653589793238462643383279502884L;
+
+// ---------------------------------------------------------------------------
+void DevBuf::ensure(size_t n)
+{
+    if (p && n <= bytes) return;
+    release();
+    if (n == 0) return;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        bytes = 0;
+        cudaGetLastError();
+        throw Error(PS_ERR_MEMORY, "device allocation of " + std::to_string(n) + " bytes failed: " +
+                                       cudaGetErrorString(e));
+    }
+    bytes = n;
+}
+
+void DevBuf::release()
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+Solver::Solver() { PS_CK(cudaGetDevice(&device)); }
+
+Solver::~Solver() = default;
+
+// ---------------------------------------------------------------------------
+// Transform plans. Stage order (which fft_lines relies on): primes above 7
+// (direct DFT stages), 7s, 5s, 3s, 16s (FP32 only), 8s, then one 4 or 2.
+static std::vector<int> factorize(int L, int max_radix)
+{
+    std::vector<int> big, small;
+    int x = L;
+    int p2 = 0;
+    while (x % 2 == 0) { x /= 2; ++p2; }
+    std::vector<int> odd;
+    for (int p : {3, 5, 7})
+        while (x % p == 0) { odd.push_back(p); x /= p; }
+    for (int p = 11; (long long)p * p <= x; p += 2)
+        while (x % p == 0) { big.push_back(p); x /= p; }
+    if (x > 1) big.push_back(x);
+    std::vector<int> r(big.begin(), big.end());
+    for (int p : {7, 5, 3})
+        for (int q : odd)
+            if (q == p) r.push_back(p);
+    if (max_radix >= 16)
+        while (p2 >= 4) { r.push_back(16); p2 -= 4; }
+    while (p2 >= 3) { r.push_back(8); p2 -= 3; }
+    if (p2 == 2) r.push_back(4);
+    if (p2 == 1) r.push_back(2);
+    return r;
+}
+
+static bool fixed_radix(int R) { return R == 2 || R == 3 || R == 4 || R == 5 || R == 7 || R == 8 || R == 16; }
+
+// e^{-2 pi i e / N}, from the exactly reduced fraction e/N in extended precision
+static std::complex<long double> root(long long e, long long N)
+{
+    e %= N;
+    const long double a = 2.0L * PI_L * (long double)e / (long double)N;
+    return {cosl(a), -sinl(a)};
+}
+
+const Plan &Solver::plan(int L, int prec)
+{
+    auto key = std::make_pair(L, prec);
+    auto it = plans.find(key);
+    if (it != plans.end()) return *it->second;
+    auto pl = std::make_unique<Plan>();
+    FftPlanDev &d = pl->dev;
+    d.L = L;
+    const int emax = e_max(prec);
+    std::vector<int> rad = L > 1 ? factorize(L, emax) : std::vector<int>{};
+    if ((int)rad.size() > MAX_STAGES) throw Error(PS_ERR_UNSUPPORTED, "transform length has too many factors");
+    d.nstages = (int)rad.size();
+    std::vector<std::complex<long double>> tab;
+    int m = 1, tpl = 1;
+    for (int s = 0; s < d.nstages; ++s) {
+        const int R = rad[s];
+        d.radix[s] = R;
+        d.m[s] = m;
+        d.tw[s] = (int)tab.size();
+        for (int j = 0; j < m; ++j)
+            for (int r = 1; r < R; ++r) tab.push_back(root((long long)j * r, (long long)m * R));
+        const int nbf = L / R;
+        if (fixed_radix(R)) {
+            const int U = emax / R;
+            tpl = std::max(tpl, (nbf + U - 1) / U);
+            d.gw[s] = 0;
+        } else {
+            d.generic = 1;
+            d.gw[s] = (int)tab.size();
+            for (int q = 0; q < R; ++q) tab.push_back(root(q, R));
+            tpl = std::max(tpl, std::min(nbf, 64));
+        }
+        m *= R;
+    }
+    d.tpl = tpl;
+    if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length " + std::to_string(L) + " too large");
+    if (!tab.empty()) {
+        if (prec == PREC_FP64) {
+            std::vector<double2> h(tab.size());
+            for (size_t i = 0; i < tab.size(); ++i) h[i] = make_double2((double)tab[i].real(), (double)tab[i].imag());
+            pl->table.ensure(h.size() * sizeof(double2));
+            PS_CK(cudaMemcpy(pl->table.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float2> h(tab.size());
+            for (size_t i = 0; i < tab.size(); ++i) h[i] = make_float2((float)tab[i].real(), (float)tab[i].imag());
+            pl->table.ensure(h.size() * sizeof(float2));
+            PS_CK(cudaMemcpy(pl->table.p, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
+        }
+    }
+    d.table = pl->table.p;
+    Plan &ref = *pl;
+    plans[key] = std::move(pl);
+    return ref;
+}
+
+// Lines per CTA: the 128-byte row default, halved until threads and shared
+// memory fit.
+static int pick_lines(int prec, int tpl, const std::function<size_t(int)> &smem)
+{
+    static int limit = 0;
+    if (!limit) limit = max_smem_per_block() - 1024;  // room for the static stage table
+    int B = prec == PREC_FP64 ? 8 : 16;
+    while (B > 1 && (B * tpl > MAX_THREADS || smem(B) > (size_t)limit)) B >>= 1;
+    if (B * tpl > MAX_THREADS || smem(B) > (size_t)limit)
+        throw Error(PS_ERR_UNSUPPORTED, "transform length too large for one CTA");
+    return B;
+}
+
+// ---------------------------------------------------------------------------
+void Solver::check_setup() const
+{
+    if (!is_setup) throw Error(PS_ERR_STATE, "setup3d has not been called");
+}
+
+void Solver::setup3d(const int ncell[3], const int bcs[3], const double dxs[3], int reg_order)
+{
+    for (int d = 0; d < 3; ++d) {
+        if (ncell[d] < 1) throw Error(PS_ERR_ARGUMENT, "ncell must be positive");
+        if (!(dxs[d] > 0.0) || !std::isfinite(dxs[d])) throw Error(PS_ERR_ARGUMENT, "dx must be positive and finite");
+        if (bcs[d] != 0 && bcs[d] != 1) throw Error(PS_ERR_BOUNDARY, "boundary condition must be 0 (unbounded) or 1 (periodic)");
+    }
+    if (reg_order < 0) throw Error(PS_ERR_ARGUMENT, "reg_order must be >= 0");
+    const int b0 = bcs[0], b1 = bcs[1], b2 = bcs[2];
+    const bool ok = (b0 == 0 && b1 == 0 && b2 == 0) || (b0 == 1 && b1 == 1 && b2 == 0) ||
+                    (b0 == 0 && b1 == 0 && b2 == 1) || (b0 == 1 && b1 == 1 && b2 == 1);
+    if (!ok) {
+        // the reference's three diagnostics (greens3d.cpp:522-541)
+        const int sum = b0 + b1 + b2;
+        if (sum == 1)
+            throw Error(PS_ERR_BOUNDARY, "for unbounded-unbounded-periodic domains the z-direction must be the periodic direction");
+        if (sum == 2)
+            throw Error(PS_ERR_BOUNDARY, "for unbounded-periodic-periodic domains the z-direction must be the unbounded direction");
+        throw Error(PS_ERR_BOUNDARY, "boundary condition configuration unknown");
+    }
+    for (int d = 0; d < 3; ++d) {
+        const long long p = (bcs[d] == 0 ? 2LL : 1LL) * ncell[d];
+        if (p > 8192) throw Error(PS_ERR_UNSUPPORTED, "padded transform length above 8192");
+    }
+    is_setup = false;
+    for (int d = 0; d < 3; ++d) {
+        n[d] = ncell[d];
+        bc[d] = bcs[d];
+        dx[d] = dxs[d];
+        P[d] = (bcs[d] == 0 ? 2 : 1) * ncell[d];
+    }
+    reg = reg_order;
+    Mx = P[0] / 2 + 1;
+    oy = P[1] / 2 + 1;
+    oz = P[2] / 2 + 1;
+    pushed = produced = rhs_ready = 0;
+    kern32.release();
+    zeta64.release();
+    zeta32.release();
+    for (int c = 0; c < 3; ++c) {
+        work[c].release();
+        fb[c].release();
+        fa[c].release();
+        fr[c].release();
+    }
+    build_kernel();
+    is_setup = true;
+}
+
+void Solver::set_option(int option, int value)
+{
+    switch (option) {
+    case PS_OPT_GRAD: opt_grad = value != 0; break;
+    case PS_OPT_DIV: opt_div = value != 0; break;
+    case PS_OPT_CURL: opt_curl = value != 0; break;
+    case PS_OPT_REPROJECT: opt_reproject = value != 0; rhs_ready = 0; break;
+    case PS_OPT_PRECISION:
+        if (value != PS_PREC_FP64 && value != PS_PREC_FP32) throw Error(PS_ERR_ARGUMENT, "unknown precision");
+        precision = value == PS_PREC_FP64 ? PREC_FP64 : PREC_FP32;
+        rhs_ready = 0;
+        break;
+    default: throw Error(PS_ERR_ARGUMENT, "unknown option");
+    }
+}
+
+int Solver::get_option(int option) const
+{
+    switch (option) {
+    case PS_OPT_GRAD: return opt_grad;
+    case PS_OPT_DIV: return opt_div;
+    case PS_OPT_CURL: return opt_curl;
+    case PS_OPT_REPROJECT: return opt_reproject;
+    case PS_OPT_PRECISION: return precision == PREC_FP64 ? PS_PREC_FP64 : PS_PREC_FP32;
+    default: throw Error(PS_ERR_ARGUMENT, "unknown option");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel build (greens3d.cpp:9-547), FP64 on the GPU.
+void Solver::build_kernel()
+{
+    const int prec = PREC_FP64;
+    const size_t nk = (size_t)Mx * oy * oz;
+    kern64.ensure(nk * sizeof(double));
+    KernelFillArgs fa{};
+    fa.kern = (double *)kern64.p;
+    fa.Mx = Mx;
+    fa.oy = oy;
+    fa.oz = oz;
+    for (int d = 0; d < 3; ++d) {
+        fa.P[d] = P[d];
+        fa.dx[d] = dx[d];
+    }
+    fa.reg = reg;
+    fa.norm = (double)P[0] * (double)P[1] * (double)P[2];
+    const int b0 = bc[0], b1 = bc[1], b2 = bc[2];
+    fa.kind = (b0 == 0 && b1 == 0 && b2 == 0) ? 0 : (b0 == 1 && b1 == 1 && b2 == 0) ? 1 : (b2 == 1 && b0 == 0) ? 2 : 3;
+
+    DevBuf oct, spec, line;
+    const int ox = P[0] / 2 + 1;
+    const Plan &px = plan(P[0], prec);
+    const Plan &py = plan(P[1], prec);
+    if (fa.kind == 0 || fa.kind == 2) {
+        const bool three = fa.kind == 0;
+        const int pz = three ? P[2] : 1;
+        const int ozs = three ? oz : 1;
+        oct.ensure((size_t)ox * oy * ozs * sizeof(double));
+        if (three) {
+            const int oext[3] = {ox, oy, oz};
+            PS_CK(launch_sample_unbounded3d((double *)oct.p, oext, P, dx, stream));
+        } else {
+            const int oext[2] = {ox, oy}, P2[2] = {P[0], P[1]};
+            const double dx2[2] = {dx[0], dx[1]};
+            PS_CK(launch_sample_unbounded2d((double *)oct.p, oext, P2, dx2, stream));
+        }
+        spec.ensure((size_t)pz * P[1] * Mx * sizeof(double2));
+        XFwdArgs xa{};
+        xa.in[0] = (const double *)oct.p;
+        xa.out[0] = spec.p;
+        xa.ncomp = 1;
+        xa.L = P[0];
+        xa.n_in = P[0];
+        xa.in_stride = 0;
+        xa.rows_y = P[1];
+        xa.rows_z = pz;
+        xa.out_y = P[1];
+        xa.Mx = Mx;
+        xa.mirror = 1;
+        xa.oct_x = ox;
+        xa.oct_y = oy;
+        xa.Py = P[1];
+        xa.Pz = pz;
+        xa.plan = px.dev;
+        xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return smem_x(prec, P[0], B, px.dev.generic); });
+        PS_CK(launch_xfwd(prec, xa, stream));
+        ColArgs ya{};
+        ya.data[0] = spec.p;
+        ya.ncomp = 1;
+        ya.L = P[1];
+        ya.n_in = P[1];
+        ya.n_out = oy;
+        ya.Mx = Mx;
+        ya.axis_stride = Mx;
+        ya.outer_stride = (long long)P[1] * Mx;
+        ya.plan = py.dev;
+        ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return smem_col(prec, P[1], B, py.dev.generic); });
+        PS_CK(launch_col(prec, 0, ya, pz, stream));
+        if (three) {
+            const Plan &pzp = plan(P[2], prec);
+            ZArgs za{};
+            za.in[0] = spec.p;
+            za.out[0] = spec.p;
+            za.nin = za.nout = 1;
+            za.L = P[2];
+            za.n_in = P[2];
+            za.n_out = oz;
+            za.Mx = Mx;
+            za.axis_stride = (long long)P[1] * Mx;
+            za.row_stride = Mx;
+            za.op = OP_FORWARD;
+            za.plan = pzp.dev;
+            za.B = pick_lines(prec, pzp.dev.tpl, [&](int B) { return smem_z(prec, P[2], B, 1, pzp.dev.generic); });
+            PS_CK(launch_z(prec, za, oy, stream));
+            fa.spec = (const double2 *)spec.p;
+        } else {
+            fa.plane = (const double2 *)spec.p;
+        }
+    } else if (fa.kind == 1) {
+        line.ensure((size_t)oz * sizeof(double));
+        PS_CK(launch_line_ppf((double *)line.p, P[2], dx[2], stream));
+        fa.line = (const double *)line.p;
+    }
+    PS_CK(launch_kernel_fill(fa, stream));
+    PS_CK(cudaStreamSynchronize(stream));
+}
+
+void Solver::ensure_kernel(int prec)
+{
+    if (prec == PREC_FP64) return;
+    const size_t nk = (size_t)Mx * oy * oz;
+    if (kern32.p && kern32.bytes >= nk * sizeof(float)) return;
+    kern32.ensure(nk * sizeof(float));
+    PS_CK(launch_to_fp32((const double *)kern64.p, (float *)kern32.p, nk, stream));
+}
+
+void Solver::ensure_zeta(int prec)
+{
+    const size_t nk = (size_t)Mx * oy * oz;
+    if (!zeta64.p) {
+        zeta64.ensure(nk * sizeof(double));
+        KernelFillArgs fa{};
+        fa.zeta_out = (double *)zeta64.p;
+        fa.Mx = Mx;
+        fa.oy = oy;
+        fa.oz = oz;
+        for (int d = 0; d < 3; ++d) {
+            fa.P[d] = P[d];
+            fa.dx[d] = dx[d];
+        }
+        fa.reg = reg;
+        fa.norm = (double)P[0] * (double)P[1] * (double)P[2];
+        PS_CK(launch_kernel_fill(fa, stream));
+    }
+    if (prec == PREC_FP32 && !zeta32.p) {
+        zeta32.ensure(nk * sizeof(float));
+        PS_CK(launch_to_fp32((const double *)zeta64.p, (float *)zeta32.p, nk, stream));
+    }
+}
+
+// ---------------------------------------------------------------------------
+int Solver::output_mask(int in_mask) const
+{
+    if (opt_grad) {
+        if (!(in_mask & 1)) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for grad option");
+        return 7;
+    }
+    if (opt_div) {
+        if (in_mask != 7) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for div option");
+        return 1;
+    }
+    if (opt_curl) {
+        if (in_mask != 7) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for curl option");
+        return 7;
+    }
+    return in_mask;
+}
+
+int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter_only)
+{
+    check_setup();
+    int in_mask = 0;
+    for (int c = 0; c < 3; ++c)
+        if (Bin[c]) in_mask |= 1 << c;
+    if (!in_mask) throw Error(PS_ERR_STATE, "no right-hand side component given");
+    int op, out_mask;
+    if (filter_only) {
+        op = OP_FILTER;
+        out_mask = in_mask;
+    } else {
+        out_mask = output_mask(in_mask);
+        op = opt_grad ? OP_GRAD : opt_div ? OP_DIV : opt_curl ? OP_CURL : OP_NONE;
+    }
+    int write_mask = 0;
+    for (int c = 0; c < 3; ++c)
+        if ((out_mask >> c & 1) && Aout[c]) write_mask |= 1 << c;
+
+    const int prec = precision;
+    const size_t csz = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
+    ensure_kernel(prec);
+    if (op == OP_FILTER) ensure_zeta(prec);
+    for (int c = 0; c < 3; ++c)
+        if ((in_mask | out_mask) >> c & 1) work[c].ensure(work_elems() * csz);
+    const Plan &px = plan(P[0], prec), &py = plan(P[1], prec), &pz = plan(P[2], prec);
+
+    // x forward over the pushed components
+    XFwdArgs xa{};
+    for (int c = 0; c < 3; ++c)
+        if (in_mask >> c & 1) {
+            xa.in[xa.ncomp] = Bin[c];
+            xa.out[xa.ncomp] = work[c].p;
+            ++xa.ncomp;
+        }
+    xa.L = P[0];
+    xa.n_in = n[0];
+    xa.in_stride = n[0];
+    xa.rows_y = n[1];
+    xa.rows_z = n[2];
+    xa.out_y = P[1];
+    xa.Mx = Mx;
+    xa.plan = px.dev;
+    xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return smem_x(prec, P[0], B, px.dev.generic); });
+    PS_CK(launch_xfwd(prec, xa, stream));
+
+    // y forward (zero-padded from Ny to Py)
+    ColArgs ya{};
+    for (int c = 0; c < 3; ++c)
+        if (in_mask >> c & 1) ya.data[ya.ncomp++] = work[c].p;
+    ya.L = P[1];
+    ya.n_in = n[1];
+    ya.n_out = P[1];
+    ya.Mx = Mx;
+    ya.axis_stride = Mx;
+    ya.outer_stride = (long long)P[1] * Mx;
+    ya.plan = py.dev;
+    ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return smem_col(prec, P[1], B, py.dev.generic); });
+    PS_CK(launch_col(prec, 0, ya, n[2], stream));
+
+    // z: forward (zero-padded from Nz to Pz), spectral operation, inverse (cropped)
+    ZArgs za{};
+    if (op == OP_GRAD) {
+        if (in_mask == 1) {
+            za.nin = 1;
+            za.in[0] = work[0].p;
+        } else {
+            za.nin = 3;
+            for (int d = 0; d < 3; ++d) za.in[d] = work[(in_mask >> d & 1) ? d : 0].p;
+        }
+        za.nout = 0;
+        for (int d = 0; d < 3; ++d) za.out[za.nout++] = (write_mask >> d & 1) ? work[d].p : nullptr;
+    } else if (op == OP_DIV || op == OP_CURL) {
+        za.nin = 3;
+        for (int d = 0; d < 3; ++d) za.in[d] = work[d].p;
+        za.nout = op == OP_DIV ? 1 : 3;
+        for (int d = 0; d < za.nout; ++d) za.out[d] = (write_mask >> d & 1) ? work[d].p : nullptr;
+    } else {
+        for (int c = 0; c < 3; ++c)
+            if (in_mask >> c & 1) {
+                za.in[za.nin] = work[c].p;
+                za.out[za.nin] = (write_mask >> c & 1) ? work[c].p : nullptr;
+                ++za.nin;
+            }
+        za.nout = za.nin;
+    }
+    za.L = P[2];
+    za.n_in = n[2];
+    za.n_out = n[2];
+    za.Mx = Mx;
+    za.axis_stride = (long long)P[1] * Mx;
+    za.row_stride = Mx;
+    za.op = op;
+    za.reproject = op == OP_FILTER && opt_reproject && in_mask == 7;
+    za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
+    za.zeta = op == OP_FILTER ? (prec == PREC_FP64 ? zeta64.p : zeta32.p) : nullptr;
+    za.oct_y = oy;
+    za.Px = P[0];
+    za.Py = P[1];
+    za.Pz = P[2];
+    za.kxc = 2.0 * M_PI / ((double)P[0] * dx[0]);
+    za.kyc = 2.0 * M_PI / ((double)P[1] * dx[1]);
+    za.kzc = 2.0 * M_PI / ((double)P[2] * dx[2]);
+    za.plan = pz.dev;
+    const int nbuf = std::max(za.nin, za.nout);
+    za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return smem_z(prec, P[2], B, nbuf, pz.dev.generic); });
+    PS_CK(launch_z(prec, za, P[1], stream));
+
+    // y inverse (cropped to Ny) and x inverse (cropped to Nx) of the written outputs
+    if (write_mask) {
+        ColArgs yi{};
+        for (int c = 0; c < 3; ++c)
+            if (write_mask >> c & 1) yi.data[yi.ncomp++] = work[c].p;
+        yi.L = P[1];
+        yi.n_in = P[1];
+        yi.n_out = n[1];
+        yi.Mx = Mx;
+        yi.axis_stride = Mx;
+        yi.outer_stride = (long long)P[1] * Mx;
+        yi.plan = py.dev;
+        yi.B = ya.B;
+        PS_CK(launch_col(prec, 1, yi, n[2], stream));
+
+        XInvArgs xi{};
+        for (int c = 0; c < 3; ++c)
+            if (write_mask >> c & 1) {
+                xi.in[xi.ncomp] = work[c].p;
+                xi.out[xi.ncomp] = Aout[c];
+                ++xi.ncomp;
+            }
+        xi.L = P[0];
+        xi.n_out = n[0];
+        xi.Mx = Mx;
+        xi.rows_y = n[1];
+        xi.rows_z = n[2];
+        xi.in_y = P[1];
+        xi.out_stride = n[0];
+        xi.plan = px.dev;
+        xi.B = xa.B;
+        PS_CK(launch_xinv(prec, xi, stream));
+    }
+    return write_mask;
+}
+
+// ---------------------------------------------------------------------------
+// push / solve3d / pull on handle-owned field buffers.
+void Solver::push(const double *const B[3], cudaMemcpyKind kind)
+{
+    check_setup();
+    const size_t bytes = field_elems() * sizeof(double);
+    int mask = 0;
+    for (int c = 0; c < 3; ++c)
+        if (B[c]) {
+            fb[c].ensure(bytes);
+            PS_CK(cudaMemcpyAsync(fb[c].p, B[c], bytes, kind, stream));
+            mask |= 1 << c;
+        }
+    PS_CK(cudaStreamSynchronize(stream));
+    pushed = mask;
+    rhs_ready = 0;
+}
+
+void Solver::solve_internal()
+{
+    check_setup();
+    if (!pushed) throw Error(PS_ERR_STATE, "solve3d called before push");
+    const int out_mask = output_mask(pushed);
+    const double *Bin[3];
+    double *Aout[3];
+    for (int c = 0; c < 3; ++c) {
+        Bin[c] = (pushed >> c & 1) ? (const double *)fb[c].p : nullptr;
+        Aout[c] = nullptr;
+        if (out_mask >> c & 1) {
+            fa[c].ensure(field_elems() * sizeof(double));
+            Aout[c] = (double *)fa[c].p;
+        }
+    }
+    produced = solve(Bin, Aout);
+    rhs_ready = 0;
+}
+
+void Solver::pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind)
+{
+    check_setup();
+    const size_t bytes = field_elems() * sizeof(double);
+    for (int c = 0; c < 3; ++c)
+        if (A[c] && (produced >> c & 1)) PS_CK(cudaMemcpyAsync(A[c], fa[c].p, bytes, kind, stream));
+    bool want_rhs = false;
+    for (int c = 0; c < 3; ++c)
+        if (RB[c] && (pushed >> c & 1)) want_rhs = true;
+    if (want_rhs) {
+        // the reference returns B after its forward/inverse round trip, i.e.
+        // B itself unless the regulariser or the reprojection changed it
+        const bool filtered = reg > 0 || (opt_reproject && pushed == 7);
+        if (filtered && !rhs_ready) {
+            const double *Bin[3];
+            double *Rout[3];
+            for (int c = 0; c < 3; ++c) {
+                Bin[c] = (pushed >> c & 1) ? (const double *)fb[c].p : nullptr;
+                Rout[c] = nullptr;
+                if (pushed >> c & 1) {
+                    fr[c].ensure(bytes);
+                    Rout[c] = (double *)fr[c].p;
+                }
+            }
+            solve(Bin, Rout, true);
+            rhs_ready = 1;
+        }
+        for (int c = 0; c < 3; ++c)
+            if (RB[c] && (pushed >> c & 1))
+                PS_CK(cudaMemcpyAsync(RB[c], filtered ? fr[c].p : fb[c].p, bytes, kind, stream));
+    }
+    PS_CK(cudaStreamSynchronize(stream));
+}
+
+size_t Solver::device_bytes() const
+{
+    size_t s = kern64.bytes + kern32.bytes + zeta64.bytes + zeta32.bytes;
+    for (int c = 0; c < 3; ++c) s += work[c].bytes + fb[c].bytes + fa[c].bytes + fr[c].bytes;
+    for (auto &kv : plans) s += kv.second->table.bytes;
+    return s;
+}
+
+void Solver::copy_kernel(double *host, long long capacity) const
+{
+    check_setup();
+    const size_t nk = (size_t)Mx * oy * oz;
+    if (capacity < (long long)nk) throw Error(PS_ERR_ARGUMENT, "kernel buffer too small");
+    PS_CK(cudaMemcpy(host, kern64.p, nk * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+}  // namespace ps

@@ -1,0 +1,96 @@
+// Host-side solver state and orchestration (C++). One handle = one problem
+// (grid, boundary conditions, spacing, regularisation) on one GPU.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+
+#include "ps_types.hpp"
+
+namespace ps {
+
+// Failure carried to the C ABI as (status, message).
+struct Error : std::runtime_error {
+    int status;
+    Error(int st, const std::string &msg) : std::runtime_error(msg), status(st) {}
+};
+
+// Grow-only device allocation.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t n);
+    void release();
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+};
+
+struct Plan {
+    FftPlanDev dev{};
+    DevBuf table;
+};
+
+struct Solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    bool is_setup = false;
+    int n[3] = {0, 0, 0}, bc[3] = {0, 0, 0}, P[3] = {0, 0, 0};
+    double dx[3] = {0, 0, 0};
+    int reg = 0;
+    int Mx = 0, oy = 0, oz = 0;  // half-spectrum length and kernel octant extents
+
+    int opt_grad = 0, opt_div = 0, opt_curl = 0, opt_reproject = 0;
+    int precision = PREC_FP64;
+
+    DevBuf kern64, kern32;  // octant K = G zeta / (Px Py Pz)
+    DevBuf zeta64, zeta32;  // octant zeta / (Px Py Pz), built on first use
+    DevBuf work[3];         // per-component spectra [Nz][Py][Mx], pass precision
+    DevBuf fb[3], fa[3], fr[3];  // handle-owned fields: pushed B, solution A, returned B
+
+    int pushed = 0;    // component mask held in fb
+    int produced = 0;  // component mask of fa from the last solve
+    int rhs_ready = 0; // fr holds the returned right-hand side of the pushed fb
+
+    std::map<std::pair<int, int>, std::unique_ptr<Plan>> plans;  // (length, precision)
+    std::string last_error;
+
+    Solver();
+    ~Solver();
+
+    void setup3d(const int ncell[3], const int bcs[3], const double dxs[3], int reg_order);
+    void set_option(int option, int value);
+    int get_option(int option) const;
+
+    // Device-pointer pipeline. B: input components (NULL = absent); A: outputs.
+    // Returns the mask of components written to A.
+    int solve(const double *const Bin[3], double *const Aout[3], bool filter_only = false);
+    // Mask of outputs a solve produces for the given input mask (throws on a
+    // combination the options reject).
+    int output_mask(int in_mask) const;
+
+    void push(const double *const B[3], cudaMemcpyKind kind);
+    void solve_internal();
+    void pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind);
+
+    size_t device_bytes() const;
+    void copy_kernel(double *host, long long capacity) const;
+
+    const Plan &plan(int L, int prec);
+    void ensure_kernel(int prec);
+    void ensure_zeta(int prec);
+
+private:
+    void build_kernel();
+    void check_setup() const;
+    size_t field_elems() const { return (size_t)n[0] * n[1] * n[2]; }
+    size_t work_elems() const { return (size_t)n[2] * P[1] * Mx; }
+};
+
+}  // namespace ps

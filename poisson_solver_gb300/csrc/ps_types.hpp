@@ -1,0 +1,145 @@
+// Types shared by the host orchestration (C++) and the CUDA pass kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ps {
+
+constexpr int MAX_STAGES = 16;
+constexpr int MAX_THREADS = 512;  // CTA size bound of the pass kernels (<= 128 registers a thread)
+
+enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
+
+// Register elements a thread holds per FFT stage, which also caps the radix:
+// 8 complex doubles (radix <= 8) or 16 complex floats (radix <= 16).
+constexpr int e_max(int prec) { return prec == PREC_FP64 ? 8 : 16; }
+
+// One 1D transform length as the kernels see it (see ps_fft.cuh).
+struct FftPlanDev {
+    int L;
+    int nstages;
+    int tpl;      // threads per line
+    int generic;  // a stage has a prime radix above 7 (needs scratch shared memory)
+    int radix[MAX_STAGES];
+    int m[MAX_STAGES];
+    int tw[MAX_STAGES];
+    int gw[MAX_STAGES];
+    const void *table;  // complex twiddles in the pass precision
+};
+
+// Spectral operation of the fused z pass.
+enum Op {
+    OP_NONE = 0,     // out_c = K in_c
+    OP_GRAD = 1,     // out_d = i k_d K in_d (component x where d was not pushed)
+    OP_DIV = 2,      // out_x = i K (k . in)
+    OP_CURL = 3,     // out = i K (k x in)
+    OP_FILTER = 4,   // out_c = Z in_c  [- K k_c (k . in) when reprojecting]
+    OP_FORWARD = 5,  // kernel build: forward transform only, spectrum stored
+};
+
+// x forward: pairs of real rows -> half spectra (real-to-complex by packing
+// row 2l as the real and row 2l+1 as the imaginary part of one complex line).
+struct XFwdArgs {
+    const double *in[3];
+    void *out[3];
+    int ncomp;
+    int L;               // Px
+    int n_in;            // leading non-zero samples per row (Nx, or Px)
+    long long in_stride; // row stride of the input rows
+    int rows_y, rows_z;  // row r = k * rows_y + j
+    int out_y;           // y extent of the output array
+    int Mx;              // L/2 + 1
+    int mirror;          // input is the octant of an even function
+    int oct_x, oct_y;    // octant extents (x, y) when mirrored
+    int Py, Pz;          // full extents the octant is reflected onto
+    int B;               // lines per CTA
+    FftPlanDev plan;
+};
+
+// Strided column pass (the y pass), in place.
+struct ColArgs {
+    void *data[3];
+    int ncomp;
+    int L, n_in, n_out;
+    int Mx;                  // number of columns (contiguous dimension)
+    long long axis_stride;   // elements between consecutive transform samples
+    long long outer_stride;  // elements between consecutive outer slabs
+    int B;
+    FftPlanDev plan;
+};
+
+// Fused z pass: forward transform of every input component, spectral
+// operation, inverse transform of every output component.
+struct ZArgs {
+    const void *in[3];
+    void *out[3];
+    int nin, nout;
+    int L, n_in, n_out;
+    int Mx;
+    long long axis_stride;  // Py * Mx
+    long long row_stride;   // Mx (between consecutive y rows)
+    int ky0;                // first y row handled (blockIdx.y offset)
+    int op;
+    int reproject;
+    const void *kern;  // octant K = G zeta / (Px Py Pz), [oz][oy][Mx]
+    const void *zeta;  // octant zeta / (Px Py Pz) for OP_FILTER
+    int oct_y;         // Py/2 + 1
+    int Px, Py, Pz;
+    double kxc, kyc, kzc;  // 2 pi / (P dx) per axis
+    int B;
+    FftPlanDev plan;
+};
+
+// x inverse: half spectra of row pairs -> real rows, cropped to n_out.
+struct XInvArgs {
+    const void *in[3];
+    double *out[3];
+    int ncomp;
+    int L;
+    int n_out;            // Nx
+    int Mx;
+    int rows_y, rows_z;
+    int in_y;             // y extent of the input array
+    long long out_stride; // row stride of the output rows
+    int B;
+    FftPlanDev plan;
+};
+
+// Launchers (ps_kernels.cu). They return the launch status.
+cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st);
+cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaStream_t st);
+cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st);
+cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st);
+
+// Shared-memory bytes each pass needs for a given line count.
+size_t smem_x(int prec, int L, int B, int generic);
+size_t smem_col(int prec, int L, int B, int generic);
+size_t smem_z(int prec, int L, int B, int nbuf, int generic);
+int max_smem_per_block();
+
+// Kernel-build helpers (ps_greens.cu), all FP64.
+cudaError_t launch_sample_unbounded3d(double *oct, const int oext[3], const int P[3], const double dx[3],
+                                      cudaStream_t st);
+cudaError_t launch_sample_unbounded2d(double *oct, const int oext[2], const int P[2], const double dx[2],
+                                      cudaStream_t st);
+// Spectrum G1[k], k <= P/2, of the 1D kernel of the periodic-periodic-unbounded domain.
+cudaError_t launch_line_ppf(double *line, int P, double dz, cudaStream_t st);
+// Octant of K = G zeta / norm from the kernel spectrum (kind 0), or from
+// 1/|k|^2 with the plane/line overrides of the mixed domains.
+struct KernelFillArgs {
+    double *kern;          // out: [oz][oy][Mx] FP64
+    double *zeta_out;      // out (optional): zeta / norm
+    const double2 *spec;   // kind 0: spectrum [oz][Py][Mx] (real part used)
+    const double2 *plane;  // kind 2 (kz = 0 plane): spectrum [oy][Mx]
+    const double *line;    // kind 1 (kx = ky = 0 line): 1D kernel spectrum, length Pz
+    int kind;              // 0 unbounded, 1 ppf, 2 ffp, 3 periodic
+    int Mx, oy, oz;
+    int P[3];
+    double dx[3];
+    int reg;
+    double norm;
+};
+cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st);
+cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t st);
+
+}  // namespace ps

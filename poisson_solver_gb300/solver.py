@@ -1,0 +1,191 @@
+"""Python mirror of the reference solver class (c++/source/poisson_solver.hpp:39-124).
+
+Same member names and argument meaning as the reference C++ class --
+setup3d, set_return_grad/div/curl, set_reprojection, push, solve3d, pull and
+the ``partition`` list -- over the C ABI of libps_gb300.so. Where the
+reference prints an error and returns, this raises PSError with the same
+message. Fields are float64 arrays shaped (Nz, Ny, Nx) (x fastest), the
+layout the reference's push/pull use.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+@dataclass
+class Partition:
+    """One entry of the reference's ``partition`` vector (class_partition.hpp:29-43)."""
+    ncell: tuple
+    icell: tuple
+    dx: tuple
+
+
+def _check(lib, h, st):
+    if st != L.PS_OK:
+        msg = lib.ps_last_error(h)
+        raise L.PSError(st, msg.decode() if msg else lib.ps_status_string(st).decode())
+
+
+def _host_ptr(a, shape, name, writable=False):
+    if a is None:
+        return None
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError(f"{name} must be a C-contiguous float64 numpy array")
+    if a.shape != shape and a.size != int(np.prod(shape)):
+        raise ValueError(f"{name} has shape {a.shape}, expected {shape}")
+    if writable and not a.flags.writeable:
+        raise ValueError(f"{name} is read-only")
+    return a.ctypes.data
+
+
+class PoissonSolver:
+    """GB300 Green's-function FFT Poisson solver: lap(A) = -B in 3D."""
+
+    def __init__(self):
+        self._lib = L.load()
+        h = ctypes.c_void_p()
+        st = self._lib.ps_create(ctypes.byref(h))
+        if st != L.PS_OK:
+            raise L.PSError(st, self._lib.ps_status_string(st).decode())
+        self._h = h
+        self.partition: list[Partition] = []
+        self._shape = None
+
+    # -- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.ps_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name, *args):
+        _check(self._lib, self._h, getattr(self._lib, name)(self._h, *args))
+
+    # -- setup (setup3d.cpp:8-71) ---------------------------------------
+    def setup3d(self, ncell, bc, dx, reg_order: int = 0):
+        nc = (ctypes.c_int * 3)(*[int(v) for v in ncell])
+        b = (ctypes.c_int * 3)(*[int(v) for v in bc])
+        d = (ctypes.c_double * 3)(*[float(v) for v in dx])
+        self._call("ps_setup3d", nc, b, d, int(reg_order))
+        self._shape = (int(ncell[2]), int(ncell[1]), int(ncell[0]))
+        self.partition = []
+        for i in range(self._lib.ps_partition_count(self._h)):
+            n3 = (ctypes.c_int * 3)()
+            i3 = (ctypes.c_int * 3)()
+            d3 = (ctypes.c_double * 3)()
+            self._call("ps_partition", i, n3, i3, d3)
+            self.partition.append(Partition(tuple(n3), tuple(i3), tuple(d3)))
+
+    def setup2d(self, ncell, bc, dx, reg_order: int = 0):
+        nc = (ctypes.c_int * 2)(*ncell)
+        b = (ctypes.c_int * 2)(*bc)
+        d = (ctypes.c_double * 2)(*dx)
+        self._call("ps_setup2d", nc, b, d, int(reg_order))
+
+    def solve2d(self):
+        self._call("ps_solve2d")
+
+    # -- options (settings.cpp:9-30) ------------------------------------
+    def set_return_grad(self, toggle: bool):
+        self._call("ps_set_option", L.PS_OPT_GRAD, int(bool(toggle)))
+
+    def set_return_div(self, toggle: bool):
+        self._call("ps_set_option", L.PS_OPT_DIV, int(bool(toggle)))
+
+    def set_return_curl(self, toggle: bool):
+        self._call("ps_set_option", L.PS_OPT_CURL, int(bool(toggle)))
+
+    def set_reprojection(self, toggle: bool):
+        self._call("ps_set_option", L.PS_OPT_REPROJECT, int(bool(toggle)))
+
+    def set_precision(self, precision: str):
+        """'fp64' (default) or 'fp32' transforms; the kernel is always built in FP64."""
+        v = {"fp64": L.PS_PREC_FP64, "fp32": L.PS_PREC_FP32}[precision]
+        self._call("ps_set_option", L.PS_OPT_PRECISION, v)
+
+    def set_stream(self, stream_handle: int):
+        self._call("ps_set_stream", ctypes.c_void_p(int(stream_handle)))
+
+    # -- host push / solve / pull ----------------------------------------
+    def push(self, bx, by=None, bz=None):
+        s = self._shape
+        self._call("ps_push", _host_ptr(bx, s, "Bx"), _host_ptr(by, s, "By"), _host_ptr(bz, s, "Bz"))
+
+    def solve3d(self):
+        self._call("ps_solve3d")
+
+    def pull(self, ax=None, ay=None, az=None, bx=None, by=None, bz=None):
+        s = self._shape
+        ptrs = [_host_ptr(a, s, n, True) for a, n in zip((ax, ay, az, bx, by, bz),
+                                                         ("Ax", "Ay", "Az", "Bx", "By", "Bz"))]
+        self._call("ps_pull", *ptrs)
+
+    # -- device pointers (raw CUDA addresses, e.g. torch tensor.data_ptr()) --
+    def push_device(self, bx, by=0, bz=0):
+        self._call("ps_push_device", bx or None, by or None, bz or None)
+
+    def pull_device(self, ax=0, ay=0, az=0, bx=0, by=0, bz=0):
+        self._call("ps_pull_device", *[p or None for p in (ax, ay, az, bx, by, bz)])
+
+    def solve3d_device(self, b_ptrs, a_ptrs):
+        """One device-resident solve: b_ptrs / a_ptrs are 3 addresses (0 = absent)."""
+        self._call("ps_solve3d_device", *[p or None for p in b_ptrs], *[p or None for p in a_ptrs])
+
+    def synchronize(self):
+        self._call("ps_synchronize")
+
+    # -- introspection -----------------------------------------------------
+    def info(self, what: int) -> float:
+        v = ctypes.c_double()
+        _check(self._lib, self._h, self._lib.ps_get_info(self._h, what, ctypes.byref(v)))
+        return v.value
+
+    def kernel_octant(self) -> np.ndarray:
+        """FP64 octant K = G zeta / (Px Py Pz), shape (Pz/2+1, Py/2+1, Px/2+1)."""
+        p = [int(self.info(w)) for w in (L.PS_INFO_PADDED_X, L.PS_INFO_PADDED_Y, L.PS_INFO_PADDED_Z)]
+        out = np.empty((p[2] // 2 + 1, p[1] // 2 + 1, p[0] // 2 + 1))
+        self._call("ps_get_kernel", out.ctypes.data, out.size)
+        return out
+
+    @property
+    def padded(self):
+        return tuple(int(self.info(w)) for w in (L.PS_INFO_PADDED_X, L.PS_INFO_PADDED_Y, L.PS_INFO_PADDED_Z))
+
+
+def solve(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,
+          reproject=False, precision="fp64", want_rhs=False):
+    """One-shot host solve; returns (A, RB) lists of 3 arrays or None."""
+    shape = (ncell[2], ncell[1], ncell[0])
+    with PoissonSolver() as ps:
+        ps.setup3d(ncell, bc, dx, reg_order)
+        ps.set_return_grad(grad)
+        ps.set_return_div(div)
+        ps.set_return_curl(curl)
+        ps.set_reprojection(reproject)
+        ps.set_precision(precision)
+        Bc = [None if b is None else np.ascontiguousarray(b, dtype=np.float64) for b in B]
+        ps.push(*Bc)
+        ps.solve3d()
+        nan = float("nan")
+        A = [np.full(shape, nan) for _ in range(3)]
+        RB = [np.full(shape, nan) for _ in range(3)] if want_rhs else [None] * 3
+        ps.pull(*A, *RB)
+    A = [a if not np.isnan(a).all() else None for a in A]
+    RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
+    return A, RB

@@ -1,0 +1,131 @@
+"""The CPU oracle (oracle/ps_oracle.c) pinned to the reference.
+
+* against the reference built from its own sources (oracle/_ref), where the
+  reference is present: special functions, the pencil FFT, the spectral kernel
+  and full solves agree bit for bit;
+* against the golden fixtures the reference build wrote (tests/golden);
+* against the known answers the reference's own validation programs print.
+"""
+import numpy as np
+import pytest
+
+import manufactured as M
+from conftest import golden_cases, load_golden, rel_l2
+
+
+def _need_ref(oracle):
+    if not oracle.available("reference"):
+        pytest.skip("reference sources not present: oracle/_ref not built")
+
+
+def test_special_functions_match_reference(oracle):
+    _need_ref(oracle)
+    xs = np.concatenate([np.linspace(0.0, 40.0, 4001), np.geomspace(1e-8, 3e3, 3000), [1.9999999, 2.0, 2.0000001]])
+    for x in xs:
+        assert oracle.sine_int(x, "port") == oracle.sine_int(x, "reference")
+        assert oracle.bessel_int_J0(x, "port") == oracle.bessel_int_J0(x, "reference")
+
+
+def test_special_functions_values(oracle):
+    # Si(inf) = pi/2; Si is odd; the integral of (1-J0)/t vanishes at 0
+    assert abs(oracle.sine_int(1e4) - np.pi / 2) < 1e-4
+    assert oracle.sine_int(-3.0) == -oracle.sine_int(3.0)
+    assert abs(oracle.sine_int(1.0) - 0.9460830703671830) < 1e-10
+    assert abs(oracle.bessel_int_J0(0.0)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 12, 16, 30, 64, 97, 128, 210, 256])
+def test_fft_matches_reference_and_numpy(oracle, n):
+    rng = np.random.default_rng(n)
+    z = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    fwd = oracle.fft(z)
+    inv = oracle.fft(z, inverse=True)
+    np.testing.assert_allclose(fwd, np.fft.fft(z), rtol=0, atol=1e-12 * max(1.0, np.abs(z).sum()))
+    np.testing.assert_allclose(inv, np.fft.ifft(z) * n, rtol=0, atol=1e-12 * max(1.0, np.abs(z).sum()))
+    if oracle.available("reference"):
+        assert np.array_equal(fwd, oracle.fft(z, kind="reference"))
+        assert np.array_equal(inv, oracle.fft(z, inverse=True, kind="reference"))
+
+
+@pytest.mark.parametrize("bc", [(0, 0, 0), (1, 1, 1), (1, 1, 0), (0, 0, 1)])
+@pytest.mark.parametrize("reg", [0, 2, 5])
+def test_kernel_matches_reference(oracle, bc, reg):
+    _need_ref(oracle)
+    nc, dx = (8, 6, 10), (0.25, 0.3, 0.2)
+    g1, z1 = oracle.greens3d(nc, bc, dx, reg, "port")
+    g2, z2 = oracle.greens3d(nc, bc, dx, reg, "reference")
+    mask = np.ones(g1.shape, bool)
+    if bc == (1, 1, 0):
+        mask[:, 0, 0] = False  # the reference leaves this line uninitialised
+    assert np.array_equal(g1[mask], g2[mask])
+    if reg:
+        assert np.array_equal(z1, z2)
+
+
+def test_kernel_is_real_and_even(oracle):
+    g, _ = oracle.greens3d((8, 6, 10), (0, 0, 0), (0.25, 0.3, 0.2), 0)
+    assert np.abs(g.imag).max() < 1e-14 * np.abs(g.real).max()
+    mirrored = g[np.ix_((-np.arange(g.shape[0])) % g.shape[0], (-np.arange(g.shape[1])) % g.shape[1],
+                        (-np.arange(g.shape[2])) % g.shape[2])]
+    assert np.abs(g - mirrored).max() < 1e-14 * np.abs(g).max()
+
+
+SOLVES = [
+    ((8, 6, 10), (0, 0, 0), (0.25, 0.3, 0.2), 0, dict(curl=True), 3, False),
+    ((8, 6, 10), (0, 0, 0), (0.25, 0.3, 0.2), 2, dict(), 1, False),
+    ((7, 5, 9), (0, 0, 0), (0.2, 0.2, 0.2), 6, dict(div=True), 3, False),
+    ((8, 6, 10), (1, 1, 1), (0.25, 0.3, 0.2), 0, dict(curl=True), 3, False),
+    ((9, 5, 7), (1, 1, 1), (0.25, 0.3, 0.2), 4, dict(grad=True), 3, False),
+    ((8, 6, 10), (1, 1, 0), (0.25, 0.3, 0.2), 0, dict(curl=True), 3, True),
+    ((8, 6, 10), (0, 0, 1), (0.25, 0.3, 0.2), 0, dict(grad=True), 3, False),
+    ((8, 6, 10), (0, 0, 0), (0.25, 0.3, 0.2), 2, dict(curl=True, reproject=True), 3, False),
+]
+
+
+@pytest.mark.parametrize("case", SOLVES, ids=[f"{c[1]}-{list(c[4])}-reg{c[3]}" for c in SOLVES])
+def test_solve_matches_reference(oracle, case):
+    _need_ref(oracle)
+    nc, bc, dx, reg, opts, ncomp, zero_mean = case
+    rng = np.random.default_rng(sum(nc) + reg)
+    B = []
+    for c in range(3):
+        if c < ncomp:
+            b = rng.standard_normal((nc[2], nc[1], nc[0]))
+            if zero_mean:
+                b -= b.mean(axis=(1, 2), keepdims=True)
+            B.append(b)
+        else:
+            B.append(None)
+    A1, R1 = oracle.solve3d(nc, bc, dx, B, reg, want_rhs=True, kind="port", **opts)
+    A2, R2 = oracle.solve3d(nc, bc, dx, B, reg, want_rhs=True, kind="reference", **opts)
+    tol = 2e-15 if bc == (1, 1, 0) else 0.0  # undefined kernel line, weighted by a ~1e-16 mean
+    assert rel_l2(A1, A2) <= tol
+    assert rel_l2(R1, R2) <= tol
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_port_matches_golden(oracle, name):
+    g = load_golden(name)
+    A, RB = oracle.solve3d(g["ncell"], g["bc"], g["dx"], g["B"], g["reg"], want_rhs=True, **g["opts"])
+    # bitwise on the machine that wrote the fixtures; libm may differ by an ulp elsewhere
+    assert rel_l2(A, g["A"]) < 1e-13
+    assert rel_l2(RB, g["RB"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["periodic3d", "mixed_ppf3d", "mixed_ffp3d"])
+def test_port_reproduces_reference_printed_errors(oracle, name):
+    nc, bc, dx, opt, B, sol = M.case(name)
+    A, _ = oracle.solve3d(nc, bc, dx, B, 0, **{opt: True})
+    err = M.printed_error(A, sol, dx)
+    assert abs(err - M.KNOWN_ERRORS[name]) <= 5e-7 * M.KNOWN_ERRORS[name] + 1e-17
+
+
+def test_rejections_match_reference(oracle):
+    nc, dx = (6, 6, 6), (0.1, 0.1, 0.1)
+    b = np.ones((6, 6, 6))
+    with pytest.raises(ValueError, match="status 3"):
+        oracle.solve3d(nc, (0, 0, 0), dx, [b, None, None], curl=True)
+    with pytest.raises(ValueError, match="status 3"):
+        oracle.solve3d(nc, (0, 0, 0), dx, [None, b, None], grad=True)
+    with pytest.raises(ValueError, match="status 2"):
+        oracle.solve3d(nc, (0, 1, 0), dx, [b, None, None])
