@@ -1,0 +1,449 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the 3D Green's-function FFT Poisson solve.
+
+Default workload: the 512^3 unbounded 3-component vector solve (padded to
+1024^3), curl output, regularisation order 10, source = 16 seeded
+Gaussian-cored vortex rings. One step = one solve of that problem.
+
+  value      Mpts/s of the device-resident solve (inputs already in HBM) with
+             FP32 transforms (FP64 kernel build and FP64 field I/O); the FP64
+             transform solve of the same inputs is reported beside it with the
+             relative L2 difference between the two
+  e2e        the same metric through the public C-ABI push/solve3d/pull with
+             pinned HOST buffers, both copies inside the timed region
+  roofline   the dominant kernel's algorithmic bytes per launch over its
+             CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline / --impl reference
+             the reference algorithm on the host cores (the C restatement in
+             oracle/, which the tests pin bit for bit to the reference build)
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Prints one JSON line (rank 0). Multi-GPU: independent replicas, one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpts/s per solve, mixed-prec vs FP64 on GPU at ≤1e-6 rel L2; HBM GB/s"
+PASS_NAMES = ["x_forward", "y_forward", "z_fused", "y_inverse", "x_inverse"]
+KERNEL_NAMES = ["k_xfwd", "k_col<fwd>", "k_z<curl>", "k_col<inv>", "k_xinv"]
+
+WORKLOADS = {
+    "rings512": dict(n=512, reg=10, rings=16, seed=2024,
+                     desc="512^3 unbounded 3-component vector Poisson (padded 1024^3), curl, reg 10, "
+                          "16 seeded Gaussian vortex rings"),
+    "rings256": dict(n=256, reg=6, rings=1, seed=7,
+                     desc="256^3 unbounded 3-component vector Poisson (padded 512^3), curl, reg 6, "
+                          "one perturbed Gaussian-cored vortex ring"),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# Synthetic sources (vorticity of Gaussian-cored rings), generated on the device.
+def ring_params(w):
+    rng = np.random.default_rng(w["seed"])
+    rings = []
+    if w["rings"] == 1:
+        # ring radius 0.5, core 0.05, unit circulation, axis z; radius perturbed by
+        # sum_{m=2..8} 0.01 R a_m cos(m theta + phi_m)
+        modes = [(m, rng.standard_normal(), rng.uniform(0, 2 * np.pi)) for m in range(2, 9)]
+        rings.append(dict(c=np.zeros(3), n=np.array([0.0, 0.0, 1.0]), R=0.5, s=0.05, G=1.0, modes=modes))
+    else:
+        for _ in range(w["rings"]):
+            v = rng.standard_normal(3)
+            rings.append(dict(c=rng.uniform(-0.55, 0.55, 3), n=v / np.linalg.norm(v), R=rng.uniform(0.1, 0.3),
+                              s=rng.uniform(0.02, 0.04), G=1.0, modes=[]))
+    return rings
+
+
+def make_source(w, device, dtype=None):
+    import torch
+    n = w["n"]
+    dx = 2.0 / n
+    x = -1.0 + (torch.arange(n, device=device, dtype=torch.float64) + 0.5) * dx
+    out = [torch.zeros((n, n, n), device=device, dtype=torch.float64) for _ in range(3)]
+    rings = ring_params(w)
+    slab = 64
+    for z0 in range(0, n, slab):
+        Z, Y, X = torch.meshgrid(x[z0:z0 + slab], x, x, indexing="ij")
+        for r in rings:
+            c, nv = r["c"], r["n"]
+            px, py, pz = X - c[0], Y - c[1], Z - c[2]
+            h = px * nv[0] + py * nv[1] + pz * nv[2]
+            qx, qy, qz = px - h * nv[0], py - h * nv[1], pz - h * nv[2]
+            rho = torch.sqrt(qx * qx + qy * qy + qz * qz).clamp_min(1e-300)
+            R = r["R"]
+            if r["modes"]:
+                th = torch.atan2(qy, qx)
+                pert = sum(a * torch.cos(m * th + ph) for m, a, ph in r["modes"])
+                R = r["R"] * (1.0 + 0.01 * pert)
+            d2 = (rho - R) ** 2 + h * h
+            mag = r["G"] / (2 * np.pi * r["s"] ** 2) * torch.exp(-d2 / (2 * r["s"] ** 2))
+            # azimuthal unit vector n x rho_hat
+            tx = (nv[1] * qz - nv[2] * qy) / rho
+            ty = (nv[2] * qx - nv[0] * qz) / rho
+            tz = (nv[0] * qy - nv[1] * qx) / rho
+            out[0][z0:z0 + slab] += mag * tx
+            out[1][z0:z0 + slab] += mag * ty
+            out[2][z0:z0 + slab] += mag * tz
+    return out
+
+
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(n, P, cin, cout, w, g=None):
+    """Bytes each pass must move at minimum (SURVEY-style accounting): real FP64
+    I/O once, half-spectrum working arrays once per read and write, the real even
+    kernel read once as an octant. w = complex working bytes, g = kernel bytes."""
+    Nx, Ny, Nz = n
+    Px, Py, Pz = P
+    Mx = Px // 2 + 1
+    g = g or w // 2
+    r = 8
+    N = Nx * Ny * Nz
+    slab_in, slab_pad = Mx * Ny * Nz, Mx * Py * Nz
+    return [
+        cin * N * r + cin * slab_in * w,
+        cin * slab_in * w + cin * slab_pad * w,
+        cin * slab_pad * w + Mx * (Py // 2 + 1) * (Pz // 2 + 1) * g + cout * slab_pad * w,
+        cout * slab_pad * w + cout * slab_in * w,
+        cout * slab_in * w + cout * N * r,
+    ]
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(workload, precision):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == workload and parts[1] == precision:
+                return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(gpu_index)], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                p = [s.strip() for s in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return None
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = max((num(r[2]) for r in rows if num(r[2]) is not None), default=None)
+        loaded = [v for v in sm if smax and v > 0.5 * smax] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": smax,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value):
+    """Max of a float over ranks (the timed region is the slowest rank's)."""
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(points_per_rank, steps, elapsed_s_max, world):
+    """Whole-job Mpts/s: every rank solves its own replica in the slowest rank's time."""
+    return world * points_per_rank * steps / elapsed_s_max / 1e6
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(n, reg, reps=2):
+    """Oracle port (the reference algorithm, one thread) on an n^3 sample: Mpts/s of solve3d."""
+    from oracle import oracle
+    w = dict(WORKLOADS["rings512"])
+    w["n"] = n
+    B = [b.numpy() for b in make_source(w, "cpu")]
+    dx = 2.0 / n
+    best = None
+    for _ in range(reps):
+        _, sec = oracle.solve3d_timed((n, n, n), (0, 0, 0), (dx,) * 3, B, reg, curl=True)
+        best = sec[1] if best is None else min(best, sec[1])
+    return n ** 3 / best / 1e6, best
+
+
+def _ref_worker(args):
+    n, reg, steps, warmup = args
+    from oracle import oracle
+    rng = np.random.default_rng(n)
+    B = [rng.standard_normal((n, n, n)) for _ in range(3)]
+    dx = 2.0 / n
+    times = []
+    for s in range(warmup + steps):
+        _, sec = oracle.solve3d_timed((n, n, n), (0, 0, 0), (dx,) * 3, B, reg, curl=True)
+        if s >= warmup:
+            times.append(sec[1])
+    return times
+
+
+def run_reference(args, w):
+    world, rank, _, pg = dist_setup()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    from oracle import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    n = 64
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_worker, [(n, w["reg"], args.steps, args.warmup)] * cores)
+    wall = time.perf_counter() - t0
+    slowest = max(sum(t) for t in res)
+    value = cores * n ** 3 * args.steps / slowest / 1e6
+    sample = (f"{cores} concurrent single-thread solves of a {n}^3 sample of the workload "
+              f"(padded {2 * n}^3, 3 components, curl, reg {w['reg']}), solve3d time only")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": slowest / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": w["desc"], "sample_grid": [n, n, n]},
+        "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, w):
+    import torch
+
+    import poisson_solver_gb300 as psg
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = w["n"]
+    nc = (n, n, n)
+    dx = (2.0 / n,) * 3
+    points = n ** 3
+    K, W = args.steps, args.warmup
+
+    log(f"[rank {rank}] building sources {n}^3")
+    B = make_source(w, dev)
+    A = [torch.empty_like(b) for b in B]
+    A64 = [torch.empty_like(b) for b in B]
+    ps = psg.PoissonSolver()
+    t0 = time.perf_counter()
+    ps.setup3d(nc, (0, 0, 0), dx, w["reg"])
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ps.set_return_curl(True)
+    stream = torch.cuda.current_stream(dev)
+    ps.set_stream(stream.cuda_stream)
+    bp = [b.data_ptr() for b in B]
+    P = ps.padded
+    launches = int(ps.info(psg._lib.PS_INFO_LAUNCHES_PER_SOLVE))
+
+    def timed_loop(precision, steps, warm, out, sample_clocks=False):
+        ps.set_precision(precision)
+        ap = [a.data_ptr() for a in out]
+        for _ in range(warm):
+            ps.solve3d_device(bp, ap)
+        torch.cuda.synchronize()
+        ps.pass_times(reset=True)
+        ps.set_pass_timing(True)
+        clocks = ClockSampler(local) if sample_clocks else None
+        barrier(pg)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ps.solve3d_device(bp, ap)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier(pg)
+        ms = e0.elapsed_time(e1)
+        clk = clocks.stop() if clocks else None
+        ps.set_pass_timing(False)
+        pms, nsolves = ps.pass_times(reset=True)
+        return ms, [v / max(nsolves, 1) for v in pms], clk
+
+    log(f"[rank {rank}] fp32 timed loop: {K} steps after {W} warm-up")
+    ms32, pass32, clocks = timed_loop("fp32", K, W, A, sample_clocks=True)
+    ms32_max = max_over_ranks(pg, ms32)
+    value = replica_throughput(points, K, ms32_max / 1e3, world)
+
+    K64 = max(2, K // 3)
+    log(f"[rank {rank}] fp64 timed loop: {K64} steps")
+    ms64, pass64, _ = timed_loop("fp64", K64, 1, A64)
+    ms64_max = max_over_ranks(pg, ms64)
+    value64 = replica_throughput(points, K64, ms64_max / 1e3, world)
+    num = sum(float(torch.sum((a - b) ** 2)) for a, b in zip(A, A64))
+    den = sum(float(torch.sum(b ** 2)) for b in A64)
+    rel = (num / den) ** 0.5
+
+    # end to end through the public API with pinned host buffers
+    ps.set_precision("fp32")
+    Bh = [b.cpu().pin_memory() for b in B]
+    Ah = [torch.empty(b.shape, dtype=torch.float64).pin_memory() for b in B]
+    Bn = [b.numpy() for b in Bh]
+    An = [a.numpy() for a in Ah]
+    for _ in range(max(1, W // 2)):
+        ps.push(*Bn)
+        ps.solve3d()
+        ps.pull(*An)
+    Ke = max(2, min(K, 5))
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        ps.push(*Bn)
+        ps.solve3d()
+        ps.pull(*An)
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e = replica_throughput(points, Ke, e2e_s, world)
+    e2e_check = max(float((Ah[i] - A[i].cpu()).abs().max()) for i in range(3))
+
+    # roofline of the dominant kernel (fp32 path), live CUDA-event durations
+    byt = algorithmic_bytes(nc, P, 3, 3, 8, 4)
+    top = int(np.argmax(pass32))
+    peak, peak_kind = measured_peaks()
+    achieved = byt[top] / (pass32[top] * 1e-3) / 1e9
+    solve_gbs = sum(byt) / (ms32 / K * 1e-3) / 1e9
+    traffic = profiled_traffic(args.workload, "fp32")
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        log("[rank 0] CPU baseline (oracle port, one thread)")
+        cv, ct = cpu_sample(64, w["reg"])
+        cpu = {"value": cv, "unit": "Mpts/s", "cores": 1, "kind": "port",
+               "sample": f"64^3 sample of the workload (padded 128^3, 3 components, curl, reg {w['reg']}), "
+                         f"oracle/ps_oracle.c solve3d on one host thread, best of 2: {ct:.2f} s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms32_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "grid": list(nc), "padded": list(P), "components": 3,
+                   "output": "curl", "reg_order": w["reg"],
+                   "precision": "FP32 transforms; FP64 kernel build, FP64 field input/output",
+                   "l2": "inputs larger than L2 (3 x %.2f GB in, 3 x %.2f GB out)" % (points * 8 / 1e9, points * 8 / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[top], "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes": byt[top], "ms": pass32[top]},
+        "passes_ms": dict(zip(PASS_NAMES, pass32)),
+        "solve_gbs_algorithmic": solve_gbs,
+        "fp64": {"value": value64, "ms_per_step": ms64_max / K64, "passes_ms": dict(zip(PASS_NAMES, pass64))},
+        "mixed_vs_fp64_speedup": value / value64,
+        "rel_l2_fp32_vs_fp64": rel,
+        "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": 3 * points * 8,
+                "d2h_bytes_per_step": 3 * points * 8, "max_abs_diff_vs_device": e2e_check},
+        "gpu_launches": K * launches,
+        "clocks": clocks,
+        "setup_s": setup_s,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rings512")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warm-up raised to the minimum of 3 steps")
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_ours(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

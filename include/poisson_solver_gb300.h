@@ -47,7 +47,8 @@ enum {
     PS_OPT_DIV = 1,        /* value 0/1: return div A    (set_return_div, settings.cpp:15)  */
     PS_OPT_CURL = 2,       /* value 0/1: return curl A   (set_return_curl, settings.cpp:21) */
     PS_OPT_REPROJECT = 3,  /* value 0/1: reproject the returned B (set_reprojection, settings.cpp:26) */
-    PS_OPT_PRECISION = 4   /* PS_PREC_FP64 (default) or PS_PREC_FP32 transforms */
+    PS_OPT_PRECISION = 4,  /* PS_PREC_FP64 (default) or PS_PREC_FP32 transforms */
+    PS_OPT_PASS_TIMING = 5 /* value 0/1: time each pass of every solve with CUDA events */
 };
 
 enum {
@@ -132,6 +133,14 @@ enum {
     PS_INFO_KERNEL_OCTANT = 5        /* elements of the stored kernel octant */
 };
 int ps_get_info(const ps_solver *h, int what, double *value);
+
+/* Per-pass device times accumulated since the last reset while
+ * PS_OPT_PASS_TIMING is on, measured with CUDA events on the handle's stream:
+ * ms[0] x forward, ms[1] y forward, ms[2] fused z pass, ms[3] y inverse,
+ * ms[4] x inverse. *nsolves receives the number of solves summed. Waits for
+ * the timed work to finish; reset != 0 clears the sums afterwards. */
+enum { PS_NUM_PASSES = 5 };
+int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset);
 
 /* Copy the FP64 kernel octant K = G * zeta / (Px Py Pz), layout
  * [Pz/2+1][Py/2+1][Px/2+1] (x fastest), to a HOST array. */

@@ -54,6 +54,10 @@ def _lib(kind: str) -> ctypes.CDLL:
     f = getattr(lib, pre + "solve3d")
     f.restype = ctypes.c_int
     f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 4 + [_dp] * 9
+    if kind == "port":
+        f = lib.oracle_solve3d_timed
+        f.restype = ctypes.c_int
+        f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 4 + [_dp] * 10
     f = getattr(lib, pre + "greens3d")
     f.restype = ctypes.c_int
     f.argtypes = [_ip, _ip, _dp, ctypes.c_int, _dp, _dp, _dp, _ip]
@@ -147,3 +151,21 @@ def solve3d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False,
     A = [a if not np.isnan(a).all() else None for a in A]
     RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
     return A, RB
+
+
+def solve3d_timed(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False, reproject=False):
+    """Port solve returning (A, seconds[setup, push+solve, pull])."""
+    nx, ny, nz = ncell
+    shape = (nz, ny, nx)
+    Bc = [_f64(b) for b in B]
+    A = [np.empty(shape) for _ in range(3)]
+    sec = np.zeros(3)
+    nc = (ctypes.c_int * 3)(*ncell)
+    b = (ctypes.c_int * 3)(*bc)
+    d = (ctypes.c_double * 3)(*dx)
+    st = _lib("port").oracle_solve3d_timed(nc, b, d, int(reg), int(grad), int(div), int(curl), int(reproject),
+                                           *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], None, None, None,
+                                           _ptr(sec))
+    if st:
+        raise ValueError(f"oracle solve3d status {st}")
+    return A, sec

@@ -21,10 +21,12 @@
  * dereferences NULL (solve3d.cpp:350-352); here a missing component d uses
  * component x, so a scalar push gives the gradient of the scalar solution.
  */
+#define _POSIX_C_SOURCE 199309L
 #include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "ps_oracle.h"
 
@@ -428,12 +430,30 @@ int oracle_greens3d(const int ncell[3], const int bc[3], const double dx[3], int
 
 /* ------------------------------------------------------------------------ */
 /* setup3d + push + solve3d + pull on one rank. */
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int reg,
                    int grad, int div, int curl, int reproject,
                    const double *bx, const double *by, const double *bz,
                    double *ax, double *ay, double *az,
                    double *rbx, double *rby, double *rbz)
 {
+    return oracle_solve3d_timed(ncell, bc, dx, reg, grad, div, curl, reproject, bx, by, bz, ax, ay, az,
+                                rbx, rby, rbz, NULL);
+}
+
+int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3], int reg,
+                         int grad, int div, int curl, int reproject,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz, double seconds[3])
+{
+    double t0 = now_s();
     const double *B[3] = {bx, by, bz};
     double *A[3] = {ax, ay, az};
     double *RB[3] = {rbx, rby, rbz};
@@ -457,6 +477,7 @@ int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int 
     kernel_t K;
     int st = kernel_build(&K, ncell, bc, dx, reg);
     if (st) { kernel_free(&K); return st; }
+    double t1 = now_s();
 
     const int nx = ncell[0], ny = ncell[1], nz = ncell[2];
     const int px = K.p[0], py = K.p[1];
@@ -581,6 +602,8 @@ int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int 
             }
     }
 
+    double t2 = now_s();
+
     /* pull (pull.cpp:327-451): real part, x cropped to Nx. */
     for (int f = 0; f < 6; ++f) {
         cplx *a = f < 3 ? lhs[f] : rhs[f - 3];
@@ -597,5 +620,10 @@ int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int 
     }
     free(pen); free(w);
     kernel_free(&K);
+    if (seconds) {
+        seconds[0] = t1 - t0;        /* setup3d: kernel build */
+        seconds[1] = t2 - t1;        /* push + solve3d */
+        seconds[2] = now_s() - t2;   /* pull */
+    }
     return 0;
 }

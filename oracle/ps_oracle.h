@@ -42,6 +42,14 @@ int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int 
                    double *ax, double *ay, double *az,
                    double *rbx, double *rby, double *rbz);
 
+/* As oracle_solve3d, also returning wall seconds of the kernel build
+ * (seconds[0]), push + solve (seconds[1]) and pull (seconds[2]). */
+int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3], int reg,
+                         int grad, int div, int curl, int reproject,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz, double seconds[3]);
+
 #ifdef __cplusplus
 }
 #endif

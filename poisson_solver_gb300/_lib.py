@@ -25,6 +25,7 @@ PS_OPT_DIV = 1
 PS_OPT_CURL = 2
 PS_OPT_REPROJECT = 3
 PS_OPT_PRECISION = 4
+PS_OPT_PASS_TIMING = 5
 
 PS_PREC_FP64 = 0
 PS_PREC_FP32 = 1
@@ -63,6 +64,7 @@ SIGNATURES = {
     "ps_status_string": (ctypes.c_char_p, [_i]),
     "ps_get_info": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_double)]),
     "ps_get_kernel": (_i, [_vp, _dp, ctypes.c_longlong]),
+    "ps_get_pass_times": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _ip, _i]),
 }
 
 _lib: ctypes.CDLL | None = None

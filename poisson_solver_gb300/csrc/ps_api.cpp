@@ -192,6 +192,20 @@ int ps_get_info(const ps_solver *h, int what, double *value)
     return PS_OK;
 }
 
+int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset)
+{
+    if (!ms) return PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) {
+        s.drain_timing();
+        for (int i = 0; i < ps::Solver::NPASS; ++i) ms[i] = s.pass_ms[i];
+        if (nsolves) *nsolves = s.timed_solves;
+        if (reset) {
+            for (double &v : s.pass_ms) v = 0.0;
+            s.timed_solves = 0;
+        }
+    });
+}
+
 int ps_get_kernel(const ps_solver *h, double *out, long long capacity)
 {
     if (!out) return PS_ERR_ARGUMENT;

@@ -289,13 +289,16 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
 // different radices never share a live range (a radix switch inside one
 // stage loop, or the stage loops inside a component loop, made the register
 // allocator keep them all live and spill).
+// Radices without an unrolled butterfly: primes above 7 (11 and 13 included).
+__device__ __forceinline__ bool is_generic_radix(int R) { return R > 8 && R != 16; }
+
 template <bool INV, typename C>
 __device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
                                           const StageInfo &si, int ncomp = 1, int cstride = 0)
 {
     const int ns = P.nstages;
     int s = 0;
-    for (; s < ns && si.st[s].x > 16; ++s)
+    for (; s < ns && is_generic_radix(si.st[s].x); ++s)
         for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, si.st[s]);
     for (; s < ns && si.st[s].x == 7; ++s)
         for (int c = 0; c < ncomp; ++c) stage<7, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);

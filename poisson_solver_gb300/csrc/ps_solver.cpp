@@ -50,7 +50,27 @@ void DevBuf::release()
 
 Solver::Solver() { PS_CK(cudaGetDevice(&device)); }
 
-Solver::~Solver() = default;
+Solver::~Solver()
+{
+    for (auto *v : {&ev_pending, &ev_pool})
+        for (auto &set : *v)
+            for (cudaEvent_t e : set) cudaEventDestroy(e);
+}
+
+void Solver::drain_timing()
+{
+    for (auto &set : ev_pending) {
+        PS_CK(cudaEventSynchronize(set[NPASS]));
+        for (int i = 0; i < NPASS; ++i) {
+            float ms = 0.f;
+            PS_CK(cudaEventElapsedTime(&ms, set[i], set[i + 1]));
+            pass_ms[i] += ms;
+        }
+        ++timed_solves;
+        ev_pool.push_back(set);
+    }
+    ev_pending.clear();
+}
 
 // ---------------------------------------------------------------------------
 // Transform plans. Stage order (which fft_lines relies on): primes above 7
@@ -219,6 +239,7 @@ void Solver::set_option(int option, int value)
     case PS_OPT_DIV: opt_div = value != 0; break;
     case PS_OPT_CURL: opt_curl = value != 0; break;
     case PS_OPT_REPROJECT: opt_reproject = value != 0; rhs_ready = 0; break;
+    case PS_OPT_PASS_TIMING: opt_timing = value != 0; break;
     case PS_OPT_PRECISION:
         if (value != PS_PREC_FP64 && value != PS_PREC_FP32) throw Error(PS_ERR_ARGUMENT, "unknown precision");
         precision = value == PS_PREC_FP64 ? PREC_FP64 : PREC_FP32;
@@ -236,6 +257,7 @@ int Solver::get_option(int option) const
     case PS_OPT_CURL: return opt_curl;
     case PS_OPT_REPROJECT: return opt_reproject;
     case PS_OPT_PRECISION: return precision == PREC_FP64 ? PS_PREC_FP64 : PS_PREC_FP32;
+    case PS_OPT_PASS_TIMING: return opt_timing;
     default: throw Error(PS_ERR_ARGUMENT, "unknown option");
     }
 }
@@ -417,6 +439,21 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         if ((in_mask | out_mask) >> c & 1) work[c].ensure(work_elems() * csz);
     const Plan &px = plan(P[0], prec), &py = plan(P[1], prec), &pz = plan(P[2], prec);
 
+    std::array<cudaEvent_t, NPASS + 1> ev{};
+    if (opt_timing) {
+        if (ev_pool.empty()) {
+            for (auto &e : ev) PS_CK(cudaEventCreate(&e));
+        } else {
+            ev = ev_pool.back();
+            ev_pool.pop_back();
+        }
+        ev_pending.push_back(ev);
+    }
+    auto mark = [&](int i) {
+        if (opt_timing) PS_CK(cudaEventRecord(ev[i], stream));
+    };
+    mark(0);
+
     // x forward over the pushed components
     XFwdArgs xa{};
     for (int c = 0; c < 3; ++c)
@@ -435,6 +472,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     xa.plan = px.dev;
     xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return smem_x(prec, P[0], B, px.dev.generic); });
     PS_CK(launch_xfwd(prec, xa, stream));
+    mark(1);
 
     // y forward (zero-padded from Ny to Py)
     ColArgs ya{};
@@ -449,6 +487,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     ya.plan = py.dev;
     ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return smem_col(prec, P[1], B, py.dev.generic); });
     PS_CK(launch_col(prec, 0, ya, n[2], stream));
+    mark(2);
 
     // z: forward (zero-padded from Nz to Pz), spectral operation, inverse (cropped)
     ZArgs za{};
@@ -497,6 +536,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     const int nbuf = std::max(za.nin, za.nout);
     za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return smem_z(prec, P[2], B, nbuf, pz.dev.generic); });
     PS_CK(launch_z(prec, za, P[1], stream));
+    mark(3);
 
     // y inverse (cropped to Ny) and x inverse (cropped to Nx) of the written outputs
     if (write_mask) {
@@ -512,6 +552,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         yi.plan = py.dev;
         yi.B = ya.B;
         PS_CK(launch_col(prec, 1, yi, n[2], stream));
+        mark(4);
 
         XInvArgs xi{};
         for (int c = 0; c < 3; ++c)
@@ -530,7 +571,10 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         xi.plan = px.dev;
         xi.B = xa.B;
         PS_CK(launch_xinv(prec, xi, stream));
+    } else {
+        mark(4);
     }
+    mark(5);
     return write_mask;
 }
 

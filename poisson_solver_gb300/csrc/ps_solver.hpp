@@ -3,7 +3,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <map>
+#include <vector>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -59,6 +61,14 @@ struct Solver {
     int rhs_ready = 0; // fr holds the returned right-hand side of the pushed fb
 
     std::map<std::pair<int, int>, std::unique_ptr<Plan>> plans;  // (length, precision)
+
+    // Optional per-pass timing: one set of boundary events per timed solve.
+    static constexpr int NPASS = 5;
+    int opt_timing = 0;
+    std::vector<std::array<cudaEvent_t, NPASS + 1>> ev_pending, ev_pool;
+    double pass_ms[NPASS] = {0, 0, 0, 0, 0};
+    int timed_solves = 0;
+    void drain_timing();
     std::string last_error;
 
     Solver();

@@ -147,6 +147,16 @@ class PoissonSolver:
         """One device-resident solve: b_ptrs / a_ptrs are 3 addresses (0 = absent)."""
         self._call("ps_solve3d_device", *[p or None for p in b_ptrs], *[p or None for p in a_ptrs])
 
+    def set_pass_timing(self, on: bool):
+        self._call("ps_set_option", L.PS_OPT_PASS_TIMING, int(bool(on)))
+
+    def pass_times(self, reset: bool = True):
+        """(per-pass milliseconds summed over timed solves, number of solves)."""
+        ms = (ctypes.c_double * 5)()
+        n = ctypes.c_int()
+        self._call("ps_get_pass_times", ms, ctypes.byref(n), int(reset))
+        return list(ms), n.value
+
     def synchronize(self):
         self._call("ps_synchronize")
 

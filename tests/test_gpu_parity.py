@@ -84,7 +84,11 @@ def test_edge_sizes(native, oracle, nc, bc):
     B = _fields(nc, (0, 1, 2), sum(nc), zero_mean=bc == (1, 1, 0))
     ref, _ = oracle.solve3d(nc, bc, dx, B, 2, curl=True)
     got, _ = native.solve(nc, bc, dx, B, 2, curl=True)
-    assert rel_l2(got, ref) < FP64_TOL
+    # On the smallest grids the exact curl can vanish (every derivative mode is
+    # a Nyquist mode); both solves then return rounding noise, so the error is
+    # measured against the scale of a unit solve there.
+    scale = max(max(float(np.abs(r).max()) for r in ref), 1e-6 * max(dx) ** 2)
+    assert max(float(np.abs(g - r).max()) for g, r in zip(got, ref)) <= FP64_TOL * scale
 
 
 @pytest.mark.parametrize("bc", BCS)
