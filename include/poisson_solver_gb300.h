@@ -104,6 +104,23 @@ int ps_pull_device(ps_solver *h, double *ax, double *ay, double *az, double *bx,
 int ps_solve3d_device(ps_solver *h, const double *bx, const double *by, const double *bz,
                       double *ax, double *ay, double *az);
 
+/* Device-resident solve that allocates no memory: no reference counterpart
+ * (the reference allocates its arrays in every push and solve). For callers
+ * that may not call cudaMalloc/cudaFree while their run is under way, e.g. a
+ * time-stepping code solving inside a device-memory budget reserved up front
+ * or owned by another framework's pool, where an allocation could fail late
+ * or synchronise the device. Same arguments and result as ps_solve3d_device
+ * on a handle set up with ps_setup3d, but always with FP64 transforms and
+ * with its spectra in 32 MiB of scratch compiled into the library: problems
+ * needing more -- (components in use) x Nz x Py x (Px/2+1) x 16 bytes, e.g.
+ * a 64^3 unbounded 3-component curl solve needs 25.6 MiB -- fail with
+ * PS_ERR_UNSUPPORTED. Every GPU that loads this part of the library holds the
+ * scratch until exit. The first call on a device resolves the scratch
+ * address; make it before any stream capture. All calls share the scratch:
+ * calls whose GPU work overlaps (other streams, handles or threads) race. */
+int ps_solve3d_device_noalloc(ps_solver *h, const double *bx, const double *by, const double *bz,
+                              double *ax, double *ay, double *az);
+
 /* The public member `std::vector<class_partition> partition`
  * (poisson_solver.hpp:102, class_partition.hpp:29-43): one GPU holds the
  * whole grid, so there is exactly one partition: ncell = the grid, icell = 0. */

@@ -54,6 +54,7 @@ SIGNATURES = {
     "ps_push_device": (_i, [_vp, _dp, _dp, _dp]),
     "ps_pull_device": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "ps_solve3d_device": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "ps_solve3d_device_noalloc": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "ps_partition_count": (_i, [_vp]),
     "ps_partition": (_i, [_vp, _i, _ip, _ip, ctypes.POINTER(ctypes.c_double)]),
     "ps_setup2d": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_double), _i]),

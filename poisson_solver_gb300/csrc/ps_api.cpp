@@ -119,6 +119,14 @@ int ps_solve3d_device(ps_solver *h, const double *bx, const double *by, const do
     return guarded(h, [&](ps::Solver &s) { s.solve(B, A); });
 }
 
+int ps_solve3d_device_noalloc(ps_solver *h, const double *bx, const double *by, const double *bz,
+                              double *ax, double *ay, double *az)
+{
+    const double *B[3] = {bx, by, bz};
+    double *A[3] = {ax, ay, az};
+    return guarded(h, [&](ps::Solver &s) { ps::solve_noalloc(s, B, A); });
+}
+
 int ps_partition_count(const ps_solver *h) { return (h && h->s.is_setup) ? 1 : 0; }
 
 int ps_partition(const ps_solver *h, int index, int ncell[3], int icell[3], double dx[3])

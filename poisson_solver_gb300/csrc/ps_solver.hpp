@@ -103,4 +103,7 @@ private:
     size_t work_elems() const { return (size_t)n[2] * P[1] * Mx; }
 };
 
+// The FP64 solve in fixed, library-owned device memory (ps_noalloc.cu).
+int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3]);
+
 }  // namespace ps
