@@ -196,37 +196,64 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *x)
 // would force a local-memory copy of the whole parameter block).
 struct StageInfo {
     int4 st[MAX_STAGES];  // radix, m, twiddle offset, generic-table offset
+    int lm[MAX_STAGES];   // log2(m) or -1
 };
 
 __device__ __forceinline__ void load_stages(StageInfo &si, const FftPlanDev &P)
 {
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int i = 0; i < MAX_STAGES; ++i) si.st[i] = make_int4(P.radix[i], P.m[i], P.tw[i], P.gw[i]);
+        for (int i = 0; i < MAX_STAGES; ++i) {
+            si.st[i] = make_int4(P.radix[i], P.m[i], P.tw[i], P.gw[i]);
+            si.lm[i] = P.lm[i];
+        }
+    }
+}
+
+// Copy the plan's twiddle table to shared memory and point the plan at it
+// (the caller synchronises before the first stage).
+template <typename C> __device__ __forceinline__ void stage_twiddles(FftPlanDev &P, C *TW)
+{
+    const C *g = reinterpret_cast<const C *>(P.table);
+    for (int i = threadIdx.x; i < P.ntw; i += blockDim.x) TW[i] = __ldg(&g[i]);
+    P.table = TW;
+}
+
+// j = bf mod m and q = bf / m, by shifts when m is a power of two
+__device__ __forceinline__ void split_index(int bf, int m, int lm, int &j, int &q)
+{
+    if (lm >= 0) {
+        j = bf & (m - 1);
+        q = bf >> lm;
+    } else {
+        q = bf / m;
+        j = bf - q * m;
     }
 }
 
 // One in-place Stockham stage with a compile-time radix.
-template <typename C> struct ElemMax { static constexpr int value = sizeof(C) == 16 ? e_max(PREC_FP64) : e_max(PREC_FP32); };
-
-template <int R, bool INV, typename C>
-__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const FftPlanDev &P, int4 sd)
+template <int EM, int R, bool INV, typename C>
+__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const FftPlanDev &P, int4 sd, int lm)
 {
-    constexpr int U = ElemMax<C>::value / R;
+    constexpr int U = EM / R;
     const int L = P.L, m = sd.y, nbf = L / R, tpl = P.tpl;
-    const C *tw = reinterpret_cast<const C *>(P.table) + sd.z;
+    const C *tw = reinterpret_cast<const C *>(P.table) + sd.z;  // shared-memory copy
+    C *Sb = S + b * sb;
+    const int rstride = nbf * sn;
     C v[U][R];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int bf = t + u * tpl;
         if (bf < nbf) {
-            const int j = bf % m;
+            int j, q;
+            split_index(bf, m, lm, j, q);
+            const C *src = Sb + bf * sn;
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[u][r] = S[(bf + r * nbf) * sn + b * sb];
+            for (int r = 0; r < R; ++r) v[u][r] = src[r * rstride];
             if (m > 1) {
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    const C w = __ldg(&tw[j * (R - 1) + r - 1]);
+                    const C w = tw[j * (R - 1) + r - 1];
                     v[u][r] = INV ? cmulc(v[u][r], w) : cmul(v[u][r], w);
                 }
             }
@@ -238,10 +265,12 @@ __device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const 
     for (int u = 0; u < U; ++u) {
         const int bf = t + u * tpl;
         if (bf < nbf) {
-            const int j = bf % m, q = bf / m;
-            const int base = q * R * m + j;
+            int j, q;
+            split_index(bf, m, lm, j, q);
+            C *dst = Sb + (q * R * m + j) * sn;
+            const int mstride = m * sn;
 #pragma unroll
-            for (int r = 0; r < R; ++r) S[(base + r * m) * sn + b * sb] = v[u][r];
+            for (int r = 0; r < R; ++r) dst[r * mstride] = v[u][r];
         }
     }
     __syncthreads();
@@ -262,10 +291,10 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
             for (int r = 0; r < R; ++r) {
                 C x = S[(bf + r * nbf) * sn + b * sb];
                 if (m > 1 && r > 0) {
-                    const C w = __ldg(&tw[j * (R - 1) + r - 1]);
+                    const C w = tw[j * (R - 1) + r - 1];
                     x = INV ? cmulc(x, w) : cmul(x, w);
                 }
-                const C g = __ldg(&gw[(r * k) % R]);
+                const C g = gw[(r * k) % R];
                 acc = cadd(acc, INV ? cmulc(x, g) : cmul(x, g));
             }
             W[(base + k * m) * sn + b * sb] = acc;
@@ -283,7 +312,8 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
 // Full transform of the CTA's lines. Threads with t >= tpl (never the case
 // with the launch shapes used) would idle through the barriers.
 // Full transform of the CTA's lines, for ncomp line sets cstride elements
-// apart. The plan orders its stages as prime radices above 7, then 7s, 5s,
+// apart. EM is the register elements a thread holds per stage (and the
+// largest radix); the plan's threads-per-line was computed for the same EM. The plan orders its stages as prime radices above 7, then 7s, 5s,
 // 3s, 16s (FP32 only), 8s, and at most one 4 or 2; each radix runs in its own
 // loop, with the line sets innermost, so that the register arrays of
 // different radices never share a live range (a radix switch inside one
@@ -292,7 +322,7 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
 // Radices without an unrolled butterfly: primes above 7 (11 and 13 included).
 __device__ __forceinline__ bool is_generic_radix(int R) { return R > 8 && R != 16; }
 
-template <bool INV, typename C>
+template <bool INV, int EM, typename C>
 __device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
                                           const StageInfo &si, int ncomp = 1, int cstride = 0)
 {
@@ -301,22 +331,22 @@ __device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int
     for (; s < ns && is_generic_radix(si.st[s].x); ++s)
         for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, si.st[s]);
     for (; s < ns && si.st[s].x == 7; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<7, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 7, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
     for (; s < ns && si.st[s].x == 5; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<5, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 5, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
     for (; s < ns && si.st[s].x == 3; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<3, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
-    if constexpr (ElemMax<C>::value >= 16)
+        for (int c = 0; c < ncomp; ++c) stage<EM, 3, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+    if constexpr (EM >= 16)
         for (; s < ns && si.st[s].x == 16; ++s)
-            for (int c = 0; c < ncomp; ++c) stage<16, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+            for (int c = 0; c < ncomp; ++c) stage<EM, 16, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
     for (; s < ns && si.st[s].x == 8; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<8, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 8, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
     if (s < ns && si.st[s].x == 4) {
-        for (int c = 0; c < ncomp; ++c) stage<4, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 4, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
         ++s;
     }
     if (s < ns && si.st[s].x == 2) {
-        for (int c = 0; c < ncomp; ++c) stage<2, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
         ++s;
     }
 }

@@ -16,6 +16,10 @@ template <typename T> struct Cplx { using type = typename CxT<T>::type; };
 
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 
+// element budget per thread: x and y passes, and the fused z pass
+template <typename T> constexpr int EMX = e_max(sizeof(T) == 8 ? PREC_FP64 : PREC_FP32);
+template <typename T> constexpr int EMZ = e_max_z(sizeof(T) == 8 ? PREC_FP64 : PREC_FP32);
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -30,6 +34,8 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     C *S = reinterpret_cast<C *>(smem_raw);
     const int B = a.B, L = a.L, ld = L + 1;
     C *W = a.plan.generic ? S + B * ld : nullptr;
+    FftPlanDev plan = a.plan;
+    stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
     const int comp = blockIdx.y;
@@ -41,8 +47,16 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
 
     // load (zero-fill n >= n_in and rows past the end)
     T *Sr = reinterpret_cast<T *>(S);
+    const int lL = (L & (L - 1)) == 0 ? __ffs(L) - 1 : -1;
     for (int idx = tid; idx < 2 * B * L; idx += nt) {
-        const int rl = idx / L, n = idx - rl * L;
+        int rl, n;
+        if (lL >= 0) {
+            rl = idx >> lL;
+            n = idx & (L - 1);
+        } else {
+            rl = idx / L;
+            n = idx - rl * L;
+        }
         const long long r = row0 + rl;
         double v = 0.0;
         if (n < a.n_in && r < rows) {
@@ -57,7 +71,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
         Sr[2 * ((rl >> 1) * ld + n) + (rl & 1)] = (T)v;
     }
     __syncthreads();
-    fft_lines<false>(S, W, 1, ld, tid % B, tid / B, a.plan, si);
+    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, tid / B, plan, si);
 
     // separate the two half spectra and store
     const int Mx = a.Mx;
@@ -92,6 +106,8 @@ __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
     const int B = a.B, L = a.L;
     C *W = a.plan.generic ? S + L * B : nullptr;
     const int lb = __ffs(B) - 1;
+    FftPlanDev plan = a.plan;
+    stage_twiddles(plan, S + L * B * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
     const int comp = blockIdx.z;
@@ -100,30 +116,39 @@ __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
     C *base = reinterpret_cast<C *>(pick3(a.data, comp)) + (long long)blockIdx.y * a.outer_stride + x0;
     const int nt = blockDim.x, tid = threadIdx.x;
 
-    for (int idx = tid; idx < L * B; idx += nt) {
-        const int n = idx >> lb, b = idx & (B - 1);
-        C v = C{0, 0};
-        if (n < a.n_in && b < nb) v = base[n * a.axis_stride + b];
-        S[idx] = v;
+    // each thread keeps one column b and walks rows n = t, t + nt/B, ...
+    const int b = tid & (B - 1), t = tid >> lb, rstep = nt >> lb;
+    const long long gstep = (long long)rstep * a.axis_stride;
+    {
+        const C *src = base + (long long)t * a.axis_stride + b;
+        const int n_in = b < nb ? a.n_in : 0;
+#pragma unroll 4
+        for (int n = t; n < L; n += rstep, src += gstep) {
+            C v = C{0, 0};
+            if (n < n_in) v = *src;
+            S[n * B + b] = v;
+        }
     }
     __syncthreads();
-    fft_lines<INV>(S, W, B, 1, tid & (B - 1), tid >> lb, a.plan, si);
-    for (int idx = tid; idx < a.n_out * B; idx += nt) {
-        const int n = idx >> lb, b = idx & (B - 1);
-        if (b < nb) base[n * a.axis_stride + b] = S[idx];
+    fft_lines<INV, EMX<T>>(S, W, B, 1, b, t, plan, si);
+    if (b < nb) {
+        C *dst = base + (long long)t * a.axis_stride + b;
+#pragma unroll 4
+        for (int n = t; n < a.n_out; n += rstep, dst += gstep) *dst = S[n * B + b];
     }
 }
 
 // ---------------------------------------------------------------------------
 // Fused z pass.
 template <typename T>
-__device__ __forceinline__ T wavenumber(int k, int P, double c, bool derivative)
+__device__ __forceinline__ T wavenumber(int k, int P, T c, bool derivative)
 {
     // k in [0, P): signed index wrapped at P/2; the derivative drops the
     // unpaired Nyquist mode (its Hermitian part vanishes in the real output).
+    // Computed in the pass precision (FP64 arithmetic is slow on this GPU).
     const int m = (2 * k < P) ? k : k - P;
     if (derivative && 2 * k == P) return (T)0;
-    return (T)((double)m * c);
+    return (T)m * c;
 }
 
 template <typename T, int OP>
@@ -142,34 +167,41 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
     const long long off = (long long)ky * a.row_stride + x0;
     const int nt = blockDim.x, tid = threadIdx.x;
     const int b = tid & (B - 1), t = tid >> lb;
+    FftPlanDev plan = a.plan;
+    stage_twiddles(plan, S + (nbuf + (a.plan.generic ? 1 : 0)) * LB);
     __shared__ StageInfo si;
     load_stages(si, a.plan);
 
+    const int rstep = nt >> lb;
+    const long long gstep = (long long)rstep * a.axis_stride;
+    const int n_in = b < nb ? a.n_in : 0;
     for (int c = 0; c < a.nin; ++c) {
-        const C *src = reinterpret_cast<const C *>(pick3(a.in, c)) + off;
-        C *buf = S + c * LB;
-        for (int idx = tid; idx < LB; idx += nt) {
-            const int n = idx >> lb, bb = idx & (B - 1);
+        const C *src = reinterpret_cast<const C *>(pick3(a.in, c)) + off + (long long)t * a.axis_stride + b;
+        C *buf = S + c * LB + b;
+#pragma unroll 4
+        for (int n = t; n < L; n += rstep, src += gstep) {
             C v = C{0, 0};
-            if (n < a.n_in && bb < nb) v = src[n * a.axis_stride + bb];
-            buf[idx] = v;
+            if (n < n_in) v = *src;
+            buf[n * B] = v;
         }
     }
     __syncthreads();
-    fft_lines<false>(S, W, B, 1, b, t, a.plan, si, a.nin, LB);
+    fft_lines<false, EMZ<T>>(S, W, B, 1, b, t, plan, si, a.nin, LB);
 
     if constexpr (OP != OP_FORWARD) {
-        const T *K = reinterpret_cast<const T *>(a.kern);
+        // the thread's column kx is fixed; it walks kz = t, t + nt/B, ...
         const int oy = imin(ky, a.Py - ky);
-        const T kyv = wavenumber<T>(ky, a.Py, a.kyc, true);
-        for (int idx = tid; idx < LB; idx += nt) {
-            const int n = idx >> lb, bb = idx & (B - 1);
-            const int kx = x0 + bb;
-            if (bb >= nb) continue;
+        const int kx = x0 + b;
+        const T *Kc = reinterpret_cast<const T *>(a.kern) + (long long)oy * a.Mx + kx;
+        const long long kzs = (long long)a.oct_y * a.Mx;
+        const T kyv = wavenumber<T>(ky, a.Py, (T)a.kyc, true);
+        const T kxv = wavenumber<T>(kx, a.Px, (T)a.kxc, true);
+        const T kzc = (T)a.kzc;
+        for (int n = t; n < (b < nb ? L : 0); n += rstep) {
+            const int idx = n * B + b;
             const int oz = imin(n, a.Pz - n);
-            const T g = K[((long long)oz * a.oct_y + oy) * a.Mx + kx];
-            const T kxv = wavenumber<T>(kx, a.Px, a.kxc, true);
-            const T kzv = wavenumber<T>(n, a.Pz, a.kzc, true);
+            const T g = Kc[oz * kzs];
+            const T kzv = wavenumber<T>(n, a.Pz, kzc, true);
             if constexpr (OP == OP_NONE) {
                 for (int c = 0; c < a.nin; ++c) S[c * LB + idx] = cscale(S[c * LB + idx], g);
             } else if constexpr (OP == OP_GRAD) {
@@ -194,15 +226,14 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
                 S[LB + idx] = C{-g * c1.y, g * c1.x};
                 S[2 * LB + idx] = C{-g * c2.y, g * c2.x};
             } else if constexpr (OP == OP_FILTER) {
-                const T *Z = reinterpret_cast<const T *>(a.zeta);
-                const T z = Z[((long long)oz * a.oct_y + oy) * a.Mx + kx];
+                const T z = (reinterpret_cast<const T *>(a.zeta) + (long long)oy * a.Mx + kx)[oz * kzs];
                 if (a.reproject && a.nin == 3) {
                     // r'_c = z r_c - K sum_d k_c k_d r_d. A product k_c k_d is
                     // even under k -> -k (and survives in the real output)
                     // unless exactly one of the two axes sits on its Nyquist
                     // mode, where the unpaired wavenumber makes it odd.
-                    const T kf[3] = {wavenumber<T>(kx, a.Px, a.kxc, false), wavenumber<T>(ky, a.Py, a.kyc, false),
-                                     wavenumber<T>(n, a.Pz, a.kzc, false)};
+                    const T kf[3] = {wavenumber<T>(kx, a.Px, (T)a.kxc, false),
+                                     wavenumber<T>(ky, a.Py, (T)a.kyc, false), wavenumber<T>(n, a.Pz, kzc, false)};
                     const bool nq[3] = {2 * kx == a.Px, 2 * ky == a.Py, 2 * n == a.Pz};
                     const C in3[3] = {S[idx], S[LB + idx], S[2 * LB + idx]};
 #pragma unroll
@@ -222,17 +253,17 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
             }
         }
         __syncthreads();
-        fft_lines<true>(S, W, B, 1, b, t, a.plan, si, a.nout, LB);
+        fft_lines<true, EMZ<T>>(S, W, B, 1, b, t, plan, si, a.nout, LB);
     }
 
-    for (int c = 0; c < a.nout; ++c) {
-        C *dst0 = reinterpret_cast<C *>(pick3(a.out, c));
-        if (dst0 == nullptr) continue;
-        C *dst = dst0 + off;
-        const C *buf = S + c * LB;
-        for (int idx = tid; idx < a.n_out * B; idx += nt) {
-            const int n = idx >> lb, bb = idx & (B - 1);
-            if (bb < nb) dst[n * a.axis_stride + bb] = buf[idx];
+    if (b < nb) {
+        for (int c = 0; c < a.nout; ++c) {
+            C *dst0 = reinterpret_cast<C *>(pick3(a.out, c));
+            if (dst0 == nullptr) continue;
+            C *dst = dst0 + off + (long long)t * a.axis_stride + b;
+            const C *buf = S + c * LB + b;
+#pragma unroll 4
+            for (int n = t; n < a.n_out; n += rstep, dst += gstep) *dst = buf[n * B];
         }
     }
 }
@@ -249,6 +280,8 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
     C *S = reinterpret_cast<C *>(smem_raw);
     const int B = a.B, L = a.L, ld = L + 1, Mx = a.Mx;
     C *W = a.plan.generic ? S + B * ld : nullptr;
+    FftPlanDev plan = a.plan;
+    stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
     const int comp = blockIdx.y;
@@ -268,12 +301,20 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
         if (k >= 1 && k <= L - Mx) S[line * ld + L - k] = C{xa.x + xb.y, xb.x - xa.y};
     }
     __syncthreads();
-    fft_lines<true>(S, W, 1, ld, tid % B, tid / B, a.plan, si);
+    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, tid / B, plan, si);
 
     const T *Sr = reinterpret_cast<const T *>(S);
     const int no = a.n_out;
+    const int lno = (no & (no - 1)) == 0 ? __ffs(no) - 1 : -1;
     for (int idx = tid; idx < 2 * B * no; idx += nt) {
-        const int rl = idx / no, n = idx - rl * no;
+        int rl, n;
+        if (lno >= 0) {
+            rl = idx >> lno;
+            n = idx & (no - 1);
+        } else {
+            rl = idx / no;
+            n = idx - rl * no;
+        }
         const long long r = row0 + rl;
         if (r < rows) out[r * a.out_stride + n] = (double)Sr[2 * ((rl >> 1) * ld + n) + (rl & 1)];
     }
@@ -284,20 +325,20 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
 
 static int threads_for(const FftPlanDev &p, int B) { return B * p.tpl; }
 
-size_t smem_x(int prec, int L, int B, int generic)
+size_t smem_x(int prec, const FftPlanDev &p, int B)
 {
     const size_t c = prec == PREC_FP64 ? 16 : 8;
-    return c * (size_t)B * (L + 1) * (generic ? 2 : 1);
+    return c * ((size_t)B * (p.L + 1) * (p.generic ? 2 : 1) + p.ntw);
 }
-size_t smem_col(int prec, int L, int B, int generic)
+size_t smem_col(int prec, const FftPlanDev &p, int B)
 {
     const size_t c = prec == PREC_FP64 ? 16 : 8;
-    return c * (size_t)B * L * (generic ? 2 : 1);
+    return c * ((size_t)B * p.L * (p.generic ? 2 : 1) + p.ntw);
 }
-size_t smem_z(int prec, int L, int B, int nbuf, int generic)
+size_t smem_z(int prec, const FftPlanDev &p, int B, int nbuf)
 {
     const size_t c = prec == PREC_FP64 ? 16 : 8;
-    return c * (size_t)B * L * (nbuf + (generic ? 1 : 0));
+    return c * ((size_t)B * p.L * (nbuf + (p.generic ? 1 : 0)) + p.ntw);
 }
 
 int max_smem_per_block()
@@ -320,7 +361,7 @@ cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st)
     const long long lines = (rows + 1) / 2;
     dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
     const int nt = threads_for(a.plan, a.B);
-    const size_t sm = smem_x(prec, a.L, a.B, a.plan.generic);
+    const size_t sm = smem_x(prec, a.plan, a.B);
     cudaError_t e;
     if (prec == PREC_FP64) {
         if ((e = prep(k_xfwd<double>, sm)) != cudaSuccess) return e;
@@ -336,7 +377,7 @@ cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaS
 {
     dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), outer, a.ncomp);
     const int nt = threads_for(a.plan, a.B);
-    const size_t sm = smem_col(prec, a.L, a.B, a.plan.generic);
+    const size_t sm = smem_col(prec, a.plan, a.B);
     cudaError_t e;
 #define PS_LAUNCH_COL(T, I)                                         \
     do {                                                            \
@@ -379,7 +420,7 @@ cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st)
     dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), ny);
     const int nt = threads_for(a.plan, a.B);
     const int nbuf = a.nin > a.nout ? a.nin : a.nout;
-    const size_t sm = smem_z(prec, a.L, a.B, nbuf, a.plan.generic);
+    const size_t sm = smem_z(prec, a.plan, a.B, nbuf);
     return prec == PREC_FP64 ? launch_z_t<double>(a, grid, nt, sm, st) : launch_z_t<float>(a, grid, nt, sm, st);
 }
 
@@ -389,7 +430,7 @@ cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
     const long long lines = (rows + 1) / 2;
     dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
     const int nt = threads_for(a.plan, a.B);
-    const size_t sm = smem_x(prec, a.L, a.B, a.plan.generic);
+    const size_t sm = smem_x(prec, a.plan, a.B);
     cudaError_t e;
     if (prec == PREC_FP64) {
         if ((e = prep(k_xinv<double>, sm)) != cudaSuccess) return e;

@@ -1,0 +1,400 @@
+// Pass kernels specialised on power-of-two transform lengths (FP32 hot path):
+// the same five passes as ps_kernels.cu, built on the compile-time FFT core of
+// ps_fft_p2.cuh. The host uses them for FP32 and 64 <= L <= 2048 and falls
+// back to the run-time kernels otherwise (p2::supported).
+#include <cuda_runtime.h>
+
+#include "ps_fft_p2.cuh"
+#include "ps_types.hpp"
+
+namespace ps {
+namespace p2 {
+
+namespace {
+
+__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+
+template <typename C, int NTW> __device__ __forceinline__ void load_twiddles(C *TW, const void *table)
+{
+    const C *g = reinterpret_cast<const C *>(table);
+    for (int i = threadIdx.x; i < NTW; i += blockDim.x) TW[i] = __ldg(&g[i]);
+}
+
+template <typename T> __device__ __forceinline__ T wavenumber(int k, int P, T c, bool derivative)
+{
+    const int m = (2 * k < P) ? k : k - P;
+    if (derivative && 2 * k == P) return (T)0;
+    return (T)m * c;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// x forward: line l = rows 2l (re) and 2l+1 (im), then the two half spectra.
+template <typename T, int L, int EM>
+__global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+{
+    using C = typename CxT<T>::type;
+    using PL = Plan<L, EM>;
+    constexpr int LL = PL::LL, TPL = PL::TPL, LT = ilog2(TPL);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = line_pitch<C>(L, B);
+    C *TW = S + B * LDP;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int comp = blockIdx.y;
+    const double *in = pick3(a.in, comp);
+    C *out = reinterpret_cast<C *>(pick3(a.out, comp));
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long row0 = (long long)blockIdx.x * 2 * B;
+
+    T *Sr = reinterpret_cast<T *>(S);
+    for (int idx = tid; idx < 2 * B * L; idx += nt) {
+        const int rl = idx >> LL, n = idx & (L - 1);
+        const long long r = row0 + rl;
+        double v = 0.0;
+        if (n < a.n_in && r < rows) {
+            if (!a.mirror) {
+                v = in[r * a.in_stride + n];
+            } else {
+                const int j = (int)(r % a.rows_y), k = (int)(r / a.rows_y);
+                const int jj = imin(j, a.Py - j), kk = imin(k, a.Pz - k), nn = imin(n, L - n);
+                v = in[((long long)kk * a.oct_y + jj) * a.oct_x + nn];
+            }
+        }
+        Sr[2 * ((rl >> 1) * LDP + sk<C>(n)) + (rl & 1)] = (T)v;
+    }
+    __syncthreads();
+    run<L, EM, false>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+
+    constexpr int Mx = L / 2 + 1;
+    for (int idx = tid; idx < B * Mx; idx += nt) {
+        const int line = idx / Mx, k = idx - line * Mx;
+        const long long ra = row0 + 2 * line, rb = ra + 1;
+        if (ra >= rows) continue;
+        const C *ln = S + line * LDP;
+        const C z = ln[sk<C>(k)], w = ln[sk<C>((L - k) & (L - 1))];
+        const T h = (T)0.5;
+        const C xa = C{h * (z.x + w.x), h * (z.y - w.y)};
+        const C xb = C{h * (z.y + w.y), h * (w.x - z.x)};
+        out[((ra / a.rows_y) * a.out_y + ra % a.rows_y) * Mx + k] = xa;
+        if (rb < rows) out[((rb / a.rows_y) * a.out_y + rb % a.rows_y) * Mx + k] = xb;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Strided column transforms, in place.
+template <typename T, int L, int EM, bool INV>
+__global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
+{
+    using C = typename CxT<T>::type;
+    using PL = Plan<L, EM>;
+    constexpr int TPL = PL::TPL, LT = ilog2(TPL);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = line_pitch<C>(L, B);
+    C *TW = S + B * LDP;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int lb = __ffs(B) - 1;
+    const int x0 = blockIdx.x * B;
+    const int nb = imin(B, a.Mx - x0);
+    C *base = reinterpret_cast<C *>(pick3(a.data, blockIdx.z)) + (long long)blockIdx.y * a.outer_stride + x0;
+
+    // coalesced phases: lane -> (column bl, row nl); each thread moves EM rows,
+    // all of its loads in flight before the first shared-memory write
+    const int bl = tid & (B - 1), nl = tid >> lb, rstep = nt >> lb;
+    const long long gstep = (long long)rstep * a.axis_stride;
+    {
+        const C *src = base + (long long)nl * a.axis_stride + bl;
+        const int n_in = bl < nb ? a.n_in : 0;
+        C *dst = S + bl * LDP;
+        C v[EM];
+#pragma unroll
+        for (int i = 0; i < EM; ++i) {
+            const int n = nl + i * rstep;
+            v[i] = n < n_in ? src[i * gstep] : C{0, 0};
+        }
+#pragma unroll
+        for (int i = 0; i < EM; ++i) dst[sk<C>(nl + i * rstep)] = v[i];
+    }
+    __syncthreads();
+    run<L, EM, INV>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    if (bl < nb) {
+        C *dst = base + (long long)nl * a.axis_stride + bl;
+        const C *src = S + bl * LDP;
+#pragma unroll 4
+        for (int n = nl; n < a.n_out; n += rstep, dst += gstep) *dst = src[sk<C>(n)];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused z pass (operators none/grad/div/curl).
+template <typename T, int L, int EM, int OP>
+__global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
+{
+    using C = typename CxT<T>::type;
+    using PL = Plan<L, EM>;
+    constexpr int TPL = PL::TPL, LT = ilog2(TPL);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = line_pitch<C>(L, B), CS = B * LDP;
+    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
+    C *TW = S + nbuf * CS;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int lb = __ffs(B) - 1;
+    const int x0 = blockIdx.x * B;
+    const int ky = a.ky0 + blockIdx.y;
+    const int nb = imin(B, a.Mx - x0);
+    const long long off = (long long)ky * a.row_stride + x0;
+    const int bl = tid & (B - 1), nl = tid >> lb, rstep = nt >> lb;
+    const long long gstep = (long long)rstep * a.axis_stride;
+    const int n_in = bl < nb ? a.n_in : 0;
+
+    for (int c = 0; c < a.nin; ++c) {
+        // every thread moves EM rows of each component, a component's loads
+        // all in flight before its shared-memory writes
+        const C *src = reinterpret_cast<const C *>(pick3(a.in, c)) + off + (long long)nl * a.axis_stride + bl;
+        C *dst = S + c * CS + bl * LDP;
+        C v[EM];
+#pragma unroll
+        for (int i = 0; i < EM; ++i) {
+            const int n = nl + i * rstep;
+            v[i] = n < n_in ? src[i * gstep] : C{0, 0};
+        }
+#pragma unroll
+        for (int i = 0; i < EM; ++i) dst[sk<C>(nl + i * rstep)] = v[i];
+    }
+    __syncthreads();
+    C *myline = S + (tid >> LT) * LDP;
+    const int t = tid & (TPL - 1);
+    run<L, EM, false>(myline, TW, t, a.nin, CS);
+
+    {
+        const int oy = imin(ky, a.Py - ky);
+        const int kx = x0 + bl;
+        const T *Kc = reinterpret_cast<const T *>(a.kern) + (long long)oy * a.Mx + kx;
+        const long long kzs = (long long)a.oct_y * a.Mx;
+        const T kyv = wavenumber<T>(ky, a.Py, (T)a.kyc, true);
+        const T kxv = wavenumber<T>(kx, a.Px, (T)a.kxc, true);
+        const T kzc = (T)a.kzc;
+        C *S0 = S + bl * LDP, *S1 = S0 + CS, *S2 = S1 + CS;
+        for (int n = nl; n < (bl < nb ? L : 0); n += rstep) {
+            const int e = sk<C>(n);
+            const int oz = imin(n, a.Pz - n);
+            const T g = Kc[oz * kzs];
+            const T kzv = wavenumber<T>(n, a.Pz, kzc, true);
+            if constexpr (OP == OP_NONE) {
+                S0[e] = cscale(S0[e], g);
+                if (a.nin > 1) S1[e] = cscale(S1[e], g);
+                if (a.nin > 2) S2[e] = cscale(S2[e], g);
+            } else if constexpr (OP == OP_GRAD) {
+                const C i0 = S0[e];
+                const C i1 = a.nin > 1 ? S1[e] : i0;
+                const C i2 = a.nin > 2 ? S2[e] : i0;
+                const T gx = g * kxv, gy = g * kyv, gz = g * kzv;
+                S0[e] = C{-gx * i0.y, gx * i0.x};
+                S1[e] = C{-gy * i1.y, gy * i1.x};
+                S2[e] = C{-gz * i2.y, gz * i2.x};
+            } else if constexpr (OP == OP_DIV) {
+                const C i0 = S0[e], i1 = S1[e], i2 = S2[e];
+                const C s = C{kxv * i0.x + kyv * i1.x + kzv * i2.x, kxv * i0.y + kyv * i1.y + kzv * i2.y};
+                S0[e] = C{-g * s.y, g * s.x};
+            } else if constexpr (OP == OP_CURL) {
+                const C i0 = S0[e], i1 = S1[e], i2 = S2[e];
+                const C c0 = C{kyv * i2.x - kzv * i1.x, kyv * i2.y - kzv * i1.y};
+                const C c1 = C{kzv * i0.x - kxv * i2.x, kzv * i0.y - kxv * i2.y};
+                const C c2 = C{kxv * i1.x - kyv * i0.x, kxv * i1.y - kyv * i0.y};
+                S0[e] = C{-g * c0.y, g * c0.x};
+                S1[e] = C{-g * c1.y, g * c1.x};
+                S2[e] = C{-g * c2.y, g * c2.x};
+            }
+        }
+    }
+    __syncthreads();
+    run<L, EM, true>(myline, TW, t, a.nout, CS);
+
+    if (bl < nb) {
+        for (int c = 0; c < a.nout; ++c) {
+            C *dst0 = reinterpret_cast<C *>(pick3(a.out, c));
+            if (dst0 == nullptr) continue;
+            C *dst = dst0 + off + (long long)nl * a.axis_stride + bl;
+            const C *src = S + c * CS + bl * LDP;
+#pragma unroll 4
+            for (int n = nl; n < a.n_out; n += rstep, dst += gstep) *dst = src[sk<C>(n)];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// x inverse: half spectra of row pairs -> real rows, cropped.
+template <typename T, int L, int EM>
+__global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+{
+    using C = typename CxT<T>::type;
+    using PL = Plan<L, EM>;
+    constexpr int TPL = PL::TPL, LT = ilog2(TPL);
+    constexpr int Mx = L / 2 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = line_pitch<C>(L, B);
+    C *TW = S + B * LDP;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int comp = blockIdx.y;
+    const C *in = reinterpret_cast<const C *>(pick3(a.in, comp));
+    double *out = pick3(a.out, comp);
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long row0 = (long long)blockIdx.x * 2 * B;
+
+    for (int idx = tid; idx < B * Mx; idx += nt) {
+        const int line = idx / Mx, k = idx - line * Mx;
+        const long long ra = row0 + 2 * line, rb = ra + 1;
+        C xa = C{0, 0}, xb = C{0, 0};
+        if (ra < rows) xa = in[((ra / a.rows_y) * a.in_y + ra % a.rows_y) * Mx + k];
+        if (rb < rows) xb = in[((rb / a.rows_y) * a.in_y + rb % a.rows_y) * Mx + k];
+        C *ln = S + line * LDP;
+        ln[sk<C>(k)] = C{xa.x - xb.y, xa.y + xb.x};
+        if (k >= 1 && k <= L - Mx) ln[sk<C>(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
+    }
+    __syncthreads();
+    run<L, EM, true>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+
+    const T *Sr = reinterpret_cast<const T *>(S);
+    const int no = a.n_out;
+    for (int idx = tid; idx < 2 * B * no; idx += nt) {
+        const int rl = idx / no, n = idx - rl * no;
+        const long long r = row0 + rl;
+        if (r < rows) out[r * a.out_stride + n] = (double)Sr[2 * ((rl >> 1) * LDP + sk<C>(n)) + (rl & 1)];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+template <typename K> cudaError_t prep(K kernel, size_t smem)
+{
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+template <int L, int EM> constexpr size_t ntw() { return Plan<L, EM>::NTW; }
+
+#define PS_P2_LENGTHS(X) X(64) X(128) X(256) X(512) X(1024) X(2048)
+
+bool supported(int prec, int L) { return prec == PREC_FP32 && L >= 64 && L <= 2048 && (L & (L - 1)) == 0; }
+
+size_t smem_lines(int prec, int L, int B, int nbuf, int ntw_entries)
+{
+    const size_t c = prec == PREC_FP64 ? 16 : 8;
+    const int ldp = prec == PREC_FP64 ? line_pitch<double2>(L, B) : line_pitch<float2>(L, B);
+    return c * ((size_t)nbuf * B * ldp + ntw_entries);
+}
+
+cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st)
+{
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
+    const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);
+    const int nt = a.B * (a.L / e_max(PREC_FP32));
+    cudaError_t e;
+    switch (a.L) {
+#define X(LV)                                                                   \
+    case LV:                                                                    \
+        if ((e = prep(k_xfwd<float, LV, 16>, sm)) != cudaSuccess) return e;     \
+        k_xfwd<float, LV, 16><<<grid, nt, sm, st>>>(a);                         \
+        break;
+        PS_P2_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st)
+{
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), outer, a.ncomp);
+    const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);
+    const int nt = a.B * (a.L / e_max(PREC_FP32));
+    cudaError_t e;
+    switch (a.L) {
+#define X(LV)                                                                            \
+    case LV:                                                                             \
+        if (inverse) {                                                                   \
+            if ((e = prep(k_col<float, LV, 16, true>, sm)) != cudaSuccess) return e;     \
+            k_col<float, LV, 16, true><<<grid, nt, sm, st>>>(a);                         \
+        } else {                                                                         \
+            if ((e = prep(k_col<float, LV, 16, false>, sm)) != cudaSuccess) return e;    \
+            k_col<float, LV, 16, false><<<grid, nt, sm, st>>>(a);                        \
+        }                                                                                \
+        break;
+        PS_P2_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int L, int EM>
+cudaError_t launch_z_len(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    cudaError_t e;
+    switch (a.op) {
+#define Z(OPV)                                                                     \
+    case OPV:                                                                      \
+        if ((e = prep(k_z<float, L, EM, OPV>, sm)) != cudaSuccess) return e;       \
+        k_z<float, L, EM, OPV><<<grid, nt, sm, st>>>(a);                           \
+        break;
+        Z(OP_NONE)
+        Z(OP_GRAD)
+        Z(OP_DIV)
+        Z(OP_CURL)
+#undef Z
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+bool supports_op(int op) { return op == OP_NONE || op == OP_GRAD || op == OP_DIV || op == OP_CURL; }
+
+cudaError_t launch_z(const ZArgs &a, int ny, int em, cudaStream_t st)
+{
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), ny);
+    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
+    const size_t sm = smem_lines(PREC_FP32, a.L, a.B, nbuf, a.plan.ntw);
+    const int nt = a.B * (a.L / em);
+    switch (a.L) {
+#define X(LV)                                                                         \
+    case LV:                                                                          \
+        return em == 8 ? launch_z_len<LV, 8>(a, grid, nt, sm, st)                     \
+                       : launch_z_len<LV, 16>(a, grid, nt, sm, st);
+        PS_P2_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st)
+{
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
+    const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);
+    const int nt = a.B * (a.L / e_max(PREC_FP32));
+    cudaError_t e;
+    switch (a.L) {
+#define X(LV)                                                                   \
+    case LV:                                                                    \
+        if ((e = prep(k_xinv<float, LV, 16>, sm)) != cudaSuccess) return e;     \
+        k_xinv<float, LV, 16><<<grid, nt, sm, st>>>(a);                         \
+        break;
+        PS_P2_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace p2
+}  // namespace ps

@@ -133,6 +133,7 @@ void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_t
         const int R = rad[s];
         d.radix[s] = R;
         d.m[s] = m;
+        d.lm[s] = (m & (m - 1)) == 0 ? __builtin_ctz((unsigned)m) : -1;
         d.tw[s] = (int)(used - base);
         for (int j = 0; j < m; ++j)
             for (int r = 1; r < R; ++r) put(root((long long)j * r, (long long)m * R));
@@ -153,6 +154,7 @@ void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_t
     }
     if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length too large");
     d.tpl = tpl;
+    d.ntw = (int)(used - base);
     d.table = dev_table + base;
 }
 
@@ -231,7 +233,7 @@ int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
     xa.out_y = P[1];
     xa.Mx = Mx;
     xa.plan = px;
-    xa.B = lines_per_cta(px.tpl, [&](int B) { return smem_x(prec, P[0], B, px.generic); });
+    xa.B = lines_per_cta(px.tpl, [&](int B) { return smem_x(prec, px, B); });
     PS_NA_CK(launch_xfwd(prec, xa, s.stream));
 
     ColArgs ya{};
@@ -244,7 +246,7 @@ int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
     ya.axis_stride = Mx;
     ya.outer_stride = (long long)P[1] * Mx;
     ya.plan = py;
-    ya.B = lines_per_cta(py.tpl, [&](int B) { return smem_col(prec, P[1], B, py.generic); });
+    ya.B = lines_per_cta(py.tpl, [&](int B) { return smem_col(prec, py, B); });
     PS_NA_CK(launch_col(prec, 0, ya, n[2], s.stream));
 
     ZArgs za{};
@@ -288,7 +290,7 @@ int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
     za.kzc = 2.0 * M_PI / ((double)P[2] * s.dx[2]);
     za.plan = pz;
     const int nbuf = za.nin > za.nout ? za.nin : za.nout;
-    za.B = lines_per_cta(pz.tpl, [&](int B) { return smem_z(prec, P[2], B, nbuf, pz.generic); });
+    za.B = lines_per_cta(pz.tpl, [&](int B) { return smem_z(prec, pz, B, nbuf); });
     PS_NA_CK(launch_z(prec, za, P[1], s.stream));
 
     if (write_mask) {

@@ -60,7 +60,7 @@ struct Solver {
     int produced = 0;  // component mask of fa from the last solve
     int rhs_ready = 0; // fr holds the returned right-hand side of the pushed fb
 
-    std::map<std::pair<int, int>, std::unique_ptr<Plan>> plans;  // (length, precision)
+    std::map<std::pair<int, int>, std::unique_ptr<Plan>> plans;  // (length, precision * 64 + element budget)
 
     // Optional per-pass timing: one set of boundary events per timed solve.
     static constexpr int NPASS = 5;
@@ -92,7 +92,7 @@ struct Solver {
     size_t device_bytes() const;
     void copy_kernel(double *host, long long capacity) const;
 
-    const Plan &plan(int L, int prec);
+    const Plan &plan(int L, int prec, int emax = 0);  // emax 0: e_max(prec)
     void ensure_kernel(int prec);
     void ensure_zeta(int prec);
 

@@ -11,8 +11,11 @@ constexpr int MAX_THREADS = 512;  // CTA size bound of the pass kernels (<= 128 
 enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
 
 // Register elements a thread holds per FFT stage, which also caps the radix:
-// 8 complex doubles (radix <= 8) or 16 complex floats (radix <= 16).
-constexpr int e_max(int prec) { return prec == PREC_FP64 ? 8 : 16; }
+// 8 complex doubles (radix <= 8) or 16 complex floats (radix <= 16). The
+// fused z pass holds three components in shared memory, so its FP32 variant
+// uses 8 to double the threads per line at the same footprint.
+__host__ __device__ constexpr int e_max(int prec) { return prec == PREC_FP64 ? 8 : 16; }
+__host__ __device__ constexpr int e_max_z(int prec) { return 8; }
 
 // One 1D transform length as the kernels see it (see ps_fft.cuh).
 struct FftPlanDev {
@@ -24,7 +27,9 @@ struct FftPlanDev {
     int m[MAX_STAGES];
     int tw[MAX_STAGES];
     int gw[MAX_STAGES];
-    const void *table;  // complex twiddles in the pass precision
+    int lm[MAX_STAGES];  // log2(m) when m is a power of two, else -1
+    int ntw;             // complex entries in the table
+    const void *table;   // complex twiddles in the pass precision (copied to shared memory per CTA)
 };
 
 // Spectral operation of the fused z pass.
@@ -111,11 +116,23 @@ cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaS
 cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st);
 cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st);
 
-// Shared-memory bytes each pass needs for a given line count.
-size_t smem_x(int prec, int L, int B, int generic);
-size_t smem_col(int prec, int L, int B, int generic);
-size_t smem_z(int prec, int L, int B, int nbuf, int generic);
+// Shared-memory bytes each pass needs for a given line count (data, scratch
+// for direct-DFT stages, twiddle table).
+size_t smem_x(int prec, const FftPlanDev &p, int B);
+size_t smem_col(int prec, const FftPlanDev &p, int B);
+size_t smem_z(int prec, const FftPlanDev &p, int B, int nbuf);
 int max_smem_per_block();
+
+// Power-of-two specialised passes (ps_kernels_p2.cu): FP32, 64 <= L <= 2048.
+namespace p2 {
+bool supported(int prec, int L);
+bool supports_op(int op);
+size_t smem_lines(int prec, int L, int B, int nbuf, int ntw_entries);
+cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st);
+cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st);
+cudaError_t launch_z(const ZArgs &a, int ny, int em, cudaStream_t st);
+cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st);
+}  // namespace p2
 
 // Kernel-build helpers (ps_greens.cu), all FP64.
 cudaError_t launch_sample_unbounded3d(double *oct, const int oext[3], const int P[3], const double dx[3],
