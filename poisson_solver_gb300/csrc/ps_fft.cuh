@@ -179,6 +179,34 @@ template <bool INV, typename C> __device__ __forceinline__ void dft7(C *x)
     dft_odd<INV, 7>(x, c, s);
 }
 
+// 32 = 2 x 16: X[k] = E[k] + w32^k O[k], X[k+16] = E[k] - w32^k O[k].
+template <bool INV, typename C> __device__ __forceinline__ void dft32(C *x)
+{
+    using S = decltype(x[0].x);
+    C e[16], o[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        e[i] = x[2 * i];
+        o[i] = x[2 * i + 1];
+    }
+    dft16<INV>(e);
+    dft16<INV>(o);
+    const S c[8] = {(S)1.0, (S)0.98078528040323044913, (S)0.92387953251128675613, (S)0.83146961230254523708,
+                    (S)0.70710678118654752440, (S)0.55557023301960222474, (S)0.38268343236508977173,
+                    (S)0.19509032201612826785};
+#pragma unroll
+    for (int k = 1; k < 16; ++k) {
+        if (k < 8) o[k] = crot<INV>(o[k], c[k], c[8 - k]);
+        else if (k == 8) o[k] = rot<INV>(o[k]);
+        else o[k] = rot<INV>(crot<INV>(o[k], c[k - 8], c[16 - k]));
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        x[k] = cadd(e[k], o[k]);
+        x[k + 16] = csub(e[k], o[k]);
+    }
+}
+
 template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *x)
 {
     if constexpr (R == 2) dft2<INV>(x[0], x[1]);
@@ -188,6 +216,7 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *x)
     else if constexpr (R == 7) dft7<INV>(x);
     else if constexpr (R == 8) dft8<INV>(x);
     else if constexpr (R == 16) dft16<INV>(x);
+    else if constexpr (R == 32) dft32<INV>(x);
 }
 
 // ---------------------------------------------------------------------------

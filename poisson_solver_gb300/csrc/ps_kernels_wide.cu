@@ -1,0 +1,568 @@
+// Wide FP32 pass kernels for L = 256, 512, 1024, 2048: 32 elements per
+// thread, so a length-1024 line is two radix-32 stages. The first stage of
+// every transform reads its inputs straight from global memory into
+// registers (zero padding: rows past the data are never loaded) and the last
+// stage writes straight to global memory (crop: rows past the output are
+// never stored); shared memory carries only the exchanges between stages.
+// Relative to the length-specialised kernels this removes a shared-memory
+// round trip at each end of every transform.
+//
+// Shared layout: line-major, one pad slot per 32 elements (sk(n) = n + n/32),
+// lines `pitch` elements apart. The banks serve an 8-byte access one half-warp
+// at a time (16 lanes, 16 eight-byte banks), so each half-warp's 16 addresses
+// must fall in 16 different banks:
+//   column passes (y, z) are lane-fast over the B lines (a warp's global
+//     accesses are B adjacent columns of 32/B rows); a half-warp holds B lines
+//     x 16/B positions, conflict-free when pitch = 16/B (mod 16);
+//   row passes (x) are lane-fast along the line (global rows contiguous); a
+//     half-warp holds 16/TPL lines when TPL = L/32 < 16, conflict-free when
+//     pitch = TPL (mod 16).
+// A bank model of every stage's reads and writes (first-stage writes
+// n = 32t + r, later reads t + r NBF, writes r M + t) gives one wavefront per
+// half-warp for L = 256..2048 and B = 1..16 with these pitches.
+#include <cuda_runtime.h>
+
+#include "ps_fft_p2.cuh"
+#include "ps_types.hpp"
+
+namespace ps {
+namespace wide {
+
+using p2::ilog2;
+
+template <int L> using WP = p2::Plan<L, 32>;
+
+__device__ __forceinline__ int skw(int n) { return n + (n >> 5); }
+
+__host__ __device__ inline int pitch_to(int L, int target)
+{
+    const int base = L + L / 32;
+    return base + (((target - base) % 16) + 16) % 16;
+}
+// lines of a column pass (lane-fast over the B lines)
+__host__ __device__ inline int pitch_col(int L, int B) { return pitch_to(L, (16 / B) % 16); }
+// lines of a row pass (lane-fast along the line)
+__host__ __device__ inline int pitch_row(int L) { return pitch_to(L, (L / 32) % 16); }
+
+// Stage S of the length-L plan: butterfly bf = t + u TPL reads positions
+// bf + r NBF and writes (q R + r) M + j, j = bf mod M, q = bf / M.
+template <int L, int S> struct St {
+    using PL = WP<L>;
+    static constexpr int R = PL::radix(S), M = PL::mm(S), NBF = L / R, U = 32 / R, TPL = PL::TPL;
+    static constexpr int LM = ilog2(M), TWO = PL::tw(S);
+    static constexpr bool LAST = S == PL::NST - 1;
+    __device__ __forceinline__ static int in_pos(int t, int u, int r) { return t + u * TPL + r * NBF; }
+    __device__ __forceinline__ static int out_pos(int t, int u, int r)
+    {
+        const int bf = t + u * TPL;
+        return ((bf >> LM) * R + r) * M + (bf & (M - 1));
+    }
+};
+
+template <int L, int S, bool INV, typename C>
+__device__ __forceinline__ void twiddle_dft(C (&v)[St<L, S>::U][St<L, S>::R], const C *tws, int t)
+{
+    using T = St<L, S>;
+#pragma unroll
+    for (int u = 0; u < T::U; ++u) {
+        if constexpr (T::M > 1) {
+            const int j = (t + u * T::TPL) & (T::M - 1);
+            const C *w = tws + T::TWO + j * (T::R - 1);
+#pragma unroll
+            for (int r = 1; r < T::R; ++r) v[u][r] = INV ? cmulc(v[u][r], w[r - 1]) : cmul(v[u][r], w[r - 1]);
+        }
+        dft<T::R, INV>(v[u]);
+    }
+}
+
+template <int L, int S, typename C>
+__device__ __forceinline__ void read_line(const C *line, int t, C (&v)[St<L, S>::U][St<L, S>::R])
+{
+    using T = St<L, S>;
+#pragma unroll
+    for (int u = 0; u < T::U; ++u)
+#pragma unroll
+        for (int r = 0; r < T::R; ++r) v[u][r] = line[skw(T::in_pos(t, u, r))];
+}
+
+template <int L, int S, typename C>
+__device__ __forceinline__ void write_line(C *line, int t, const C (&v)[St<L, S>::U][St<L, S>::R])
+{
+    using T = St<L, S>;
+#pragma unroll
+    for (int u = 0; u < T::U; ++u)
+#pragma unroll
+        for (int r = 0; r < T::R; ++r) line[skw(T::out_pos(t, u, r))] = v[u][r];
+}
+
+// Shared-memory stages from S up to (excluding) the last, in place: read,
+// barrier, write, barrier. nsets line sets cstride elements apart.
+template <int L, int S, bool INV, typename C>
+__device__ __forceinline__ void middle_stages(C *line, const C *tws, int t, int nsets, int cstride)
+{
+    if constexpr (S < WP<L>::NST - 1) {
+        using T = St<L, S>;
+        for (int c = 0; c < nsets; ++c) {
+            C v[T::U][T::R];
+            read_line<L, S>(line + c * cstride, t, v);
+            twiddle_dft<L, S, INV>(v, tws, t);
+            __syncthreads();
+            write_line<L, S>(line + c * cstride, t, v);
+        }
+        __syncthreads();
+        middle_stages<L, S + 1, INV>(line, tws, t, nsets, cstride);
+    }
+}
+
+template <typename C, int NTW> __device__ __forceinline__ void load_twiddles(C *TW, const void *table)
+{
+    const C *g = reinterpret_cast<const C *>(table);
+    for (int i = threadIdx.x; i < NTW; i += blockDim.x) TW[i] = __ldg(&g[i]);
+}
+
+__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+
+template <typename T> __device__ __forceinline__ T wavenumber(int k, int P, T c, bool derivative)
+{
+    const int m = (2 * k < P) ? k : k - P;
+    if (derivative && 2 * k == P) return (T)0;
+    return (T)m * c;
+}
+
+// ---------------------------------------------------------------------------
+// y pass: strided columns, in place.
+template <int L, bool INV>
+__global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
+{
+    using C = float2;
+    using PL = WP<L>;
+    constexpr int LAST = PL::NST - 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = pitch_col(L, B);
+    C *TW = S + B * LDP;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int lb = __ffs(B) - 1;
+    const int b = threadIdx.x & (B - 1), t = threadIdx.x >> lb;
+    const int x0 = blockIdx.x * B;
+    const bool active = b < imin(B, a.Mx - x0);
+    C *col = reinterpret_cast<C *>(pick3(a.data, blockIdx.z)) + (long long)blockIdx.y * a.outer_stride + x0 + b;
+    const long long as = a.axis_stride;
+    C *line = S + b * LDP;
+
+    {   // first stage from global
+        using T0 = St<L, 0>;
+        C v[T0::U][T0::R];
+        const int n_in = active ? a.n_in : 0;
+#pragma unroll
+        for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+            for (int r = 0; r < T0::R; ++r) {
+                const int n = T0::in_pos(t, u, r);
+                v[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
+            }
+        twiddle_dft<L, 0, INV>(v, TW, t);
+        write_line<L, 0>(line, t, v);
+    }
+    __syncthreads();
+    middle_stages<L, 1, INV>(line, TW, t, 1, 0);
+    {   // last stage to global
+        using TL = St<L, LAST>;
+        C v[TL::U][TL::R];
+        read_line<L, LAST>(line, t, v);
+        twiddle_dft<L, LAST, INV>(v, TW, t);
+        if (active) {
+#pragma unroll
+            for (int u = 0; u < TL::U; ++u)
+#pragma unroll
+                for (int r = 0; r < TL::R; ++r) {
+                    const int n = TL::out_pos(t, u, r);
+                    if (n < a.n_out) col[n * as] = v[u][r];
+                }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused z pass.
+template <int L, int OP>
+__global__ void __launch_bounds__(Z_MAX_THREADS) k_z(const ZArgs a)
+{
+    using C = float2;
+    using T = float;
+    using PL = WP<L>;
+    constexpr int LAST = PL::NST - 1;
+    using TL = St<L, LAST>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = pitch_col(L, B), CS = B * LDP;
+    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
+    C *TW = S + nbuf * CS;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int lb = __ffs(B) - 1;
+    const int b = threadIdx.x & (B - 1), t = threadIdx.x >> lb;
+    const int x0 = blockIdx.x * B;
+    const int ky = a.ky0 + blockIdx.y;
+    const bool active = b < imin(B, a.Mx - x0);
+    const long long off = (long long)ky * a.row_stride + x0 + b;
+    const long long as = a.axis_stride;
+    C *line = S + b * LDP;
+
+    // forward: first stage of every input component from global
+    for (int c = 0; c < a.nin; ++c) {
+        using T0 = St<L, 0>;
+        const C *col = reinterpret_cast<const C *>(pick3(a.in, c)) + off;
+        C v[T0::U][T0::R];
+        const int n_in = active ? a.n_in : 0;
+#pragma unroll
+        for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+            for (int r = 0; r < T0::R; ++r) {
+                const int n = T0::in_pos(t, u, r);
+                v[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
+            }
+        twiddle_dft<L, 0, false>(v, TW, t);
+        write_line<L, 0>(line + c * CS, t, v);
+    }
+    __syncthreads();
+    middle_stages<L, 1, false>(line, TW, t, a.nin, CS);
+    // last forward stage: in place on the thread's own positions
+    for (int c = 0; c < a.nin; ++c) {
+        C v[TL::U][TL::R];
+        read_line<L, LAST>(line + c * CS, t, v);
+        twiddle_dft<L, LAST, false>(v, TW, t);
+        write_line<L, LAST>(line + c * CS, t, v);
+    }
+
+    // spectral operation on the positions this thread owns (no barrier:
+    // the same thread wrote them)
+    {
+        const int oy = imin(ky, a.Py - ky);
+        const int kx = x0 + b;
+        const T *Kc = reinterpret_cast<const T *>(a.kern) + (long long)oy * a.Mx + (active ? kx : 0);
+        const long long kzs = (long long)a.oct_y * a.Mx;
+        const T kyv = wavenumber<T>(ky, a.Py, (T)a.kyc, true);
+        const T kxv = wavenumber<T>(kx, a.Px, (T)a.kxc, true);
+        const T kzc = (T)a.kzc;
+        C *S0 = line, *S1 = line + CS, *S2 = line + 2 * CS;
+#pragma unroll 4
+        for (int i = 0; i < TL::U * TL::R; ++i) {
+            const int n = TL::out_pos(t, i / TL::R, i % TL::R);
+            const int e = skw(n);
+            const int oz = imin(n, a.Pz - n);
+            const T g = active ? Kc[oz * kzs] : (T)0;
+            const T kzv = wavenumber<T>(n, a.Pz, kzc, true);
+            if constexpr (OP == OP_NONE) {
+                S0[e] = cscale(S0[e], g);
+                if (a.nin > 1) S1[e] = cscale(S1[e], g);
+                if (a.nin > 2) S2[e] = cscale(S2[e], g);
+            } else if constexpr (OP == OP_GRAD) {
+                const C i0 = S0[e];
+                const C i1 = a.nin > 1 ? S1[e] : i0;
+                const C i2 = a.nin > 2 ? S2[e] : i0;
+                const T gx = g * kxv, gy = g * kyv, gz = g * kzv;
+                S0[e] = C{-gx * i0.y, gx * i0.x};
+                S1[e] = C{-gy * i1.y, gy * i1.x};
+                S2[e] = C{-gz * i2.y, gz * i2.x};
+            } else if constexpr (OP == OP_DIV) {
+                const C i0 = S0[e], i1 = S1[e], i2 = S2[e];
+                const C s = C{kxv * i0.x + kyv * i1.x + kzv * i2.x, kxv * i0.y + kyv * i1.y + kzv * i2.y};
+                S0[e] = C{-g * s.y, g * s.x};
+            } else if constexpr (OP == OP_CURL) {
+                const C i0 = S0[e], i1 = S1[e], i2 = S2[e];
+                const C c0 = C{kyv * i2.x - kzv * i1.x, kyv * i2.y - kzv * i1.y};
+                const C c1 = C{kzv * i0.x - kxv * i2.x, kzv * i0.y - kxv * i2.y};
+                const C c2 = C{kxv * i1.x - kyv * i0.x, kxv * i1.y - kyv * i0.y};
+                S0[e] = C{-g * c0.y, g * c0.x};
+                S1[e] = C{-g * c1.y, g * c1.x};
+                S2[e] = C{-g * c2.y, g * c2.x};
+            }
+        }
+    }
+    __syncthreads();
+
+    // inverse: first stage in place (read, barrier, write), middle stages,
+    // last stage to global
+    for (int c = 0; c < a.nout; ++c) {
+        using T0 = St<L, 0>;
+        C v[T0::U][T0::R];
+        read_line<L, 0>(line + c * CS, t, v);
+        twiddle_dft<L, 0, true>(v, TW, t);
+        __syncthreads();
+        write_line<L, 0>(line + c * CS, t, v);
+    }
+    __syncthreads();
+    middle_stages<L, 1, true>(line, TW, t, a.nout, CS);
+    for (int c = 0; c < a.nout; ++c) {
+        C *col0 = reinterpret_cast<C *>(pick3(a.out, c));
+        C v[TL::U][TL::R];
+        read_line<L, LAST>(line + c * CS, t, v);
+        twiddle_dft<L, LAST, true>(v, TW, t);
+        if (active && col0) {
+            C *col = col0 + off;
+#pragma unroll
+            for (int u = 0; u < TL::U; ++u)
+#pragma unroll
+                for (int r = 0; r < TL::R; ++r) {
+                    const int n = TL::out_pos(t, u, r);
+                    if (n < a.n_out) col[n * as] = v[u][r];
+                }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// x forward: threads run along the line; line l carries rows 2l and 2l+1.
+template <int L>
+__global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+{
+    using C = float2;
+    using PL = WP<L>;
+    constexpr int LAST = PL::NST - 1, TPL = PL::TPL, LT = ilog2(TPL);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = pitch_row(L);
+    C *TW = S + B * LDP;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int b = threadIdx.x >> LT, t = threadIdx.x & (TPL - 1);
+    const int comp = blockIdx.y;
+    const double *in = pick3(a.in, comp);
+    C *out = reinterpret_cast<C *>(pick3(a.out, comp));
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long ra = (long long)blockIdx.x * 2 * B + 2 * b, rb = ra + 1;
+    C *line = S + b * LDP;
+    {
+        using T0 = St<L, 0>;
+        C v[T0::U][T0::R];
+        const bool va = ra < rows, vb = rb < rows;
+        const int ja = (int)(ra % a.rows_y), ka = (int)(ra / a.rows_y);
+        const int jb = (int)(rb % a.rows_y), kb = (int)(rb / a.rows_y);
+#pragma unroll
+        for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+            for (int r = 0; r < T0::R; ++r) {
+                const int n = T0::in_pos(t, u, r);
+                double xa = 0.0, xb = 0.0;
+                if (n < a.n_in) {
+                    if (!a.mirror) {
+                        if (va) xa = in[ra * a.in_stride + n];
+                        if (vb) xb = in[rb * a.in_stride + n];
+                    } else {
+                        const int nn = imin(n, L - n);
+                        if (va)
+                            xa = in[((long long)imin(ka, a.Pz - ka) * a.oct_y + imin(ja, a.Py - ja)) * a.oct_x + nn];
+                        if (vb)
+                            xb = in[((long long)imin(kb, a.Pz - kb) * a.oct_y + imin(jb, a.Py - jb)) * a.oct_x + nn];
+                    }
+                }
+                v[u][r] = C{(float)xa, (float)xb};
+            }
+        twiddle_dft<L, 0, false>(v, TW, t);
+        write_line<L, 0>(line, t, v);
+    }
+    __syncthreads();
+    middle_stages<L, 1, false>(line, TW, t, 1, 0);
+    {
+        using TL = St<L, LAST>;
+        C v[TL::U][TL::R];
+        read_line<L, LAST>(line, t, v);
+        twiddle_dft<L, LAST, false>(v, TW, t);
+        write_line<L, LAST>(line, t, v);
+    }
+    __syncthreads();
+    // separate the half spectra of rows a and b
+    constexpr int Mx = L / 2 + 1;
+    const int nt = blockDim.x;
+    const long long row0 = (long long)blockIdx.x * 2 * B;
+    for (int idx = threadIdx.x; idx < B * Mx; idx += nt) {
+        const int l = idx / Mx, k = idx - l * Mx;
+        const long long r0 = row0 + 2 * l, r1 = r0 + 1;
+        if (r0 >= rows) continue;
+        const C *ln = S + l * LDP;
+        const C z = ln[skw(k)], w = ln[skw((L - k) & (L - 1))];
+        const C xa = C{0.5f * (z.x + w.x), 0.5f * (z.y - w.y)};
+        const C xb = C{0.5f * (z.y + w.y), 0.5f * (w.x - z.x)};
+        out[((r0 / a.rows_y) * a.out_y + r0 % a.rows_y) * Mx + k] = xa;
+        if (r1 < rows) out[((r1 / a.rows_y) * a.out_y + r1 % a.rows_y) * Mx + k] = xb;
+    }
+}
+
+// x inverse: rebuild Z = Xa + i Xb, transform back, Re -> row a, Im -> row b.
+template <int L>
+__global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+{
+    using C = float2;
+    using PL = WP<L>;
+    constexpr int LAST = PL::NST - 1, TPL = PL::TPL, LT = ilog2(TPL);
+    constexpr int Mx = L / 2 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *S = reinterpret_cast<C *>(smem_raw);
+    const int B = a.B, LDP = pitch_row(L);
+    C *TW = S + B * LDP;
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    const int comp = blockIdx.y;
+    const C *in = reinterpret_cast<const C *>(pick3(a.in, comp));
+    double *out = pick3(a.out, comp);
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    const long long row0 = (long long)blockIdx.x * 2 * B;
+    const int nt = blockDim.x;
+    for (int idx = threadIdx.x; idx < B * Mx; idx += nt) {
+        const int l = idx / Mx, k = idx - l * Mx;
+        const long long r0 = row0 + 2 * l, r1 = r0 + 1;
+        C xa = C{0.f, 0.f}, xb = C{0.f, 0.f};
+        if (r0 < rows) xa = in[((r0 / a.rows_y) * a.in_y + r0 % a.rows_y) * Mx + k];
+        if (r1 < rows) xb = in[((r1 / a.rows_y) * a.in_y + r1 % a.rows_y) * Mx + k];
+        C *ln = S + l * LDP;
+        ln[skw(k)] = C{xa.x - xb.y, xa.y + xb.x};
+        if (k >= 1 && k <= L - Mx) ln[skw(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
+    }
+    __syncthreads();
+    const int b = threadIdx.x >> LT, t = threadIdx.x & (TPL - 1);
+    C *line = S + b * LDP;
+    {
+        using T0 = St<L, 0>;
+        C v[T0::U][T0::R];
+        read_line<L, 0>(line, t, v);
+        twiddle_dft<L, 0, true>(v, TW, t);
+        __syncthreads();
+        write_line<L, 0>(line, t, v);
+    }
+    __syncthreads();
+    middle_stages<L, 1, true>(line, TW, t, 1, 0);
+    {
+        using TL = St<L, LAST>;
+        C v[TL::U][TL::R];
+        read_line<L, LAST>(line, t, v);
+        twiddle_dft<L, LAST, true>(v, TW, t);
+        const long long ra = row0 + 2 * b, rb = ra + 1;
+#pragma unroll
+        for (int u = 0; u < TL::U; ++u)
+#pragma unroll
+            for (int r = 0; r < TL::R; ++r) {
+                const int n = TL::out_pos(t, u, r);
+                if (n < a.n_out) {
+                    if (ra < rows) out[ra * a.out_stride + n] = (double)v[u][r].x;
+                    if (rb < rows) out[rb * a.out_stride + n] = (double)v[u][r].y;
+                }
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <typename K> cudaError_t prep(K kernel, size_t smem)
+{
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+#define PS_WIDE_LENGTHS(X) X(256) X(512) X(1024) X(2048)
+
+bool supported(int prec, int L) { return prec == PREC_FP32 && (L == 256 || L == 512 || L == 1024 || L == 2048); }
+
+size_t smem_lines(int L, int B, int nbuf, int ntw_entries, bool column)
+{
+    const int ldp = column ? pitch_col(L, B) : pitch_row(L);
+    return sizeof(float2) * ((size_t)nbuf * B * ldp + ntw_entries);
+}
+
+cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st)
+{
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
+    const size_t sm = smem_lines(a.L, a.B, 1, a.plan.ntw, false);
+    const int nt = a.B * (a.L / 32);
+    cudaError_t e;
+    switch (a.L) {
+#define X(LV)                                                            \
+    case LV:                                                             \
+        if ((e = prep(k_xfwd<LV>, sm)) != cudaSuccess) return e;         \
+        k_xfwd<LV><<<grid, nt, sm, st>>>(a);                             \
+        break;
+        PS_WIDE_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st)
+{
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), outer, a.ncomp);
+    const size_t sm = smem_lines(a.L, a.B, 1, a.plan.ntw, true);
+    const int nt = a.B * (a.L / 32);
+    cudaError_t e;
+    switch (a.L) {
+#define X(LV)                                                                      \
+    case LV:                                                                       \
+        if (inverse) {                                                             \
+            if ((e = prep(k_col<LV, true>, sm)) != cudaSuccess) return e;          \
+            k_col<LV, true><<<grid, nt, sm, st>>>(a);                              \
+        } else {                                                                   \
+            if ((e = prep(k_col<LV, false>, sm)) != cudaSuccess) return e;         \
+            k_col<LV, false><<<grid, nt, sm, st>>>(a);                             \
+        }                                                                          \
+        break;
+        PS_WIDE_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int L> cudaError_t launch_z_len(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    cudaError_t e;
+    switch (a.op) {
+#define Z(OPV)                                                           \
+    case OPV:                                                            \
+        if ((e = prep(k_z<L, OPV>, sm)) != cudaSuccess) return e;        \
+        k_z<L, OPV><<<grid, nt, sm, st>>>(a);                            \
+        break;
+        Z(OP_NONE)
+        Z(OP_GRAD)
+        Z(OP_DIV)
+        Z(OP_CURL)
+#undef Z
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_z(const ZArgs &a, int ny, cudaStream_t st)
+{
+    if (a.B * (a.L / 32) > Z_MAX_THREADS) return cudaErrorInvalidConfiguration;
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), ny);
+    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
+    const size_t sm = smem_lines(a.L, a.B, nbuf, a.plan.ntw, true);
+    const int nt = a.B * (a.L / 32);
+    switch (a.L) {
+#define X(LV) \
+    case LV: return launch_z_len<LV>(a, grid, nt, sm, st);
+        PS_WIDE_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st)
+{
+    const long long rows = (long long)a.rows_y * a.rows_z;
+    dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
+    const size_t sm = smem_lines(a.L, a.B, 1, a.plan.ntw, false);
+    const int nt = a.B * (a.L / 32);
+    cudaError_t e;
+    switch (a.L) {
+#define X(LV)                                                            \
+    case LV:                                                             \
+        if ((e = prep(k_xinv<LV>, sm)) != cudaSuccess) return e;         \
+        k_xinv<LV><<<grid, nt, sm, st>>>(a);                             \
+        break;
+        PS_WIDE_LENGTHS(X)
+#undef X
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace wide
+}  // namespace ps

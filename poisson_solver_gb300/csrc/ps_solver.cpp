@@ -92,6 +92,8 @@ static std::vector<int> factorize(int L, int max_radix)
     for (int p : {7, 5, 3})
         for (int q : odd)
             if (q == p) r.push_back(p);
+    if (max_radix >= 32)
+        while (p2 >= 5) { r.push_back(32); p2 -= 5; }
     if (max_radix >= 16)
         while (p2 >= 4) { r.push_back(16); p2 -= 4; }
     while (p2 >= 3) { r.push_back(8); p2 -= 3; }
@@ -100,7 +102,10 @@ static std::vector<int> factorize(int L, int max_radix)
     return r;
 }
 
-static bool fixed_radix(int R) { return R == 2 || R == 3 || R == 4 || R == 5 || R == 7 || R == 8 || R == 16; }
+static bool fixed_radix(int R)
+{
+    return R == 2 || R == 3 || R == 4 || R == 5 || R == 7 || R == 8 || R == 16 || R == 32;
+}
 
 // e^{-2 pi i e / N}, from the exactly reduced fraction e/N in extended precision
 static std::complex<long double> root(long long e, long long N)
@@ -171,7 +176,7 @@ const Plan &Solver::plan(int L, int prec, int emax)
 // environment variable `env`, e.g. PS_LINES_Z=4), halved until threads and
 // shared memory fit.
 static int pick_lines(int prec, int tpl, const std::function<size_t(int)> &smem, const char *env = nullptr,
-                      int pref = 0)
+                      int pref = 0, int max_threads = MAX_THREADS)
 {
     static int limit = 0;
     if (!limit) limit = max_smem_per_block() - 1024;  // room for the static stage table
@@ -180,8 +185,8 @@ static int pick_lines(int prec, int tpl, const std::function<size_t(int)> &smem,
         const int want = atoi(v);
         if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) B = want;
     }
-    while (B > 1 && (B * tpl > MAX_THREADS || smem(B) > (size_t)limit)) B >>= 1;
-    if (B * tpl > MAX_THREADS || smem(B) > (size_t)limit)
+    while (B > 1 && (B * tpl > max_threads || smem(B) > (size_t)limit)) B >>= 1;
+    if (B * tpl > max_threads || smem(B) > (size_t)limit)
         throw Error(PS_ERR_UNSUPPORTED, "transform length too large for one CTA");
     return B;
 }
@@ -446,15 +451,34 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     if (op == OP_FILTER) ensure_zeta(prec);
     for (int c = 0; c < 3; ++c)
         if ((in_mask | out_mask) >> c & 1) work[c].ensure(work_elems() * csz);
-    // FP32 with power-of-two lengths takes the length-specialised kernels
-    const bool p2x = p2::supported(prec, P[0]), p2y = p2::supported(prec, P[1]);
-    const bool p2z = p2::supported(prec, P[2]) && p2::supports_op(op);
+    // Kernel family per axis. FP32: the wide kernels for the y and z passes
+    // (lengths 256..2048), the length-specialised ones for x (measured faster
+    // there: 2.3 vs 3.4 ms for the 512^3 forward x pass) and for other
+    // power-of-two lengths 64..2048; the run-time kernels for the rest and
+    // for FP64. PS_KERNELS (all axes) or PS_KERNELS_X/_Y/_Z = wide, p2 or
+    // runtime override the choice.
+    auto family = [&](int axis, int L, bool op_ok) -> char {
+        static const char *names[3] = {"PS_KERNELS_X", "PS_KERNELS_Y", "PS_KERNELS_Z"};
+        const char *f = getenv(names[axis]);
+        if (!f) f = getenv("PS_KERNELS");
+        const bool force = f != nullptr;
+        const bool w_ok = wide::supported(prec, L) && op_ok, p_ok = p2::supported(prec, L) && op_ok;
+        if (force && strcmp(f, "runtime") == 0) return 'r';
+        if (force && strcmp(f, "p2") == 0) return p_ok ? 'p' : 'r';
+        if (force && strcmp(f, "wide") == 0) return w_ok ? 'w' : p_ok ? 'p' : 'r';
+        if (w_ok && axis > 0) return 'w';
+        return p_ok ? 'p' : 'r';
+    };
+    const char fx = family(0, P[0], true), fy = family(1, P[1], true), fz = family(2, P[2], p2::supports_op(op));
+    const bool wx = fx == 'w', wy = fy == 'w', wz = fz == 'w';
+    const bool p2x = fx == 'p', p2y = fy == 'p', p2z = fz == 'p';
     int emz = e_max_z(prec);
     if (p2z) {
         emz = 16;  // measured faster than 8 at 512^3 (13.4 vs 15.4 ms for the curl pass)
         if (const char *v = getenv("PS_Z_EM")) emz = atoi(v) == 8 ? 8 : 16;
     }
-    const Plan &px = plan(P[0], prec), &py = plan(P[1], prec), &pz = plan(P[2], prec, emz);
+    if (wz) emz = 32;
+    const Plan &px = plan(P[0], prec, wx ? 32 : 0), &py = plan(P[1], prec, wy ? 32 : 0), &pz = plan(P[2], prec, emz);
 
     std::array<cudaEvent_t, NPASS + 1> ev{};
     if (opt_timing) {
@@ -487,7 +511,11 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     xa.out_y = P[1];
     xa.Mx = Mx;
     xa.plan = px.dev;
-    if (p2x) {
+    if (wx) {
+        xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return wide::smem_lines(P[0], B, 1, px.dev.ntw, false); },
+                          "PS_LINES_X", 4);
+        PS_CK(wide::launch_xfwd(xa, stream));
+    } else if (p2x) {
         // two lines (four rows) per CTA measured fastest for the x passes
         xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[0], B, 1, px.dev.ntw); },
                           "PS_LINES_X", 2);
@@ -509,7 +537,11 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     ya.axis_stride = Mx;
     ya.outer_stride = (long long)P[1] * Mx;
     ya.plan = py.dev;
-    if (p2y) {
+    if (wy) {
+        ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return wide::smem_lines(P[1], B, 1, py.dev.ntw, true); },
+                          "PS_LINES_Y", 8);
+        PS_CK(wide::launch_col(0, ya, n[2], stream));
+    } else if (p2y) {
         ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[1], B, 1, py.dev.ntw); },
                           "PS_LINES_Y");
         PS_CK(p2::launch_col(0, ya, n[2], stream));
@@ -564,7 +596,11 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     za.kzc = 2.0 * M_PI / ((double)P[2] * dx[2]);
     za.plan = pz.dev;
     const int nbuf = std::max(za.nin, za.nout);
-    if (p2z) {
+    if (wz) {
+        za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return wide::smem_lines(P[2], B, nbuf, pz.dev.ntw, true); },
+                          "PS_LINES_Z", 8, wide::Z_MAX_THREADS);
+        PS_CK(wide::launch_z(za, P[1], stream));
+    } else if (p2z) {
         za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[2], B, nbuf, pz.dev.ntw); },
                           "PS_LINES_Z");
         PS_CK(p2::launch_z(za, P[1], emz, stream));
@@ -587,7 +623,8 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         yi.outer_stride = (long long)P[1] * Mx;
         yi.plan = py.dev;
         yi.B = ya.B;
-        if (p2y) PS_CK(p2::launch_col(1, yi, n[2], stream));
+        if (wy) PS_CK(wide::launch_col(1, yi, n[2], stream));
+        else if (p2y) PS_CK(p2::launch_col(1, yi, n[2], stream));
         else PS_CK(launch_col(prec, 1, yi, n[2], stream));
         mark(4);
 
@@ -607,7 +644,8 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         xi.out_stride = n[0];
         xi.plan = px.dev;
         xi.B = xa.B;
-        if (p2x) PS_CK(p2::launch_xinv(xi, stream));
+        if (wx) PS_CK(wide::launch_xinv(xi, stream));
+        else if (p2x) PS_CK(p2::launch_xinv(xi, stream));
         else PS_CK(launch_xinv(prec, xi, stream));
     } else {
         mark(4);

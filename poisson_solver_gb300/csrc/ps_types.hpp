@@ -134,6 +134,21 @@ cudaError_t launch_z(const ZArgs &a, int ny, int em, cudaStream_t st);
 cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st);
 }  // namespace p2
 
+// Wide passes (ps_kernels_wide.cu): FP32, L = 256, 512, 1024, 2048, 32
+// elements per thread, first and last stages fused with global memory.
+namespace wide {
+// threads per CTA of the fused z kernel: its 32-element stages need ~220
+// registers a thread
+constexpr int Z_MAX_THREADS = 256;
+bool supported(int prec, int L);
+// column = true for the y and z passes (lanes across lines), false for x
+size_t smem_lines(int L, int B, int nbuf, int ntw_entries, bool column);
+cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st);
+cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st);
+cudaError_t launch_z(const ZArgs &a, int ny, cudaStream_t st);
+cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st);
+}  // namespace wide
+
 // Kernel-build helpers (ps_greens.cu), all FP64.
 cudaError_t launch_sample_unbounded3d(double *oct, const int oext[3], const int P[3], const double dx[3],
                                       cudaStream_t st);
