@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mpts/s per solve, mixed-prec vs FP64 on GPU at ≤1e-6 rel L2; HBM GB/s"
 PASS_NAMES = ["x_forward", "y_forward", "z_fused", "y_inverse", "x_inverse"]
-KERNEL_NAMES = ["k_xfwd", "k_col<fwd>", "k_z<curl>", "k_col<inv>", "k_xinv"]
+KERNEL_NAMES = ["k_xfwd", "k_col<fwd>", "k_zt<curl>", "k_col<inv>", "k_xinv"]
 
 WORKLOADS = {
     "rings512": dict(n=512, reg=10, rings=16, seed=2024,

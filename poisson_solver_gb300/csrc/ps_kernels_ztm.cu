@@ -1,0 +1,384 @@
+// Fused z pass with tensor-memory staging (FP32, L = 256, 512, 1024, 2048).
+//
+// One CTA transforms B z-columns of every component: forward FFT, spectral
+// operation, inverse FFT. After its last forward stage a thread holds the 32
+// spectral values of its own positions n = out_pos(t, u, r) in registers. The
+// components other than the last are parked in the thread's private row of
+// tensor memory (two slots of 64 columns), so the spectral operation runs in
+// registers on all three components at once, and the inverse transform
+// starts from the same registers: it is the adjoint of the forward stages
+// taken in reverse order (gather from a stage's output positions, inverse
+// radix-R DFT, conjugate twiddles, scatter to its input positions), so its
+// first stage needs the values of exactly the positions the thread owns.
+//
+// Shared memory carries only the exchanges inside each transform, through
+// two line buffers used in turn (a transform writes one buffer, barrier,
+// reads it; the next transform writes the other), one barrier per exchange.
+// Against the wide fused kernel, which keeps all components in shared memory,
+// this removes four of the eight shared-memory passes per component line and
+// two of the three component buffers.
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "ps_tmem.cuh"
+#include "ps_wide.cuh"
+
+namespace ps {
+namespace wide {
+
+// Adjoint of stage S on registers gathered from its output positions:
+// inverse DFT, then conjugate twiddles.
+template <int L, int S, typename C>
+__device__ __forceinline__ void adjoint_dft(C (&v)[St<L, S>::U][St<L, S>::R], const C *tws, int t)
+{
+    using T = St<L, S>;
+#pragma unroll
+    for (int u = 0; u < T::U; ++u) {
+        dft<T::R, true>(v[u]);
+        if constexpr (T::M > 1) {
+            // keep the twiddle loads behind the DFT: hoisted above it they
+            // would hold R - 1 more complex values in registers
+            asm volatile("" ::: "memory");
+            const int j = (t + u * T::TPL) & (T::M - 1);
+            const C *w = tws + T::TWO + j * (T::R - 1);
+#pragma unroll
+            for (int r = 1; r < T::R; ++r) v[u][r] = cmulc(v[u][r], w[r - 1]);
+        }
+    }
+}
+
+template <int L, int S, typename C>
+__device__ __forceinline__ void read_out(const C *line, int t, C (&v)[St<L, S>::U][St<L, S>::R])
+{
+    using T = St<L, S>;
+#pragma unroll
+    for (int u = 0; u < T::U; ++u)
+#pragma unroll
+        for (int r = 0; r < T::R; ++r) v[u][r] = line[skw(T::out_pos(t, u, r))];
+}
+
+template <int L, int S, typename C>
+__device__ __forceinline__ void write_in(C *line, int t, const C (&v)[St<L, S>::U][St<L, S>::R])
+{
+    using T = St<L, S>;
+#pragma unroll
+    for (int u = 0; u < T::U; ++u)
+#pragma unroll
+        for (int r = 0; r < T::R; ++r) line[skw(T::in_pos(t, u, r))] = v[u][r];
+}
+
+// Adjoint middle stages S = from .. 1, in place on one line.
+template <int L, int S, typename C>
+__device__ __forceinline__ void adjoint_middle(C *line, const C *tws, int t)
+{
+    if constexpr (S >= 1) {
+        using T = St<L, S>;
+        C v[T::U][T::R];
+        read_out<L, S>(line, t, v);
+        adjoint_dft<L, S>(v, tws, t);
+        __syncthreads();
+        write_in<L, S>(line, t, v);
+        __syncthreads();
+        adjoint_middle<L, S - 1>(line, tws, t);
+    }
+}
+
+// 32 values <-> 4 x 16 columns of the thread's TMEM row.
+template <int U, int R>
+__device__ __forceinline__ void stash(uint32_t taddr, const float2 (&v)[U][R])
+{
+    static_assert(U * R == 32, "32 values per thread");
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+        uint32_t w[16];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int i = ch * 8 + e;
+            w[2 * e] = __float_as_uint(v[i / R][i % R].x);
+            w[2 * e + 1] = __float_as_uint(v[i / R][i % R].y);
+        }
+        tmem::st16(taddr + 16 * ch, w);
+    }
+}
+
+template <int U, int R>
+__device__ __forceinline__ void unstash(uint32_t taddr, float2 (&v)[U][R])
+{
+    uint32_t w[4][16];
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) tmem::ld16(taddr + 16 * ch, w[ch]);
+    tmem::wait_ld16x2(w[0], w[1]);
+    tmem::wait_ld16x2(w[2], w[3]);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i / R][i % R] = float2{__uint_as_float(w[i / 8][2 * (i % 8)]), __uint_as_float(w[i / 8][2 * (i % 8) + 1])};
+}
+
+constexpr int SLOT_COLUMNS = 64;  // 32 complex values
+
+template <int L, int OP>
+__global__ void __launch_bounds__(ZT_MAX_THREADS) k_zt(const ZArgs a, const int tm_cols)
+{
+    using C = float2;
+    using T = float;
+    using PL = WP<L>;
+    constexpr int LAST = PL::NST - 1;
+    using T0 = St<L, 0>;
+    using TL = St<L, LAST>;
+    static_assert(TL::U * TL::R == 32, "32 values per thread");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem_raw);
+    C *TW = reinterpret_cast<C *>(smem_raw + 16);
+    C *S = TW + PL::NTW;
+    const int B = a.B, LDP = pitch_col(L, B), CS = B * LDP;
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        tmem::alloc(tslot, tm_cols);
+        tmem::relinquish();
+    }
+    load_twiddles<C, PL::NTW>(TW, a.plan.table);
+    tmem::fence_before_sync();
+    __syncthreads();
+    tmem::fence_after_sync();
+    const uint32_t tbase = *tslot + tmem::lane_base(warp) + (uint32_t)((warp >> 2) * 2 * SLOT_COLUMNS);
+
+    const int lb = __ffs(B) - 1;
+    const int b = threadIdx.x & (B - 1), t = threadIdx.x >> lb;
+    const int x0 = blockIdx.x * B;
+    const int ky = a.ky0 + blockIdx.y;
+    const bool active = b < imin(B, a.Mx - x0);
+    const long long off = (long long)ky * a.row_stride + x0 + b;
+    const long long as = a.axis_stride;
+    const int n_in = active ? a.n_in : 0;
+    int ph = 0;  // transforms done: buffer ph & 1 is the next one
+
+    // forward transform of input component c, ending in v (own positions)
+    auto forward = [&](int c, C(&v)[TL::U][TL::R]) {
+        C *line = S + (ph & 1) * CS + b * LDP;
+        {
+            const C *col = reinterpret_cast<const C *>(pick3(a.in, c)) + off;
+            C v0[T0::U][T0::R];
+#pragma unroll
+            for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+                for (int r = 0; r < T0::R; ++r) {
+                    const int n = T0::in_pos(t, u, r);
+                    v0[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
+                }
+            twiddle_dft<L, 0, false>(v0, TW, t);
+            write_line<L, 0>(line, t, v0);
+        }
+        __syncthreads();
+        middle_stages<L, 1, false>(line, TW, t, 1, 0);
+        read_line<L, LAST>(line, t, v);
+        twiddle_dft<L, LAST, false>(v, TW, t);
+        ++ph;
+    };
+
+    C cur[TL::U][TL::R];
+    for (int c = 0; c + 1 < a.nin; ++c) {
+        forward(c, cur);
+        stash(tbase + c * SLOT_COLUMNS, cur);
+    }
+    forward(a.nin - 1, cur);
+    if (a.nin > 1) tmem::wait_st();
+
+    // spectral operation: components 0 .. nin-2 from TMEM, the last in cur;
+    // outputs 0 .. nout-2 back to TMEM, the last to cur
+    {
+        const int oy = imin(ky, a.Py - ky);
+        const int kx = x0 + b;
+        const T *Kc = reinterpret_cast<const T *>(a.kern) + (long long)oy * a.Mx + (active ? kx : 0);
+        const long long kzs = (long long)a.oct_y * a.Mx;
+        const T kyv = wavenumber<T>(ky, a.Py, (T)a.kyc, true);
+        const T kxv = wavenumber<T>(kx, a.Px, (T)a.kxc, true);
+        const T kzc = (T)a.kzc;
+        const int nslot_in = a.nin - 1;
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+            T g[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int i = ch * 8 + e;
+                const int n = TL::out_pos(t, i / TL::R, i % TL::R);
+                g[e] = active ? __ldg(&Kc[imin(n, a.Pz - n) * kzs]) : (T)0;
+            }
+            uint32_t s0[16], s1[16];
+            if (nslot_in > 0) tmem::ld16(tbase + 16 * ch, s0);
+            if (nslot_in > 1) tmem::ld16(tbase + SLOT_COLUMNS + 16 * ch, s1);
+            if (nslot_in > 0) tmem::wait_ld16x2(s0, s1);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int i = ch * 8 + e, u = i / TL::R, r = i % TL::R;
+                const int n = TL::out_pos(t, u, r);
+                const T kzv = wavenumber<T>(n, a.Pz, kzc, true);
+                const C ic = cur[u][r];
+                const C i0 = C{__uint_as_float(s0[2 * e]), __uint_as_float(s0[2 * e + 1])};
+                const C i1 = C{__uint_as_float(s1[2 * e]), __uint_as_float(s1[2 * e + 1])};
+                const T gi = g[e];
+                C o0{0.f, 0.f}, o1{0.f, 0.f}, o2;
+                if constexpr (OP == OP_NONE) {
+                    o0 = cscale(i0, gi);
+                    o1 = cscale(i1, gi);
+                    o2 = cscale(ic, gi);
+                } else if constexpr (OP == OP_GRAD) {
+                    // nin = 1: every output from the one input; nin = 3: output d from input d
+                    const C a0 = a.nin > 1 ? i0 : ic, a1 = a.nin > 1 ? i1 : ic;
+                    const T gx = gi * kxv, gy = gi * kyv, gz = gi * kzv;
+                    o0 = C{-gx * a0.y, gx * a0.x};
+                    o1 = C{-gy * a1.y, gy * a1.x};
+                    o2 = C{-gz * ic.y, gz * ic.x};
+                } else if constexpr (OP == OP_DIV) {
+                    const C s = C{kxv * i0.x + kyv * i1.x + kzv * ic.x, kxv * i0.y + kyv * i1.y + kzv * ic.y};
+                    o2 = C{-gi * s.y, gi * s.x};
+                } else {  // OP_CURL
+                    const C c0 = C{kyv * ic.x - kzv * i1.x, kyv * ic.y - kzv * i1.y};
+                    const C c1 = C{kzv * i0.x - kxv * ic.x, kzv * i0.y - kxv * ic.y};
+                    const C c2 = C{kxv * i1.x - kyv * i0.x, kxv * i1.y - kyv * i0.y};
+                    o0 = C{-gi * c0.y, gi * c0.x};
+                    o1 = C{-gi * c1.y, gi * c1.x};
+                    o2 = C{-gi * c2.y, gi * c2.x};
+                }
+                s0[2 * e] = __float_as_uint(o0.x);
+                s0[2 * e + 1] = __float_as_uint(o0.y);
+                s1[2 * e] = __float_as_uint(o1.x);
+                s1[2 * e + 1] = __float_as_uint(o1.y);
+                cur[u][r] = o2;
+            }
+            if (a.nout > 1) tmem::st16(tbase + 16 * ch, s0);
+            if (a.nout > 2) tmem::st16(tbase + SLOT_COLUMNS + 16 * ch, s1);
+        }
+        tmem::wait_st();
+    }
+
+    // inverse transforms: output nout-1 from cur, then nout-2 .. 0 from TMEM
+    for (int oc = a.nout - 1; oc >= 0; --oc) {
+        C *col0 = reinterpret_cast<C *>(pick3(a.out, oc));
+        if (!col0) continue;  // uniform over the CTA
+        if (oc < a.nout - 1) unstash(tbase + oc * SLOT_COLUMNS, cur);
+        C *line = S + (ph & 1) * CS + b * LDP;
+        adjoint_dft<L, LAST>(cur, TW, t);
+        write_in<L, LAST>(line, t, cur);
+        __syncthreads();
+        adjoint_middle<L, LAST - 1>(line, TW, t);
+        C v0[T0::U][T0::R];
+        read_out<L, 0>(line, t, v0);
+        adjoint_dft<L, 0>(v0, TW, t);
+        if (active) {
+            C *col = col0 + off;
+#pragma unroll
+            for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+                for (int r = 0; r < T0::R; ++r) {
+                    const int n = T0::in_pos(t, u, r);
+                    if (n < a.n_out) col[n * as] = v0[u][r];
+                }
+        }
+        ++ph;
+    }
+
+    tmem::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tmem::fence_after_sync();
+        tmem::dealloc(*tslot, tm_cols);
+    }
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+
+size_t smem_zt(int L, int B, int ntw) { return 16 + sizeof(float2) * ((size_t)ntw + 2 * (size_t)B * pitch_col(L, B)); }
+
+// TMEM columns of one CTA: two 64-column slots per thread, warps w and w + 4
+// on disjoint columns.
+int columns_zt(int threads)
+{
+    const int warps = (threads + 31) / 32, rows = (warps + 3) / 4;
+    int cols = 32;
+    while (cols < rows * 2 * SLOT_COLUMNS) cols *= 2;
+    return cols;
+}
+
+// Dynamic shared memory for a launch such that (resident CTAs per SM) x
+// (TMEM columns per CTA) <= 512: a CTA's tcgen05.alloc then never waits for
+// another CTA's columns. Returns 0 if no size achieves it.
+template <typename K> size_t smem_for_columns(K kernel, int threads, size_t sm, int cols)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, size_t, int>, size_t> cache;
+    const auto key = std::make_tuple((const void *)kernel, threads, sm, cols);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    const int cap = tmem::COLUMNS_PER_SM / cols;
+    int dev = 0, per_sm = 0, per_block = 0;
+    size_t out = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess) {
+        for (int attempt = 0; attempt < 2 && !out; ++attempt) {
+            if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) break;
+            int occ = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, sm) != cudaSuccess) break;
+            if (occ >= 1 && occ <= cap) out = sm;
+            else if (occ > cap) sm = std::max(sm, (size_t)per_sm / (cap + 1) + 1);
+            if (sm > (size_t)per_block) break;
+        }
+    }
+    cudaGetLastError();
+    cache[key] = out;
+    return out;
+}
+
+template <int L, int OP> cudaError_t launch_zt_op(const ZArgs &a, dim3 grid, int nt, cudaStream_t st)
+{
+    const int cols = columns_zt(nt);
+    const size_t sm = smem_for_columns(k_zt<L, OP>, nt, smem_zt(L, a.B, a.plan.ntw), cols);
+    if (!sm) return cudaErrorInvalidConfiguration;
+    // the attribute is per kernel: another configuration may have lowered it
+    const cudaError_t e = cudaFuncSetAttribute(k_zt<L, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_zt<L, OP><<<grid, nt, sm, st>>>(a, cols);
+    return cudaGetLastError();
+}
+
+template <int L> cudaError_t launch_zt_len(const ZArgs &a, dim3 grid, int nt, cudaStream_t st)
+{
+    switch (a.op) {
+    case OP_NONE: return launch_zt_op<L, OP_NONE>(a, grid, nt, st);
+    case OP_GRAD: return launch_zt_op<L, OP_GRAD>(a, grid, nt, st);
+    case OP_DIV: return launch_zt_op<L, OP_DIV>(a, grid, nt, st);
+    case OP_CURL: return launch_zt_op<L, OP_CURL>(a, grid, nt, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+bool zt_supported(int prec, int L, int op, int nin, int nout)
+{
+    return prec == PREC_FP32 && (L == 256 || L == 512 || L == 1024 || L == 2048) &&
+           (op == OP_NONE || op == OP_GRAD || op == OP_DIV || op == OP_CURL) && nin >= 1 && nin <= 3 && nout >= 1 &&
+           nout <= 3;
+}
+
+size_t smem_lines_zt(int L, int B, int ntw_entries) { return smem_zt(L, B, ntw_entries); }
+
+cudaError_t launch_zt(const ZArgs &a, int ny, cudaStream_t st)
+{
+    const int nt = a.B * (a.L / 32);
+    // whole warps only: the tcgen05 instructions are warp-collective
+    if (nt > ZT_MAX_THREADS || nt % 32 != 0) return cudaErrorInvalidConfiguration;
+    dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), ny);
+    switch (a.L) {
+    case 256: return launch_zt_len<256>(a, grid, nt, st);
+    case 512: return launch_zt_len<512>(a, grid, nt, st);
+    case 1024: return launch_zt_len<1024>(a, grid, nt, st);
+    case 2048: return launch_zt_len<2048>(a, grid, nt, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace wide
+}  // namespace ps

@@ -456,7 +456,8 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     // there: 2.3 vs 3.4 ms for the 512^3 forward x pass) and for other
     // power-of-two lengths 64..2048; the run-time kernels for the rest and
     // for FP64. PS_KERNELS (all axes) or PS_KERNELS_X/_Y/_Z = wide, p2 or
-    // runtime override the choice.
+    // runtime override the choice (PS_KERNELS_Z=wide: the shared-memory fused
+    // z kernel instead of the tensor-memory one).
     auto family = [&](int axis, int L, bool op_ok) -> char {
         static const char *names[3] = {"PS_KERNELS_X", "PS_KERNELS_Y", "PS_KERNELS_Z"};
         const char *f = getenv(names[axis]);
@@ -596,7 +597,18 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     za.kzc = 2.0 * M_PI / ((double)P[2] * dx[2]);
     za.plan = pz.dev;
     const int nbuf = std::max(za.nin, za.nout);
-    if (wz) {
+    // The wide z family runs as the tensor-memory kernel unless
+    // PS_KERNELS_Z=wide asks for the shared-memory one.
+    const char *zfam = getenv("PS_KERNELS_Z");
+    const bool zt = wz && !(zfam && strcmp(zfam, "wide") == 0) && wide::zt_supported(prec, P[2], op, za.nin, za.nout);
+    if (zt) {
+        // 8 columns a CTA (64-byte rows in global memory): measured 8.7 ms
+        // against 10.0 ms with 4 for the 512^3 curl pass (Pz = 1024)
+        za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return wide::smem_lines_zt(P[2], B, pz.dev.ntw); },
+                          "PS_LINES_Z", 8, wide::ZT_MAX_THREADS);
+        while (za.B * pz.dev.tpl < 32) za.B *= 2;  // whole warps (tcgen05 is warp-collective)
+        PS_CK(wide::launch_zt(za, P[1], stream));
+    } else if (wz) {
         za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return wide::smem_lines(P[2], B, nbuf, pz.dev.ntw, true); },
                           "PS_LINES_Z", 8, wide::Z_MAX_THREADS);
         PS_CK(wide::launch_z(za, P[1], stream));

@@ -147,6 +147,11 @@ cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st);
 cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st);
 cudaError_t launch_z(const ZArgs &a, int ny, cudaStream_t st);
 cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st);
+// fused z pass with the components parked in tensor memory (ps_kernels_ztm.cu)
+constexpr int ZT_MAX_THREADS = 256;
+bool zt_supported(int prec, int L, int op, int nin, int nout);
+size_t smem_lines_zt(int L, int B, int ntw_entries);
+cudaError_t launch_zt(const ZArgs &a, int ny, cudaStream_t st);
 }  // namespace wide
 
 // Kernel-build helpers (ps_greens.cu), all FP64.

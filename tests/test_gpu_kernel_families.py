@@ -1,0 +1,85 @@
+"""Every FP32 z-pass kernel family against the oracle, at the z lengths the
+wide kernels cover (Pz = 256 .. 2048), for every spectral operation.
+
+The families: the tensor-memory fused kernel (default), the shared-memory
+fused kernel (PS_KERNELS_Z=wide) and the length-specialised one
+(PS_KERNELS_Z=p2). Narrow x-y extents keep the oracle fast while the z
+columns reach the long lengths; the narrow x extent also leaves part of each
+CTA's columns inactive.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 5e-6
+
+# (ncell, bc) -> Pz: 256, 512, 1024, 2048 unbounded; 1024 and 512 periodic in z
+SHAPES = [
+    ((6, 5, 128), (0, 0, 0)),
+    ((5, 6, 256), (0, 0, 0)),
+    ((4, 6, 512), (0, 0, 0)),
+    ((4, 4, 1024), (0, 0, 0)),
+    ((6, 4, 1024), (1, 1, 1)),
+    ((8, 6, 512), (0, 0, 1)),
+]
+
+# (options, components pushed)
+OPS = [
+    (dict(), (0, 1, 2)),
+    (dict(), (1,)),
+    (dict(grad=True), (0,)),
+    (dict(grad=True), (0, 1, 2)),
+    (dict(div=True), (0, 1, 2)),
+    (dict(curl=True), (0, 1, 2)),
+]
+
+FAMILIES = ["tmem", "wide", "p2"]
+
+
+def _fields(nc, comps, seed):
+    rng = np.random.default_rng(seed)
+    shape = (nc[2], nc[1], nc[0])
+    return [rng.standard_normal(shape) if c in comps else None for c in range(3)]
+
+
+_ref_cache = {}
+
+
+def _reference(oracle, si, oi):
+    key = (si, oi)
+    if key not in _ref_cache:
+        nc, bc = SHAPES[si]
+        opts, comps = OPS[oi]
+        dx = (2.0 / nc[0], 1.5 / nc[1], 2.5 / nc[2])
+        B = _fields(nc, comps, 10 * si + oi)
+        ref, _ = oracle.solve3d(nc, bc, dx, B, 2, **opts)
+        _ref_cache[key] = (dx, B, ref)
+    return _ref_cache[key]
+
+
+@pytest.mark.parametrize("family", FAMILIES)
+@pytest.mark.parametrize("oi", range(len(OPS)))
+@pytest.mark.parametrize("si", range(len(SHAPES)))
+def test_fp32_z_family_vs_oracle(native, oracle, monkeypatch, si, oi, family):
+    nc, bc = SHAPES[si]
+    opts, _ = OPS[oi]
+    dx, B, ref = _reference(oracle, si, oi)
+    monkeypatch.setenv("PS_KERNELS_Z", family)
+    got, _ = native.solve(nc, bc, dx, B, 2, precision="fp32", **opts)
+    assert rel_l2(got, ref) < FP32_TOL
+
+
+@pytest.mark.parametrize("lines", [1, 2, 4, 8])
+def test_tmem_z_lines_per_cta(native, oracle, monkeypatch, lines):
+    """The tensor-memory kernel with 1..8 columns a CTA at Pz = 1024 (1..8 warps)."""
+    si, oi = 2, 5
+    nc, bc = SHAPES[si]
+    opts, _ = OPS[oi]
+    dx, B, ref = _reference(oracle, si, oi)
+    monkeypatch.setenv("PS_KERNELS_Z", "tmem")
+    monkeypatch.setenv("PS_LINES_Z", str(lines))
+    got, _ = native.solve(nc, bc, dx, B, 2, precision="fp32", **opts)
+    assert rel_l2(got, ref) < FP32_TOL
