@@ -44,52 +44,50 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     const int nt = blockDim.x, tid = threadIdx.x;
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * B;
+    __shared__ long long rofs[2 * MAX_LINES];
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, a.Mx);
 
-    // load (zero-fill n >= n_in and rows past the end)
-    T *Sr = reinterpret_cast<T *>(S);
-    const int lL = (L & (L - 1)) == 0 ? __ffs(L) - 1 : -1;
-    for (int idx = tid; idx < 2 * B * L; idx += nt) {
-        int rl, n;
-        if (lL >= 0) {
-            rl = idx >> lL;
-            n = idx & (L - 1);
-        } else {
-            rl = idx / L;
-            n = idx - rl * L;
-        }
-        const long long r = row0 + rl;
-        double v = 0.0;
-        if (n < a.n_in && r < rows) {
-            if (!a.mirror) {
-                v = in[r * a.in_stride + n];
-            } else {
-                const int j = (int)(r % a.rows_y), k = (int)(r / a.rows_y);
-                const int jj = imin(j, a.Py - j), kk = imin(k, a.Pz - k), nn = imin(n, L - n);
-                v = in[((long long)kk * a.oct_y + jj) * a.oct_x + nn];
+    // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last
+    // row. With the mirror flag the rows are those of the kernel octant,
+    // (z, y) -> (min(z, Pz-z), min(y, Py-y)), and n -> min(n, L-n).
+    for (int line = 0; line < B; ++line) {
+        const long long ra = row0 + 2 * line;
+        const bool va = ra < rows, vb = ra + 1 < rows;
+        long long oa = ra * a.in_stride, ob = oa + a.in_stride;
+        if (a.mirror) {
+            if (va) {
+                const int j = (int)(ra % a.rows_y), k = (int)(ra / a.rows_y);
+                oa = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
+            }
+            if (vb) {
+                const int j = (int)((ra + 1) % a.rows_y), k = (int)((ra + 1) / a.rows_y);
+                ob = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
             }
         }
-        Sr[2 * ((rl >> 1) * ld + n) + (rl & 1)] = (T)v;
+        C *ln = S + line * ld;
+        for (int n = tid; n < L; n += nt) {
+            T xa = (T)0, xb = (T)0;
+            if (n < a.n_in) {
+                const int nn = a.mirror ? imin(n, L - n) : n;
+                if (va) xa = (T)in[oa + nn];
+                if (vb) xb = (T)in[ob + nn];
+            }
+            ln[n] = C{xa, xb};
+        }
     }
     __syncthreads();
     fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, tid / B, plan, si);
 
     // separate the two half spectra and store
     const int Mx = a.Mx;
-    for (int idx = tid; idx < B * Mx; idx += nt) {
-        const int line = idx / Mx, k = idx - line * Mx;
-        const long long ra = row0 + 2 * line, rb = ra + 1;
-        if (ra >= rows) continue;
-        const C z = S[line * ld + k], w = S[line * ld + (k == 0 ? 0 : L - k)];
-        const T h = (T)0.5;
-        const C xa = C{h * (z.x + w.x), h * (z.y - w.y)};
-        const C xb = C{h * (z.y + w.y), h * (w.x - z.x)};
-        {
-            const long long j = ra % a.rows_y, kz = ra / a.rows_y;
-            out[(kz * a.out_y + j) * Mx + k] = xa;
-        }
-        if (rb < rows) {
-            const long long j = rb % a.rows_y, kz = rb / a.rows_y;
-            out[(kz * a.out_y + j) * Mx + k] = xb;
+    for (int line = 0; line < B; ++line) {
+        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
+        if (oa < 0) break;
+        for (int k = tid; k < Mx; k += nt) {
+            const C z = S[line * ld + k], w = S[line * ld + (k == 0 ? 0 : L - k)];
+            const T h = (T)0.5;
+            out[oa + k] = C{h * (z.x + w.x), h * (z.y - w.y)};
+            if (ob >= 0) out[ob + k] = C{h * (z.y + w.y), h * (w.x - z.x)};
         }
     }
 }
@@ -290,33 +288,36 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
     const int nt = blockDim.x, tid = threadIdx.x;
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * B;
+    __shared__ long long rofs[2 * MAX_LINES];
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
+    __syncthreads();
 
-    for (int idx = tid; idx < B * Mx; idx += nt) {
-        const int line = idx / Mx, k = idx - line * Mx;
-        const long long ra = row0 + 2 * line, rb = ra + 1;
-        C xa = C{0, 0}, xb = C{0, 0};
-        if (ra < rows) xa = in[((ra / a.rows_y) * a.in_y + ra % a.rows_y) * Mx + k];
-        if (rb < rows) xb = in[((rb / a.rows_y) * a.in_y + rb % a.rows_y) * Mx + k];
-        S[line * ld + k] = C{xa.x - xb.y, xa.y + xb.x};
-        if (k >= 1 && k <= L - Mx) S[line * ld + L - k] = C{xa.x + xb.y, xb.x - xa.y};
+    for (int line = 0; line < B; ++line) {
+        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
+        for (int k = tid; k < Mx; k += nt) {
+            C xa = C{0, 0}, xb = C{0, 0};
+            if (oa >= 0) xa = in[oa + k];
+            if (ob >= 0) xb = in[ob + k];
+            S[line * ld + k] = C{xa.x - xb.y, xa.y + xb.x};
+            if (k >= 1 && k <= L - Mx) S[line * ld + L - k] = C{xa.x + xb.y, xb.x - xa.y};
+        }
     }
     __syncthreads();
     fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, tid / B, plan, si);
 
-    const T *Sr = reinterpret_cast<const T *>(S);
+    // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;
-    const int lno = (no & (no - 1)) == 0 ? __ffs(no) - 1 : -1;
-    for (int idx = tid; idx < 2 * B * no; idx += nt) {
-        int rl, n;
-        if (lno >= 0) {
-            rl = idx >> lno;
-            n = idx & (no - 1);
-        } else {
-            rl = idx / no;
-            n = idx - rl * no;
+    for (int line = 0; line < B; ++line) {
+        const long long ra = row0 + 2 * line;
+        if (ra >= rows) break;
+        const bool vb = ra + 1 < rows;
+        double *oa = out + ra * a.out_stride, *ob = oa + a.out_stride;
+        const C *ln = S + line * ld;
+        for (int n = tid; n < no; n += nt) {
+            const C v = ln[n];
+            oa[n] = (double)v.x;
+            if (vb) ob[n] = (double)v.y;
         }
-        const long long r = row0 + rl;
-        if (r < rows) out[r * a.out_stride + n] = (double)Sr[2 * ((rl >> 1) * ld + n) + (rl & 1)];
     }
 }
 
@@ -357,6 +358,7 @@ template <typename K> static cudaError_t prep(K kernel, size_t smem)
 
 cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st)
 {
+    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long lines = (rows + 1) / 2;
     dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
@@ -426,6 +428,7 @@ cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st)
 
 cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
 {
+    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long lines = (rows + 1) / 2;
     dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
 {
     using C = typename CxT<T>::type;
     using PL = Plan<L, EM>;
-    constexpr int LL = PL::LL, TPL = PL::TPL, LT = ilog2(TPL);
+    constexpr int TPL = PL::TPL, LT = ilog2(TPL);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
     const int B = a.B, LDP = line_pitch<C>(L, B);
@@ -48,38 +48,71 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     C *out = reinterpret_cast<C *>(pick3(a.out, comp));
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * B;
+    __shared__ long long rofs[2 * MAX_LINES];
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, L / 2 + 1);
 
-    T *Sr = reinterpret_cast<T *>(S);
-    for (int idx = tid; idx < 2 * B * L; idx += nt) {
-        const int rl = idx >> LL, n = idx & (L - 1);
-        const long long r = row0 + rl;
-        double v = 0.0;
-        if (n < a.n_in && r < rows) {
-            if (!a.mirror) {
-                v = in[r * a.in_stride + n];
-            } else {
-                const int j = (int)(r % a.rows_y), k = (int)(r / a.rows_y);
-                const int jj = imin(j, a.Py - j), kk = imin(k, a.Pz - k), nn = imin(n, L - n);
-                v = in[((long long)kk * a.oct_y + jj) * a.oct_x + nn];
+    // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last row
+    if (!a.mirror) {
+        // B L = EM nt: EM (line, n) pairs a thread, every load issued before
+        // the first shared-memory store
+        constexpr int LL = PL::LL;
+        C v[EM];
+#pragma unroll
+        for (int i = 0; i < EM; ++i) {
+            const int idx = tid + i * nt, line = idx >> LL, n = idx & (L - 1);
+            const long long ra = row0 + 2 * line;
+            T xa = (T)0, xb = (T)0;
+            if (n < a.n_in) {
+                if (ra < rows) xa = (T)in[ra * a.in_stride + n];
+                if (ra + 1 < rows) xb = (T)in[(ra + 1) * a.in_stride + n];
+            }
+            v[i] = C{xa, xb};
+        }
+#pragma unroll
+        for (int i = 0; i < EM; ++i) {
+            const int idx = tid + i * nt, line = idx >> LL, n = idx & (L - 1);
+            S[line * LDP + sk<C>(n)] = v[i];
+        }
+    } else {
+        // rows of the kernel octant, mirrored: (z, y) -> (min(z, Pz-z), min(y, Py-y)), n -> min(n, L-n)
+        for (int line = 0; line < B; ++line) {
+            const long long ra = row0 + 2 * line;
+            const bool va = ra < rows, vb = ra + 1 < rows;
+            long long oa = 0, ob = 0;
+            if (va) {
+                const int j = (int)(ra % a.rows_y), k = (int)(ra / a.rows_y);
+                oa = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
+            }
+            if (vb) {
+                const int j = (int)((ra + 1) % a.rows_y), k = (int)((ra + 1) / a.rows_y);
+                ob = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
+            }
+            C *ln = S + line * LDP;
+            for (int n = tid; n < L; n += nt) {
+                T xa = (T)0, xb = (T)0;
+                if (n < a.n_in) {
+                    const int nn = imin(n, L - n);
+                    if (va) xa = (T)in[oa + nn];
+                    if (vb) xb = (T)in[ob + nn];
+                }
+                ln[sk<C>(n)] = C{xa, xb};
             }
         }
-        Sr[2 * ((rl >> 1) * LDP + sk<C>(n)) + (rl & 1)] = (T)v;
     }
     __syncthreads();
     run<L, EM, false>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
 
     constexpr int Mx = L / 2 + 1;
-    for (int idx = tid; idx < B * Mx; idx += nt) {
-        const int line = idx / Mx, k = idx - line * Mx;
-        const long long ra = row0 + 2 * line, rb = ra + 1;
-        if (ra >= rows) continue;
+    for (int line = 0; line < B; ++line) {
+        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
+        if (oa < 0) break;
         const C *ln = S + line * LDP;
-        const C z = ln[sk<C>(k)], w = ln[sk<C>((L - k) & (L - 1))];
-        const T h = (T)0.5;
-        const C xa = C{h * (z.x + w.x), h * (z.y - w.y)};
-        const C xb = C{h * (z.y + w.y), h * (w.x - z.x)};
-        out[((ra / a.rows_y) * a.out_y + ra % a.rows_y) * Mx + k] = xa;
-        if (rb < rows) out[((rb / a.rows_y) * a.out_y + rb % a.rows_y) * Mx + k] = xb;
+        for (int k = tid; k < Mx; k += nt) {
+            const C z = ln[sk<C>(k)], w = ln[sk<C>((L - k) & (L - 1))];
+            const T h = (T)0.5;
+            out[oa + k] = C{h * (z.x + w.x), h * (z.y - w.y)};
+            if (ob >= 0) out[ob + k] = C{h * (z.y + w.y), h * (w.x - z.x)};
+        }
     }
 }
 
@@ -248,26 +281,37 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
     double *out = pick3(a.out, comp);
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * B;
+    __shared__ long long rofs[2 * MAX_LINES];
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
+    __syncthreads();
 
-    for (int idx = tid; idx < B * Mx; idx += nt) {
-        const int line = idx / Mx, k = idx - line * Mx;
-        const long long ra = row0 + 2 * line, rb = ra + 1;
-        C xa = C{0, 0}, xb = C{0, 0};
-        if (ra < rows) xa = in[((ra / a.rows_y) * a.in_y + ra % a.rows_y) * Mx + k];
-        if (rb < rows) xb = in[((rb / a.rows_y) * a.in_y + rb % a.rows_y) * Mx + k];
+    for (int line = 0; line < B; ++line) {
+        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
         C *ln = S + line * LDP;
-        ln[sk<C>(k)] = C{xa.x - xb.y, xa.y + xb.x};
-        if (k >= 1 && k <= L - Mx) ln[sk<C>(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
+        for (int k = tid; k < Mx; k += nt) {
+            C xa = C{0, 0}, xb = C{0, 0};
+            if (oa >= 0) xa = in[oa + k];
+            if (ob >= 0) xb = in[ob + k];
+            ln[sk<C>(k)] = C{xa.x - xb.y, xa.y + xb.x};
+            if (k >= 1 && k <= L - Mx) ln[sk<C>(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
+        }
     }
     __syncthreads();
     run<L, EM, true>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
 
-    const T *Sr = reinterpret_cast<const T *>(S);
+    // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;
-    for (int idx = tid; idx < 2 * B * no; idx += nt) {
-        const int rl = idx / no, n = idx - rl * no;
-        const long long r = row0 + rl;
-        if (r < rows) out[r * a.out_stride + n] = (double)Sr[2 * ((rl >> 1) * LDP + sk<C>(n)) + (rl & 1)];
+    for (int line = 0; line < B; ++line) {
+        const long long ra = row0 + 2 * line;
+        if (ra >= rows) break;
+        const bool vb = ra + 1 < rows;
+        double *oa = out + ra * a.out_stride, *ob = oa + a.out_stride;
+        const C *ln = S + line * LDP;
+        for (int n = tid; n < no; n += nt) {
+            const C v = ln[sk<C>(n)];
+            oa[n] = (double)v.x;
+            if (vb) ob[n] = (double)v.y;
+        }
     }
 }
 
@@ -295,6 +339,7 @@ size_t smem_lines(int prec, int L, int B, int nbuf, int ntw_entries)
 
 cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st)
 {
+    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
     const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);
@@ -378,6 +423,7 @@ cudaError_t launch_z(const ZArgs &a, int ny, int em, cudaStream_t st)
 
 cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st)
 {
+    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
     const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);

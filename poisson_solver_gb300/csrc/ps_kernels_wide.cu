@@ -208,6 +208,8 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     C *out = reinterpret_cast<C *>(pick3(a.out, comp));
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long ra = (long long)blockIdx.x * 2 * B + 2 * b, rb = ra + 1;
+    __shared__ long long rofs[2 * MAX_LINES];
+    row_offsets(rofs, (long long)blockIdx.x * 2 * B, 2 * B, rows, a.rows_y, a.out_y, L / 2 + 1);
     C *line = S + b * LDP;
     {
         using T0 = St<L, 0>;
@@ -251,17 +253,14 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     // separate the half spectra of rows a and b
     constexpr int Mx = L / 2 + 1;
     const int nt = blockDim.x;
-    const long long row0 = (long long)blockIdx.x * 2 * B;
     for (int idx = threadIdx.x; idx < B * Mx; idx += nt) {
         const int l = idx / Mx, k = idx - l * Mx;
-        const long long r0 = row0 + 2 * l, r1 = r0 + 1;
-        if (r0 >= rows) continue;
+        const long long oa = rofs[2 * l], ob = rofs[2 * l + 1];
+        if (oa < 0) continue;
         const C *ln = S + l * LDP;
         const C z = ln[skw(k)], w = ln[skw((L - k) & (L - 1))];
-        const C xa = C{0.5f * (z.x + w.x), 0.5f * (z.y - w.y)};
-        const C xb = C{0.5f * (z.y + w.y), 0.5f * (w.x - z.x)};
-        out[((r0 / a.rows_y) * a.out_y + r0 % a.rows_y) * Mx + k] = xa;
-        if (r1 < rows) out[((r1 / a.rows_y) * a.out_y + r1 % a.rows_y) * Mx + k] = xb;
+        out[oa + k] = C{0.5f * (z.x + w.x), 0.5f * (z.y - w.y)};
+        if (ob >= 0) out[ob + k] = C{0.5f * (z.y + w.y), 0.5f * (w.x - z.x)};
     }
 }
 
@@ -284,12 +283,15 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * B;
     const int nt = blockDim.x;
+    __shared__ long long rofs[2 * MAX_LINES];
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
+    __syncthreads();
     for (int idx = threadIdx.x; idx < B * Mx; idx += nt) {
         const int l = idx / Mx, k = idx - l * Mx;
-        const long long r0 = row0 + 2 * l, r1 = r0 + 1;
+        const long long oa = rofs[2 * l], ob = rofs[2 * l + 1];
         C xa = C{0.f, 0.f}, xb = C{0.f, 0.f};
-        if (r0 < rows) xa = in[((r0 / a.rows_y) * a.in_y + r0 % a.rows_y) * Mx + k];
-        if (r1 < rows) xb = in[((r1 / a.rows_y) * a.in_y + r1 % a.rows_y) * Mx + k];
+        if (oa >= 0) xa = in[oa + k];
+        if (ob >= 0) xb = in[ob + k];
         C *ln = S + l * LDP;
         ln[skw(k)] = C{xa.x - xb.y, xa.y + xb.x};
         if (k >= 1 && k <= L - Mx) ln[skw(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
@@ -345,6 +347,7 @@ size_t smem_lines(int L, int B, int nbuf, int ntw_entries, bool column)
 
 cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st)
 {
+    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
     const size_t sm = smem_lines(a.L, a.B, 1, a.plan.ntw, false);
@@ -424,6 +427,7 @@ cudaError_t launch_z(const ZArgs &a, int ny, cudaStream_t st)
 
 cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st)
 {
+    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
     const size_t sm = smem_lines(a.L, a.B, 1, a.plan.ntw, false);

@@ -194,15 +194,17 @@ __global__ void __launch_bounds__(ZT_MAX_THREADS) k_zt(const ZArgs a, const int 
         const T kxv = wavenumber<T>(kx, a.Px, (T)a.kxc, true);
         const T kzc = (T)a.kzc;
         const int nslot_in = a.nin - 1;
+        T gall[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            const int n = TL::out_pos(t, i / TL::R, i % TL::R);
+            gall[i] = active ? __ldg(&Kc[imin(n, a.Pz - n) * kzs]) : (T)0;
+        }
 #pragma unroll
         for (int ch = 0; ch < 4; ++ch) {
             T g[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int i = ch * 8 + e;
-                const int n = TL::out_pos(t, i / TL::R, i % TL::R);
-                g[e] = active ? __ldg(&Kc[imin(n, a.Pz - n) * kzs]) : (T)0;
-            }
+            for (int e = 0; e < 8; ++e) g[e] = gall[ch * 8 + e];
             uint32_t s0[16], s1[16];
             if (nslot_in > 0) tmem::ld16(tbase + 16 * ch, s0);
             if (nslot_in > 1) tmem::ld16(tbase + SLOT_COLUMNS + 16 * ch, s1);

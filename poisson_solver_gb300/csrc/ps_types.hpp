@@ -7,6 +7,7 @@ namespace ps {
 
 constexpr int MAX_STAGES = 16;
 constexpr int MAX_THREADS = 512;  // CTA size bound of the pass kernels (<= 128 registers a thread)
+constexpr int MAX_LINES = 64;     // lines a CTA of any pass kernel (the x passes keep 2 row offsets a line)
 
 enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
 
