@@ -163,6 +163,49 @@ int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset);
  * [Pz/2+1][Py/2+1][Px/2+1] (x fastest), to a HOST array. */
 int ps_get_kernel(const ps_solver *h, double *out, long long capacity);
 
+/* ---------------------------------------------------------------------------
+ * Batched solves. No reference counterpart as one call: the reference solves
+ * many problems by holding one poisson_solver object per problem and calling
+ * setup3d / push / solve3d / pull on each (c++/test/<case>/sources/main.cpp
+ * drive one object each). A batch holds many independent problems -- any grid,
+ * boundary conditions, regularisation order, components and output option
+ * each -- and solves them all with one kernel launch per pass (five launches
+ * in all, whatever the number of problems), replayed through a CUDA graph
+ * that is captured on the first solve and again after any change to the set
+ * of problems, their options or their pushed components.
+ *
+ *   ps_batch_create(&b, PS_PREC_FP64 or PS_PREC_FP32)   one precision a batch
+ *   ps_batch_add(b, ncell, bc, dx, reg, &i)             setup3d of problem i
+ *   ps_batch_set_option(b, i, PS_OPT_GRAD/DIV/CURL/REPROJECT, 0/1)
+ *   ps_batch_push(b, i, bx, by, bz)                     push of problem i
+ *   ps_batch_solve(b)                                   solve3d of every problem
+ *   ps_batch_pull(b, i, ax, ay, az)                     pull of problem i's A
+ *
+ * Same field layout, components and errors as the single-problem calls; a
+ * solve fails with PS_ERR_STATE if a problem has nothing pushed. Every
+ * problem is solved with the run-time transform kernels (any length).
+ * ps_batch_solve runs asynchronously on the batch's stream; pulls wait. */
+typedef struct ps_batch ps_batch;
+int ps_batch_create(ps_batch **out, int precision);
+int ps_batch_destroy(ps_batch *b);
+int ps_batch_add(ps_batch *b, const int ncell[3], const int bc[3], const double dx[3], int reg_order, int *index);
+int ps_batch_count(const ps_batch *b, int *count);
+int ps_batch_set_option(ps_batch *b, int index, int option, int value);
+int ps_batch_push(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
+int ps_batch_push_device(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
+int ps_batch_solve(ps_batch *b);
+int ps_batch_pull(ps_batch *b, int index, double *ax, double *ay, double *az);
+int ps_batch_pull_device(ps_batch *b, int index, double *ax, double *ay, double *az);
+int ps_batch_set_stream(ps_batch *b, void *stream);
+int ps_batch_synchronize(ps_batch *b);
+enum {
+    PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0, /* kernels one batched solve launches (5) */
+    PS_BATCH_INFO_TILES_PER_SOLVE = 1,    /* CTA tiles of the last captured solve, all passes */
+    PS_BATCH_INFO_POINTS = 2              /* grid points over all problems */
+};
+int ps_batch_get_info(const ps_batch *b, int what, double *value);
+const char *ps_batch_last_error(const ps_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,10 @@ PS_INFO_LAUNCHES_PER_SOLVE = 3
 PS_INFO_DEVICE_BYTES = 4
 PS_INFO_KERNEL_OCTANT = 5
 
+PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0
+PS_BATCH_INFO_TILES_PER_SOLVE = 1
+PS_BATCH_INFO_POINTS = 2
+
 # Every symbol the header declares, with (restype, argtypes).
 _vp = ctypes.c_void_p
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -66,6 +70,20 @@ SIGNATURES = {
     "ps_get_info": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_double)]),
     "ps_get_kernel": (_i, [_vp, _dp, ctypes.c_longlong]),
     "ps_get_pass_times": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _ip, _i]),
+    "ps_batch_create": (_i, [ctypes.POINTER(_vp), _i]),
+    "ps_batch_destroy": (_i, [_vp]),
+    "ps_batch_add": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_double), _i, _ip]),
+    "ps_batch_count": (_i, [_vp, _ip]),
+    "ps_batch_set_option": (_i, [_vp, _i, _i, _i]),
+    "ps_batch_push": (_i, [_vp, _i, _dp, _dp, _dp]),
+    "ps_batch_push_device": (_i, [_vp, _i, _dp, _dp, _dp]),
+    "ps_batch_solve": (_i, [_vp]),
+    "ps_batch_pull": (_i, [_vp, _i, _dp, _dp, _dp]),
+    "ps_batch_pull_device": (_i, [_vp, _i, _dp, _dp, _dp]),
+    "ps_batch_set_stream": (_i, [_vp, _vp]),
+    "ps_batch_synchronize": (_i, [_vp]),
+    "ps_batch_get_info": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_double)]),
+    "ps_batch_last_error": (ctypes.c_char_p, [_vp]),
 }
 
 _lib: ctypes.CDLL | None = None

@@ -1,0 +1,454 @@
+// Batched solves: many independent problems (any grid, boundary conditions,
+// components and output option each) run as five launches, one per pass,
+// each launch covering the tiles of every problem (ps_kernels.cu, k_*_batch).
+// The five launches are captured once into a CUDA graph and replayed by every
+// solve until the set of problems, their options or their pushed components
+// change.
+//
+// Each problem keeps a ps::Solver for its state: the kernel build, the FFT
+// plans and the device buffers. A solve reuses the solver's pass arguments
+// (Solver::prepare) with the run-time kernel family, which covers every length.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "poisson_solver_gb300.h"
+#include "ps_solver.hpp"
+
+namespace ps {
+
+#define PS_BCK(expr)                                                                                           \
+    do {                                                                                                       \
+        cudaError_t e_ = (expr);                                                                               \
+        if (e_ != cudaSuccess) throw ps::Error(PS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct Batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int precision = PREC_FP64;
+    std::vector<std::unique_ptr<Solver>> items;
+    std::string last_error;
+
+    // The executable: per pass, the arguments of every problem and the tile
+    // list, in device memory, with the launch's block and shared-memory sizes.
+    struct PassExec {
+        DevBuf args, tiles;
+        int ntiles = 0, nt = 0;
+        size_t smem = 0;
+    };
+    PassExec ex[5];
+    std::vector<int> write_masks;  // outputs of each problem in the captured solve
+    bool dirty = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    explicit Batch(int prec) : precision(prec)
+    {
+        if (prec != PREC_FP64 && prec != PREC_FP32) throw Error(PS_ERR_ARGUMENT, "precision must be FP64 or FP32");
+        PS_BCK(cudaGetDevice(&device));
+    }
+    ~Batch() { release_graph(); }
+
+    Solver &at(int i)
+    {
+        if (i < 0 || i >= (int)items.size()) throw Error(PS_ERR_ARGUMENT, "problem index out of range");
+        return *items[i];
+    }
+
+    int add(const int ncell[3], const int bc[3], const double dx[3], int reg)
+    {
+        auto s = std::make_unique<Solver>();
+        s->stream = stream;
+        s->precision = precision;
+        s->setup3d(ncell, bc, dx, reg);
+        items.push_back(std::move(s));
+        dirty = true;
+        return (int)items.size() - 1;
+    }
+
+    void set_option(int i, int option, int value)
+    {
+        if (option == PS_OPT_PRECISION) throw Error(PS_ERR_ARGUMENT, "a batch has one precision, set at creation");
+        at(i).set_option(option, value);
+        dirty = true;
+    }
+
+    void push(int i, const double *const B[3], cudaMemcpyKind kind)
+    {
+        Solver &s = at(i);
+        const int before = s.pushed;
+        s.push(B, kind);
+        if (s.pushed != before) dirty = true;
+    }
+
+    void pull(int i, double *const A[3], cudaMemcpyKind kind)
+    {
+        double *const none[3] = {nullptr, nullptr, nullptr};
+        at(i).pull(A, none, kind);
+    }
+
+    void set_stream(cudaStream_t st)
+    {
+        stream = st;
+        for (auto &s : items) s->stream = st;
+    }
+
+    void release_graph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+
+    // Lines per CTA of each problem in one batched pass. The launch's block
+    // size nt is the largest of the problems' usual CTA sizes (capped at
+    // BATCH_MAX_THREADS); each problem then takes the most lines (a power of
+    // two) that fit nt threads and the largest usual shared-memory size, so
+    // that its CTAs leave as few threads idle as the smem budget allows.
+    template <typename SmemFn>
+    static void choose_lines(const std::vector<int> &tpl, const SmemFn &smem, int max_lines, std::vector<int> &B,
+                             int &nt, size_t &smem_max)
+    {
+        const int start_lines = 16;
+        const size_t limit = (size_t)max_smem_per_block() - 2048;  // room for static shared data
+        const int n = (int)tpl.size();
+        B.assign(n, 1);
+        nt = 0;
+        size_t cap = 0;
+        for (int p = 0; p < n; ++p) {
+            int b = std::min(start_lines, max_lines);
+            while (b > 1 && (b * tpl[p] > BATCH_MAX_THREADS || smem(p, b) > limit)) b >>= 1;
+            if (b * tpl[p] > BATCH_MAX_THREADS || smem(p, b) > limit)
+                throw Error(PS_ERR_UNSUPPORTED, "a transform of the batch is too long for one CTA");
+            nt = std::max(nt, b * tpl[p]);
+            cap = std::max(cap, smem(p, b));
+        }
+        smem_max = 0;
+        for (int p = 0; p < n; ++p) {
+            int b = 1;
+            while (2 * b <= max_lines && 2 * b * tpl[p] <= nt && smem(p, 2 * b) <= cap) b *= 2;
+            B[p] = b;
+            smem_max = std::max(smem_max, smem(p, b));
+        }
+        nt = (nt + 31) / 32 * 32;
+    }
+
+    template <typename Args> static void upload(PassExec &e, const std::vector<Args> &args, const std::vector<BatchTile> &tiles)
+    {
+        e.ntiles = (int)tiles.size();
+        if (args.empty() || tiles.empty()) return;
+        e.args.ensure(args.size() * sizeof(Args));
+        e.tiles.ensure(tiles.size() * sizeof(BatchTile));
+        PS_BCK(cudaMemcpy(e.args.p, args.data(), args.size() * sizeof(Args), cudaMemcpyHostToDevice));
+        PS_BCK(cudaMemcpy(e.tiles.p, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice));
+    }
+
+    void build()
+    {
+        if (items.empty()) throw Error(PS_ERR_STATE, "the batch holds no problem");
+        const int n = (int)items.size(), prec = precision;
+        std::vector<PassArgs> pa(n);
+        std::vector<const Plan *> plx(n), ply(n), plz(n);
+        write_masks.assign(n, 0);
+        for (int p = 0; p < n; ++p) {
+            Solver &s = *items[p];
+            if (!s.pushed) throw Error(PS_ERR_STATE, "problem " + std::to_string(p) + ": solve called before push");
+            const int out_mask = s.output_mask(s.pushed);
+            const double *Bin[3];
+            double *Aout[3];
+            for (int c = 0; c < 3; ++c) {
+                Bin[c] = (s.pushed >> c & 1) ? (const double *)s.fb[c].p : nullptr;
+                Aout[c] = nullptr;
+                if (out_mask >> c & 1) {
+                    s.fa[c].ensure((size_t)s.n[0] * s.n[1] * s.n[2] * sizeof(double));
+                    Aout[c] = (double *)s.fa[c].p;
+                }
+            }
+            write_masks[p] = s.prepare(Bin, Aout, false, pa[p]);
+            plx[p] = &s.plan(s.P[0], prec);
+            ply[p] = &s.plan(s.P[1], prec);
+            plz[p] = &s.plan(s.P[2], prec, e_max_z(prec));  // the z body's element budget
+        }
+        std::vector<int> tx(n), ty(n), tz(n), Bx, By, Bz;
+        for (int p = 0; p < n; ++p) {
+            tx[p] = plx[p]->dev.tpl;
+            ty[p] = ply[p]->dev.tpl;
+            tz[p] = plz[p]->dev.tpl;
+        }
+        choose_lines(tx, [&](int p, int B) { return smem_x(prec, plx[p]->dev, B); }, MAX_LINES, Bx, ex[0].nt,
+                     ex[0].smem);
+        choose_lines(ty, [&](int p, int B) { return smem_col(prec, ply[p]->dev, B); }, MAX_LINES, By, ex[1].nt,
+                     ex[1].smem);
+        choose_lines(
+            tz,
+            [&](int p, int B) { return smem_z(prec, plz[p]->dev, B, std::max(pa[p].z.nin, pa[p].z.nout)); },
+            MAX_LINES, Bz, ex[2].nt, ex[2].smem);
+        ex[3].nt = ex[1].nt;
+        ex[3].smem = ex[1].smem;
+        ex[4].nt = ex[0].nt;
+        ex[4].smem = ex[0].smem;
+
+        std::vector<XFwdArgs> ax(n);
+        std::vector<ColArgs> ay(n), ayi(n);
+        std::vector<ZArgs> az(n);
+        std::vector<XInvArgs> axi(n);
+        std::vector<BatchTile> t0, t1, t2, t3, t4;
+        for (int p = 0; p < n; ++p) {
+            const Solver &s = *items[p];
+            ax[p] = pa[p].x;
+            ax[p].plan = plx[p]->dev;
+            ax[p].B = Bx[p];
+            ay[p] = pa[p].y;
+            ay[p].plan = ply[p]->dev;
+            ay[p].B = By[p];
+            az[p] = pa[p].z;
+            az[p].plan = plz[p]->dev;
+            az[p].B = Bz[p];
+            ayi[p] = pa[p].yi;
+            ayi[p].plan = ply[p]->dev;
+            ayi[p].B = By[p];
+            axi[p] = pa[p].xi;
+            axi[p].plan = plx[p]->dev;
+            axi[p].B = Bx[p];
+
+            const long long lines = ((long long)s.n[1] * s.n[2] + 1) / 2;
+            const int gx = (int)((lines + Bx[p] - 1) / Bx[p]);
+            for (int c = 0; c < ax[p].ncomp; ++c)
+                for (int b = 0; b < gx; ++b) t0.push_back({p, b, c, 0});
+            const int gy = (s.Mx + By[p] - 1) / By[p];
+            for (int c = 0; c < ay[p].ncomp; ++c)
+                for (int z = 0; z < s.n[2]; ++z)
+                    for (int b = 0; b < gy; ++b) t1.push_back({p, b, z, c});
+            const int gz = (s.Mx + Bz[p] - 1) / Bz[p];
+            for (int ky = 0; ky < s.P[1]; ++ky)
+                for (int b = 0; b < gz; ++b) t2.push_back({p, b, ky, 0});
+            if (write_masks[p]) {
+                for (int c = 0; c < ayi[p].ncomp; ++c)
+                    for (int z = 0; z < s.n[2]; ++z)
+                        for (int b = 0; b < gy; ++b) t3.push_back({p, b, z, c});
+                for (int c = 0; c < axi[p].ncomp; ++c)
+                    for (int b = 0; b < gx; ++b) t4.push_back({p, b, c, 0});
+            }
+        }
+        PS_BCK(cudaStreamSynchronize(stream));  // kernel builds done before the arguments change hands
+        upload(ex[0], ax, t0);
+        upload(ex[1], ay, t1);
+        upload(ex[2], az, t2);
+        upload(ex[3], ayi, t3);
+        upload(ex[4], axi, t4);
+
+        // capture the five launches
+        release_graph();
+        cudaStream_t cs = stream;
+        bool own = false;
+        if (!cs) {
+            // the legacy default stream cannot be captured: capture on a
+            // private stream, replay on the batch's
+            PS_BCK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            own = true;
+        }
+        PS_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+        cudaError_t e = launch_xfwd_batch(prec, (const XFwdArgs *)ex[0].args.p, (const BatchTile *)ex[0].tiles.p,
+                                          ex[0].ntiles, ex[0].nt, ex[0].smem, cs);
+        if (e == cudaSuccess)
+            e = launch_col_batch(prec, 0, (const ColArgs *)ex[1].args.p, (const BatchTile *)ex[1].tiles.p, ex[1].ntiles,
+                                 ex[1].nt, ex[1].smem, cs);
+        if (e == cudaSuccess)
+            e = launch_z_batch(prec, (const ZArgs *)ex[2].args.p, (const BatchTile *)ex[2].tiles.p, ex[2].ntiles,
+                               ex[2].nt, ex[2].smem, cs);
+        if (e == cudaSuccess)
+            e = launch_col_batch(prec, 1, (const ColArgs *)ex[3].args.p, (const BatchTile *)ex[3].tiles.p, ex[3].ntiles,
+                                 ex[3].nt, ex[3].smem, cs);
+        if (e == cudaSuccess)
+            e = launch_xinv_batch(prec, (const XInvArgs *)ex[4].args.p, (const BatchTile *)ex[4].tiles.p,
+                                  ex[4].ntiles, ex[4].nt, ex[4].smem, cs);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+        if (own) cudaStreamDestroy(cs);
+        if (e != cudaSuccess || ec != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            throw Error(PS_ERR_CUDA, std::string("batched launch capture: ") +
+                                         cudaGetErrorString(e != cudaSuccess ? e : ec));
+        }
+        graph = g;
+        PS_BCK(cudaGraphInstantiate(&exec, graph, 0));
+        dirty = false;
+    }
+
+    void solve()
+    {
+        if (dirty) build();
+        PS_BCK(cudaGraphLaunch(exec, stream));
+        for (size_t p = 0; p < items.size(); ++p) {
+            items[p]->produced = write_masks[p];
+            items[p]->rhs_ready = 0;
+        }
+    }
+
+    long long tiles_per_solve() const
+    {
+        long long t = 0;
+        for (const auto &e : ex) t += e.ntiles;
+        return t;
+    }
+};
+
+}  // namespace ps
+
+struct ps_batch {
+    std::unique_ptr<ps::Batch> b;
+    std::string create_error;
+};
+
+namespace {
+
+template <typename F> int bguarded(ps_batch *h, F &&f)
+{
+    if (!h || !h->b) return PS_ERR_ARGUMENT;
+    ps::Batch &b = *h->b;
+    try {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != b.device) cudaSetDevice(b.device);
+        f(b);
+        b.last_error.clear();
+        return PS_OK;
+    } catch (const ps::Error &e) {
+        b.last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        b.last_error = "host allocation failed";
+        return PS_ERR_MEMORY;
+    } catch (const std::exception &e) {
+        b.last_error = e.what();
+        return PS_ERR_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ps_batch_create(ps_batch **out, int precision)
+{
+    if (!out) return PS_ERR_ARGUMENT;
+    *out = nullptr;
+    try {
+        auto h = std::make_unique<ps_batch>();
+        h->b = std::make_unique<ps::Batch>(precision);
+        *out = h.release();
+    } catch (const ps::Error &e) {
+        return e.status;
+    } catch (...) {
+        return PS_ERR_MEMORY;
+    }
+    return PS_OK;
+}
+
+int ps_batch_destroy(ps_batch *h)
+{
+    if (!h) return PS_OK;
+    if (h->b) cudaSetDevice(h->b->device);
+    delete h;
+    return PS_OK;
+}
+
+int ps_batch_add(ps_batch *h, const int ncell[3], const int bc[3], const double dx[3], int reg_order, int *index)
+{
+    if (!ncell || !bc || !dx) return PS_ERR_ARGUMENT;
+    return bguarded(h, [&](ps::Batch &b) {
+        const int i = b.add(ncell, bc, dx, reg_order);
+        if (index) *index = i;
+    });
+}
+
+int ps_batch_count(const ps_batch *h, int *count)
+{
+    if (!h || !h->b || !count) return PS_ERR_ARGUMENT;
+    *count = (int)h->b->items.size();
+    return PS_OK;
+}
+
+int ps_batch_set_option(ps_batch *h, int index, int option, int value)
+{
+    return bguarded(h, [&](ps::Batch &b) { b.set_option(index, option, value); });
+}
+
+int ps_batch_push(ps_batch *h, int index, const double *bx, const double *by, const double *bz)
+{
+    return bguarded(h, [&](ps::Batch &b) {
+        const double *B[3] = {bx, by, bz};
+        b.push(index, B, cudaMemcpyHostToDevice);
+    });
+}
+
+int ps_batch_push_device(ps_batch *h, int index, const double *bx, const double *by, const double *bz)
+{
+    return bguarded(h, [&](ps::Batch &b) {
+        const double *B[3] = {bx, by, bz};
+        b.push(index, B, cudaMemcpyDeviceToDevice);
+    });
+}
+
+int ps_batch_solve(ps_batch *h)
+{
+    return bguarded(h, [&](ps::Batch &b) { b.solve(); });
+}
+
+int ps_batch_pull(ps_batch *h, int index, double *ax, double *ay, double *az)
+{
+    return bguarded(h, [&](ps::Batch &b) {
+        double *A[3] = {ax, ay, az};
+        b.pull(index, A, cudaMemcpyDeviceToHost);
+    });
+}
+
+int ps_batch_pull_device(ps_batch *h, int index, double *ax, double *ay, double *az)
+{
+    return bguarded(h, [&](ps::Batch &b) {
+        double *A[3] = {ax, ay, az};
+        b.pull(index, A, cudaMemcpyDeviceToDevice);
+    });
+}
+
+int ps_batch_set_stream(ps_batch *h, void *stream)
+{
+    return bguarded(h, [&](ps::Batch &b) { b.set_stream((cudaStream_t)stream); });
+}
+
+int ps_batch_synchronize(ps_batch *h)
+{
+    return bguarded(h, [&](ps::Batch &b) { PS_BCK(cudaStreamSynchronize(b.stream)); });
+}
+
+int ps_batch_get_info(const ps_batch *h, int what, double *value)
+{
+    if (!h || !h->b || !value) return PS_ERR_ARGUMENT;
+    const ps::Batch &b = *h->b;
+    switch (what) {
+    case PS_BATCH_INFO_LAUNCHES_PER_SOLVE: *value = 5; break;
+    case PS_BATCH_INFO_TILES_PER_SOLVE: *value = (double)b.tiles_per_solve(); break;
+    case PS_BATCH_INFO_POINTS: {
+        double pts = 0;
+        for (const auto &s : b.items) pts += (double)s->n[0] * s->n[1] * s->n[2];
+        *value = pts;
+        break;
+    }
+    default: return PS_ERR_ARGUMENT;
+    }
+    return PS_OK;
+}
+
+const char *ps_batch_last_error(const ps_batch *h)
+{
+    if (!h || !h->b) return "NULL batch handle";
+    return h->b->last_error.c_str();
+}
+
+}  // extern "C"

@@ -228,24 +228,23 @@ struct StageInfo {
     int lm[MAX_STAGES];   // log2(m) or -1
 };
 
+// One stage a thread (the caller synchronises before the first use).
 __device__ __forceinline__ void load_stages(StageInfo &si, const FftPlanDev &P)
 {
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int i = 0; i < MAX_STAGES; ++i) {
-            si.st[i] = make_int4(P.radix[i], P.m[i], P.tw[i], P.gw[i]);
-            si.lm[i] = P.lm[i];
-        }
+    const int i = threadIdx.x;
+    if (i < MAX_STAGES) {
+        si.st[i] = make_int4(P.radix[i], P.m[i], P.tw[i], P.gw[i]);
+        si.lm[i] = P.lm[i];
     }
 }
 
-// Copy the plan's twiddle table to shared memory and point the plan at it
-// (the caller synchronises before the first stage).
-template <typename C> __device__ __forceinline__ void stage_twiddles(FftPlanDev &P, C *TW)
+// Copy the plan's twiddle table to shared memory and return the copy, which
+// the stages read (the caller synchronises before the first stage).
+template <typename C> __device__ __forceinline__ const C *stage_twiddles(const FftPlanDev &P, C *TW)
 {
     const C *g = reinterpret_cast<const C *>(P.table);
     for (int i = threadIdx.x; i < P.ntw; i += blockDim.x) TW[i] = __ldg(&g[i]);
-    P.table = TW;
+    return TW;
 }
 
 // j = bf mod m and q = bf / m, by shifts when m is a power of two
@@ -262,11 +261,12 @@ __device__ __forceinline__ void split_index(int bf, int m, int lm, int &j, int &
 
 // One in-place Stockham stage with a compile-time radix.
 template <int EM, int R, bool INV, typename C>
-__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const FftPlanDev &P, int4 sd, int lm)
+__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws, int4 sd,
+                                      int lm)
 {
     constexpr int U = EM / R;
     const int L = P.L, m = sd.y, nbf = L / R, tpl = P.tpl;
-    const C *tw = reinterpret_cast<const C *>(P.table) + sd.z;  // shared-memory copy
+    const C *tw = tws + sd.z;
     C *Sb = S + b * sb;
     const int rstride = nbf * sn;
     C v[U][R];
@@ -307,11 +307,11 @@ __device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const 
 
 // A stage with a prime radix above 7: out of place into W, then copied back.
 template <bool INV, typename C>
-__device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, int4 sd)
+__device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws, int4 sd)
 {
     const int L = P.L, R = sd.x, m = sd.y, nbf = L / R, tpl = P.tpl;
-    const C *tw = reinterpret_cast<const C *>(P.table) + sd.z;
-    const C *gw = reinterpret_cast<const C *>(P.table) + sd.w;
+    const C *tw = tws + sd.z;
+    const C *gw = tws + sd.w;
     for (int bf = t; bf < nbf; bf += tpl) {
         const int j = bf % m, q = bf / m;
         const int base = q * R * m + j;
@@ -338,44 +338,46 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
     __syncthreads();
 }
 
-// Full transform of the CTA's lines. Threads with t >= tpl (never the case
-// with the launch shapes used) would idle through the barriers.
 // Full transform of the CTA's lines, for ncomp line sets cstride elements
 // apart. EM is the register elements a thread holds per stage (and the
-// largest radix); the plan's threads-per-line was computed for the same EM. The plan orders its stages as prime radices above 7, then 7s, 5s,
-// 3s, 16s (FP32 only), 8s, and at most one 4 or 2; each radix runs in its own
-// loop, with the line sets innermost, so that the register arrays of
-// different radices never share a live range (a radix switch inside one
-// stage loop, or the stage loops inside a component loop, made the register
-// allocator keep them all live and spill).
+// largest radix); the plan's threads-per-line was computed for the same EM.
+// Thread t of a line takes butterflies t, t + tpl, ...: a caller passes t = L
+// for a thread that must only join the barriers (every butterfly index it
+// would take is then past the stage's count).
+// The plan orders its stages as prime radices above 7, then 7s, 5s, 3s, 16s
+// (FP32 only), 8s, and at most one 4 or 2; each radix runs in its own loop,
+// with the line sets innermost, so that the register arrays of different
+// radices never share a live range (a radix switch inside one stage loop, or
+// the stage loops inside a component loop, made the register allocator keep
+// them all live and spill).
 // Radices without an unrolled butterfly: primes above 7 (11 and 13 included).
 __device__ __forceinline__ bool is_generic_radix(int R) { return R > 8 && R != 16; }
 
 template <bool INV, int EM, typename C>
-__device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+__device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws,
                                           const StageInfo &si, int ncomp = 1, int cstride = 0)
 {
     const int ns = P.nstages;
     int s = 0;
     for (; s < ns && is_generic_radix(si.st[s].x); ++s)
-        for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, si.st[s]);
+        for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, tws, si.st[s]);
     for (; s < ns && si.st[s].x == 7; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 7, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 7, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
     for (; s < ns && si.st[s].x == 5; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 5, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 5, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
     for (; s < ns && si.st[s].x == 3; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 3, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 3, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
     if constexpr (EM >= 16)
         for (; s < ns && si.st[s].x == 16; ++s)
-            for (int c = 0; c < ncomp; ++c) stage<EM, 16, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+            for (int c = 0; c < ncomp; ++c) stage<EM, 16, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
     for (; s < ns && si.st[s].x == 8; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 8, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 8, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
     if (s < ns && si.st[s].x == 4) {
-        for (int c = 0; c < ncomp; ++c) stage<EM, 4, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 4, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
         ++s;
     }
     if (s < ns && si.st[s].x == 2) {
-        for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
         ++s;
     }
 }

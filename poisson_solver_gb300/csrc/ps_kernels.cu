@@ -26,24 +26,31 @@ template <typename T> constexpr int EMZ = e_max_z(sizeof(T) == 8 ? PREC_FP64 : P
 // x forward. Line l of the CTA carries rows 2l (real part) and 2l+1 (imag
 // part); after the complex transform Z the two half spectra are
 // Xa[k] = (Z[k] + conj Z[L-k]) / 2 and Xb[k] = (Z[k] - conj Z[L-k]) / 2i.
+//
+// The pass bodies take the CTA's tile coordinates and its working thread count
+// nt explicitly, so the same code serves the per-problem launches and the
+// batched ones (one launch over the tiles of many problems, where a CTA may
+// have more threads than the problem of its tile uses). Threads tid >= nt only
+// join the barriers: their line-thread index is set to L, past every
+// butterfly, and the load/store loops skip them.
 template <typename T>
-__global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+__device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, int nt)
 {
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
     const int B = a.B, L = a.L, ld = L + 1;
     C *W = a.plan.generic ? S + B * ld : nullptr;
-    FftPlanDev plan = a.plan;
-    stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
+    const FftPlanDev &plan = a.plan;
+    const C *tws = stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
-    const int comp = blockIdx.y;
     const double *in = pick3(a.in, comp);
     C *out = reinterpret_cast<C *>(pick3(a.out, comp));
-    const int nt = blockDim.x, tid = threadIdx.x;
+    const int tid = threadIdx.x;
+    const bool live = tid < nt;
     const long long rows = (long long)a.rows_y * a.rows_z;
-    const long long row0 = (long long)blockIdx.x * 2 * B;
+    const long long row0 = (long long)bx * 2 * B;
     __shared__ long long rofs[2 * MAX_LINES];
     row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, a.Mx);
 
@@ -65,7 +72,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
             }
         }
         C *ln = S + line * ld;
-        for (int n = tid; n < L; n += nt) {
+        for (int n = live ? tid : L; n < L; n += nt) {
             T xa = (T)0, xb = (T)0;
             if (n < a.n_in) {
                 const int nn = a.mirror ? imin(n, L - n) : n;
@@ -76,14 +83,14 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
         }
     }
     __syncthreads();
-    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, tid / B, plan, si);
+    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : L, plan, tws, si);
 
     // separate the two half spectra and store
     const int Mx = a.Mx;
     for (int line = 0; line < B; ++line) {
         const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
         if (oa < 0) break;
-        for (int k = tid; k < Mx; k += nt) {
+        for (int k = live ? tid : Mx; k < Mx; k += nt) {
             const C z = S[line * ld + k], w = S[line * ld + (k == 0 ? 0 : L - k)];
             const T h = (T)0.5;
             out[oa + k] = C{h * (z.x + w.x), h * (z.y - w.y)};
@@ -92,11 +99,16 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     }
 }
 
+template <typename T> __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+{
+    xfwd_body<T>(a, blockIdx.x, blockIdx.y, blockDim.x);
+}
+
 // ---------------------------------------------------------------------------
 // Column transforms along a strided axis, in place: the CTA takes B adjacent
 // columns (one 128-byte row segment per sample for the default B) of one slab.
 template <typename T, bool INV>
-__global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
+__device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int comp, int nt)
 {
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -104,18 +116,17 @@ __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
     const int B = a.B, L = a.L;
     C *W = a.plan.generic ? S + L * B : nullptr;
     const int lb = __ffs(B) - 1;
-    FftPlanDev plan = a.plan;
-    stage_twiddles(plan, S + L * B * (a.plan.generic ? 2 : 1));
+    const FftPlanDev &plan = a.plan;
+    const C *tws = stage_twiddles(plan, S + L * B * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
-    const int comp = blockIdx.z;
-    const int x0 = blockIdx.x * B;
+    const int x0 = bx * B;
     const int nb = imin(B, a.Mx - x0);
-    C *base = reinterpret_cast<C *>(pick3(a.data, comp)) + (long long)blockIdx.y * a.outer_stride + x0;
-    const int nt = blockDim.x, tid = threadIdx.x;
+    C *base = reinterpret_cast<C *>(pick3(a.data, comp)) + (long long)slab * a.outer_stride + x0;
+    const int tid = threadIdx.x;
 
     // each thread keeps one column b and walks rows n = t, t + nt/B, ...
-    const int b = tid & (B - 1), t = tid >> lb, rstep = nt >> lb;
+    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : L, rstep = nt >> lb;
     const long long gstep = (long long)rstep * a.axis_stride;
     {
         const C *src = base + (long long)t * a.axis_stride + b;
@@ -128,12 +139,17 @@ __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
         }
     }
     __syncthreads();
-    fft_lines<INV, EMX<T>>(S, W, B, 1, b, t, plan, si);
+    fft_lines<INV, EMX<T>>(S, W, B, 1, b, t, plan, tws, si);
     if (b < nb) {
         C *dst = base + (long long)t * a.axis_stride + b;
 #pragma unroll 4
         for (int n = t; n < a.n_out; n += rstep, dst += gstep) *dst = S[n * B + b];
     }
+}
+
+template <typename T, bool INV> __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
+{
+    col_body<T, INV>(a, blockIdx.x, blockIdx.y, blockIdx.z, blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -149,9 +165,12 @@ __device__ __forceinline__ T wavenumber(int k, int P, T c, bool derivative)
     return (T)m * c;
 }
 
-template <typename T, int OP>
-__global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
+// OPT: the spectral operation, or -1 to take it from a.op at run time (the
+// batched pass); a fixed OPT folds every test on op away.
+template <typename T, int OPT>
+__device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
 {
+    const int op = OPT >= 0 ? OPT : a.op;
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
@@ -159,14 +178,14 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
     const int nbuf = a.nin > a.nout ? a.nin : a.nout;
     C *W = a.plan.generic ? S + nbuf * LB : nullptr;
     const int lb = __ffs(B) - 1;
-    const int x0 = blockIdx.x * B;
-    const int ky = a.ky0 + blockIdx.y;
+    const int x0 = bx * B;
+    const int ky = a.ky0 + by;
     const int nb = imin(B, a.Mx - x0);
     const long long off = (long long)ky * a.row_stride + x0;
-    const int nt = blockDim.x, tid = threadIdx.x;
-    const int b = tid & (B - 1), t = tid >> lb;
-    FftPlanDev plan = a.plan;
-    stage_twiddles(plan, S + (nbuf + (a.plan.generic ? 1 : 0)) * LB);
+    const int tid = threadIdx.x;
+    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : L;
+    const FftPlanDev &plan = a.plan;
+    const C *tws = stage_twiddles(plan, S + (nbuf + (a.plan.generic ? 1 : 0)) * LB);
     __shared__ StageInfo si;
     load_stages(si, a.plan);
 
@@ -184,9 +203,9 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
         }
     }
     __syncthreads();
-    fft_lines<false, EMZ<T>>(S, W, B, 1, b, t, plan, si, a.nin, LB);
+    fft_lines<false, EMZ<T>>(S, W, B, 1, b, t, plan, tws, si, a.nin, LB);
 
-    if constexpr (OP != OP_FORWARD) {
+    if (op != OP_FORWARD) {
         // the thread's column kx is fixed; it walks kz = t, t + nt/B, ...
         const int oy = imin(ky, a.Py - ky);
         const int kx = x0 + b;
@@ -200,9 +219,9 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
             const int oz = imin(n, a.Pz - n);
             const T g = Kc[oz * kzs];
             const T kzv = wavenumber<T>(n, a.Pz, kzc, true);
-            if constexpr (OP == OP_NONE) {
+            if (op == OP_NONE) {
                 for (int c = 0; c < a.nin; ++c) S[c * LB + idx] = cscale(S[c * LB + idx], g);
-            } else if constexpr (OP == OP_GRAD) {
+            } else if (op == OP_GRAD) {
                 // out_d = i k_d K in_d; in_d falls back to component x
                 const C i0 = S[idx];
                 const C i1 = a.nin > 1 ? S[LB + idx] : i0;
@@ -211,11 +230,11 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
                 S[idx] = C{-gx * i0.y, gx * i0.x};
                 S[LB + idx] = C{-gy * i1.y, gy * i1.x};
                 S[2 * LB + idx] = C{-gz * i2.y, gz * i2.x};
-            } else if constexpr (OP == OP_DIV) {
+            } else if (op == OP_DIV) {
                 const C i0 = S[idx], i1 = S[LB + idx], i2 = S[2 * LB + idx];
                 const C s = C{kxv * i0.x + kyv * i1.x + kzv * i2.x, kxv * i0.y + kyv * i1.y + kzv * i2.y};
                 S[idx] = C{-g * s.y, g * s.x};
-            } else if constexpr (OP == OP_CURL) {
+            } else if (op == OP_CURL) {
                 const C i0 = S[idx], i1 = S[LB + idx], i2 = S[2 * LB + idx];
                 const C c0 = C{kyv * i2.x - kzv * i1.x, kyv * i2.y - kzv * i1.y};
                 const C c1 = C{kzv * i0.x - kxv * i2.x, kzv * i0.y - kxv * i2.y};
@@ -223,7 +242,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
                 S[idx] = C{-g * c0.y, g * c0.x};
                 S[LB + idx] = C{-g * c1.y, g * c1.x};
                 S[2 * LB + idx] = C{-g * c2.y, g * c2.x};
-            } else if constexpr (OP == OP_FILTER) {
+            } else if (op == OP_FILTER) {
                 const T z = (reinterpret_cast<const T *>(a.zeta) + (long long)oy * a.Mx + kx)[oz * kzs];
                 if (a.reproject && a.nin == 3) {
                     // r'_c = z r_c - K sum_d k_c k_d r_d. A product k_c k_d is
@@ -251,7 +270,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
             }
         }
         __syncthreads();
-        fft_lines<true, EMZ<T>>(S, W, B, 1, b, t, plan, si, a.nout, LB);
+        fft_lines<true, EMZ<T>>(S, W, B, 1, b, t, plan, tws, si, a.nout, LB);
     }
 
     if (b < nb) {
@@ -266,35 +285,40 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
     }
 }
 
+template <typename T, int OP> __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
+{
+    z_body<T, OP>(a, blockIdx.x, blockIdx.y, blockDim.x);
+}
+
 // ---------------------------------------------------------------------------
 // x inverse. Line l rebuilds Z = Xa + i Xb over the full length from the two
 // half spectra (Z[L-k] = conj Xa[k] + i conj Xb[k]), transforms back and
 // writes Re -> row 2l, Im -> row 2l+1, first n_out samples only.
 template <typename T>
-__global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+__device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, int nt)
 {
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
     const int B = a.B, L = a.L, ld = L + 1, Mx = a.Mx;
     C *W = a.plan.generic ? S + B * ld : nullptr;
-    FftPlanDev plan = a.plan;
-    stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
+    const FftPlanDev &plan = a.plan;
+    const C *tws = stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
-    const int comp = blockIdx.y;
     const C *in = reinterpret_cast<const C *>(pick3(a.in, comp));
     double *out = pick3(a.out, comp);
-    const int nt = blockDim.x, tid = threadIdx.x;
+    const int tid = threadIdx.x;
+    const bool live = tid < nt;
     const long long rows = (long long)a.rows_y * a.rows_z;
-    const long long row0 = (long long)blockIdx.x * 2 * B;
+    const long long row0 = (long long)bx * 2 * B;
     __shared__ long long rofs[2 * MAX_LINES];
     row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
     __syncthreads();
 
     for (int line = 0; line < B; ++line) {
         const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
-        for (int k = tid; k < Mx; k += nt) {
+        for (int k = live ? tid : Mx; k < Mx; k += nt) {
             C xa = C{0, 0}, xb = C{0, 0};
             if (oa >= 0) xa = in[oa + k];
             if (ob >= 0) xb = in[ob + k];
@@ -303,7 +327,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
         }
     }
     __syncthreads();
-    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, tid / B, plan, si);
+    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : L, plan, tws, si);
 
     // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;
@@ -313,11 +337,85 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
         const bool vb = ra + 1 < rows;
         double *oa = out + ra * a.out_stride, *ob = oa + a.out_stride;
         const C *ln = S + line * ld;
-        for (int n = tid; n < no; n += nt) {
+        for (int n = live ? tid : no; n < no; n += nt) {
             const C v = ln[n];
             oa[n] = (double)v.x;
             if (vb) ob[n] = (double)v.y;
         }
+    }
+}
+
+template <typename T> __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+{
+    xinv_body<T>(a, blockIdx.x, blockIdx.y, blockDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// Batched passes: one launch runs a pass of many independent problems. Each
+// persistent CTA walks the tile list (tile i, i + gridDim.x, ...), copies the
+// arguments of its tile's problem into shared memory and runs the pass body
+// with that problem's thread count (the launch's block size is the largest
+// of them). With the arguments in memory rather than in the constant bank the
+// bodies need more registers: up to 255 a thread at 256 threads a CTA keeps
+// them from spilling (at 512 threads ptxas held them to 64 and spilled
+// 0.6-6.6 KB a thread).
+template <typename Args> __device__ __forceinline__ void load_args(Args &dst, const Args *src)
+{
+    static_assert(sizeof(Args) % sizeof(int) == 0, "argument blocks are whole words");
+    const int *s = reinterpret_cast<const int *>(src);
+    int *d = reinterpret_cast<int *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(Args) / sizeof(int)); i += blockDim.x) d[i] = s[i];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_xfwd_batch(const XFwdArgs *args, const BatchTile *tiles, int ntiles)
+{
+    __shared__ XFwdArgs a;
+    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
+        const BatchTile tl = tiles[i];
+        __syncthreads();  // the previous tile no longer reads a or the shared buffers
+        load_args(a, args + tl.p);
+        __syncthreads();
+        xfwd_body<T>(a, tl.bx, tl.by, a.B * a.plan.tpl);
+    }
+}
+
+template <typename T, bool INV>
+__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_col_batch(const ColArgs *args, const BatchTile *tiles, int ntiles)
+{
+    __shared__ ColArgs a;
+    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
+        const BatchTile tl = tiles[i];
+        __syncthreads();
+        load_args(a, args + tl.p);
+        __syncthreads();
+        col_body<T, INV>(a, tl.bx, tl.by, tl.bz, a.B * a.plan.tpl);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_z_batch(const ZArgs *args, const BatchTile *tiles, int ntiles)
+{
+    __shared__ ZArgs a;
+    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
+        const BatchTile tl = tiles[i];
+        __syncthreads();
+        load_args(a, args + tl.p);
+        __syncthreads();
+        z_body<T, -1>(a, tl.bx, tl.by, a.B * a.plan.tpl);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_xinv_batch(const XInvArgs *args, const BatchTile *tiles, int ntiles)
+{
+    __shared__ XInvArgs a;
+    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
+        const BatchTile tl = tiles[i];
+        __syncthreads();
+        load_args(a, args + tl.p);
+        __syncthreads();
+        xinv_body<T>(a, tl.bx, tl.by, a.B * a.plan.tpl);
     }
 }
 
@@ -441,6 +539,91 @@ cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
     } else {
         if ((e = prep(k_xinv<float>, sm)) != cudaSuccess) return e;
         k_xinv<float><<<grid, nt, sm, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+// Batched launchers: nt threads and smem bytes a CTA (the largest over the
+// batch's problems), as many persistent CTAs as fit on the GPU at once.
+template <typename K> static cudaError_t launch_persistent(K kernel, int ntiles, int nt, size_t smem, cudaStream_t st,
+                                                          int &grid)
+{
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, dev = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, smem)) != cudaSuccess) return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    grid = ntiles < per_sm * sms ? ntiles : per_sm * sms;
+    return cudaSuccess;
+}
+
+cudaError_t launch_xfwd_batch(int prec, const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                              cudaStream_t st)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    int grid = 0;
+    cudaError_t e;
+    if (prec == PREC_FP64) {
+        if ((e = launch_persistent(k_xfwd_batch<double>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
+        k_xfwd_batch<double><<<grid, nt, smem, st>>>(args, tiles, ntiles);
+    } else {
+        if ((e = launch_persistent(k_xfwd_batch<float>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
+        k_xfwd_batch<float><<<grid, nt, smem, st>>>(args, tiles, ntiles);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col_batch(int prec, int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt,
+                             size_t smem, cudaStream_t st)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    int grid = 0;
+    cudaError_t e;
+#define PS_LAUNCH_COLB(T, I)                                                                            \
+    do {                                                                                                \
+        if ((e = launch_persistent(k_col_batch<T, I>, ntiles, nt, smem, st, grid)) != cudaSuccess)      \
+            return e;                                                                                   \
+        k_col_batch<T, I><<<grid, nt, smem, st>>>(args, tiles, ntiles);                                 \
+    } while (0)
+    if (prec == PREC_FP64) {
+        if (inverse) PS_LAUNCH_COLB(double, true); else PS_LAUNCH_COLB(double, false);
+    } else {
+        if (inverse) PS_LAUNCH_COLB(float, true); else PS_LAUNCH_COLB(float, false);
+    }
+#undef PS_LAUNCH_COLB
+    return cudaGetLastError();
+}
+
+cudaError_t launch_z_batch(int prec, const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                           cudaStream_t st)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    int grid = 0;
+    cudaError_t e;
+    if (prec == PREC_FP64) {
+        if ((e = launch_persistent(k_z_batch<double>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
+        k_z_batch<double><<<grid, nt, smem, st>>>(args, tiles, ntiles);
+    } else {
+        if ((e = launch_persistent(k_z_batch<float>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
+        k_z_batch<float><<<grid, nt, smem, st>>>(args, tiles, ntiles);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xinv_batch(int prec, const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                              cudaStream_t st)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    int grid = 0;
+    cudaError_t e;
+    if (prec == PREC_FP64) {
+        if ((e = launch_persistent(k_xinv_batch<double>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
+        k_xinv_batch<double><<<grid, nt, smem, st>>>(args, tiles, ntiles);
+    } else {
+        if ((e = launch_persistent(k_xinv_batch<float>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
+        k_xinv_batch<float><<<grid, nt, smem, st>>>(args, tiles, ntiles);
     }
     return cudaGetLastError();
 }

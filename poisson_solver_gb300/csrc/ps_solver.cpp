@@ -426,7 +426,7 @@ int Solver::output_mask(int in_mask) const
     return in_mask;
 }
 
-int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter_only)
+int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filter_only, PassArgs &pa)
 {
     check_setup();
     int in_mask = 0;
@@ -451,6 +451,118 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     if (op == OP_FILTER) ensure_zeta(prec);
     for (int c = 0; c < 3; ++c)
         if ((in_mask | out_mask) >> c & 1) work[c].ensure(work_elems() * csz);
+    pa = PassArgs{};
+    pa.write_mask = write_mask;
+
+    // x forward over the pushed components
+    XFwdArgs &xa = pa.x;
+    for (int c = 0; c < 3; ++c)
+        if (in_mask >> c & 1) {
+            xa.in[xa.ncomp] = Bin[c];
+            xa.out[xa.ncomp] = work[c].p;
+            ++xa.ncomp;
+        }
+    xa.L = P[0];
+    xa.n_in = n[0];
+    xa.in_stride = n[0];
+    xa.rows_y = n[1];
+    xa.rows_z = n[2];
+    xa.out_y = P[1];
+    xa.Mx = Mx;
+
+    // y forward (zero-padded from Ny to Py)
+    ColArgs &ya = pa.y;
+    for (int c = 0; c < 3; ++c)
+        if (in_mask >> c & 1) ya.data[ya.ncomp++] = work[c].p;
+    ya.L = P[1];
+    ya.n_in = n[1];
+    ya.n_out = P[1];
+    ya.Mx = Mx;
+    ya.axis_stride = Mx;
+    ya.outer_stride = (long long)P[1] * Mx;
+
+    // z: forward (zero-padded from Nz to Pz), spectral operation, inverse (cropped)
+    ZArgs &za = pa.z;
+    if (op == OP_GRAD) {
+        if (in_mask == 1) {
+            za.nin = 1;
+            za.in[0] = work[0].p;
+        } else {
+            za.nin = 3;
+            for (int d = 0; d < 3; ++d) za.in[d] = work[(in_mask >> d & 1) ? d : 0].p;
+        }
+        za.nout = 0;
+        for (int d = 0; d < 3; ++d) za.out[za.nout++] = (write_mask >> d & 1) ? work[d].p : nullptr;
+    } else if (op == OP_DIV || op == OP_CURL) {
+        za.nin = 3;
+        for (int d = 0; d < 3; ++d) za.in[d] = work[d].p;
+        za.nout = op == OP_DIV ? 1 : 3;
+        for (int d = 0; d < za.nout; ++d) za.out[d] = (write_mask >> d & 1) ? work[d].p : nullptr;
+    } else {
+        for (int c = 0; c < 3; ++c)
+            if (in_mask >> c & 1) {
+                za.in[za.nin] = work[c].p;
+                za.out[za.nin] = (write_mask >> c & 1) ? work[c].p : nullptr;
+                ++za.nin;
+            }
+        za.nout = za.nin;
+    }
+    za.L = P[2];
+    za.n_in = n[2];
+    za.n_out = n[2];
+    za.Mx = Mx;
+    za.axis_stride = (long long)P[1] * Mx;
+    za.row_stride = Mx;
+    za.op = op;
+    za.reproject = op == OP_FILTER && opt_reproject && in_mask == 7;
+    za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
+    za.zeta = op == OP_FILTER ? (prec == PREC_FP64 ? zeta64.p : zeta32.p) : nullptr;
+    za.oct_y = oy;
+    za.Px = P[0];
+    za.Py = P[1];
+    za.Pz = P[2];
+    za.kxc = 2.0 * M_PI / ((double)P[0] * dx[0]);
+    za.kyc = 2.0 * M_PI / ((double)P[1] * dx[1]);
+    za.kzc = 2.0 * M_PI / ((double)P[2] * dx[2]);
+
+    // y inverse (cropped to Ny) and x inverse (cropped to Nx) of the written outputs
+    ColArgs &yi = pa.yi;
+    for (int c = 0; c < 3; ++c)
+        if (write_mask >> c & 1) yi.data[yi.ncomp++] = work[c].p;
+    yi.L = P[1];
+    yi.n_in = P[1];
+    yi.n_out = n[1];
+    yi.Mx = Mx;
+    yi.axis_stride = Mx;
+    yi.outer_stride = (long long)P[1] * Mx;
+
+    XInvArgs &xi = pa.xi;
+    for (int c = 0; c < 3; ++c)
+        if (write_mask >> c & 1) {
+            xi.in[xi.ncomp] = work[c].p;
+            xi.out[xi.ncomp] = Aout[c];
+            ++xi.ncomp;
+        }
+    xi.L = P[0];
+    xi.n_out = n[0];
+    xi.Mx = Mx;
+    xi.rows_y = n[1];
+    xi.rows_z = n[2];
+    xi.in_y = P[1];
+    xi.out_stride = n[0];
+    return write_mask;
+}
+
+int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter_only)
+{
+    PassArgs pa;
+    const int write_mask = prepare(Bin, Aout, filter_only, pa);
+    const int prec = precision, op = pa.z.op;
+    XFwdArgs &xa = pa.x;
+    ColArgs &ya = pa.y, &yi = pa.yi;
+    ZArgs &za = pa.z;
+    XInvArgs &xi = pa.xi;
+
     // Kernel family per axis. FP32: the wide kernels for the y and z passes
     // (lengths 256..2048), the length-specialised ones for x (measured faster
     // there: 2.3 vs 3.4 ms for the 512^3 forward x pass) and for other
@@ -497,20 +609,6 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     mark(0);
 
     // x forward over the pushed components
-    XFwdArgs xa{};
-    for (int c = 0; c < 3; ++c)
-        if (in_mask >> c & 1) {
-            xa.in[xa.ncomp] = Bin[c];
-            xa.out[xa.ncomp] = work[c].p;
-            ++xa.ncomp;
-        }
-    xa.L = P[0];
-    xa.n_in = n[0];
-    xa.in_stride = n[0];
-    xa.rows_y = n[1];
-    xa.rows_z = n[2];
-    xa.out_y = P[1];
-    xa.Mx = Mx;
     xa.plan = px.dev;
     if (wx) {
         xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return wide::smem_lines(P[0], B, 1, px.dev.ntw, false); },
@@ -527,16 +625,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     }
     mark(1);
 
-    // y forward (zero-padded from Ny to Py)
-    ColArgs ya{};
-    for (int c = 0; c < 3; ++c)
-        if (in_mask >> c & 1) ya.data[ya.ncomp++] = work[c].p;
-    ya.L = P[1];
-    ya.n_in = n[1];
-    ya.n_out = P[1];
-    ya.Mx = Mx;
-    ya.axis_stride = Mx;
-    ya.outer_stride = (long long)P[1] * Mx;
+    // y forward
     ya.plan = py.dev;
     if (wy) {
         ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return wide::smem_lines(P[1], B, 1, py.dev.ntw, true); },
@@ -552,49 +641,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     }
     mark(2);
 
-    // z: forward (zero-padded from Nz to Pz), spectral operation, inverse (cropped)
-    ZArgs za{};
-    if (op == OP_GRAD) {
-        if (in_mask == 1) {
-            za.nin = 1;
-            za.in[0] = work[0].p;
-        } else {
-            za.nin = 3;
-            for (int d = 0; d < 3; ++d) za.in[d] = work[(in_mask >> d & 1) ? d : 0].p;
-        }
-        za.nout = 0;
-        for (int d = 0; d < 3; ++d) za.out[za.nout++] = (write_mask >> d & 1) ? work[d].p : nullptr;
-    } else if (op == OP_DIV || op == OP_CURL) {
-        za.nin = 3;
-        for (int d = 0; d < 3; ++d) za.in[d] = work[d].p;
-        za.nout = op == OP_DIV ? 1 : 3;
-        for (int d = 0; d < za.nout; ++d) za.out[d] = (write_mask >> d & 1) ? work[d].p : nullptr;
-    } else {
-        for (int c = 0; c < 3; ++c)
-            if (in_mask >> c & 1) {
-                za.in[za.nin] = work[c].p;
-                za.out[za.nin] = (write_mask >> c & 1) ? work[c].p : nullptr;
-                ++za.nin;
-            }
-        za.nout = za.nin;
-    }
-    za.L = P[2];
-    za.n_in = n[2];
-    za.n_out = n[2];
-    za.Mx = Mx;
-    za.axis_stride = (long long)P[1] * Mx;
-    za.row_stride = Mx;
-    za.op = op;
-    za.reproject = op == OP_FILTER && opt_reproject && in_mask == 7;
-    za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
-    za.zeta = op == OP_FILTER ? (prec == PREC_FP64 ? zeta64.p : zeta32.p) : nullptr;
-    za.oct_y = oy;
-    za.Px = P[0];
-    za.Py = P[1];
-    za.Pz = P[2];
-    za.kxc = 2.0 * M_PI / ((double)P[0] * dx[0]);
-    za.kyc = 2.0 * M_PI / ((double)P[1] * dx[1]);
-    za.kzc = 2.0 * M_PI / ((double)P[2] * dx[2]);
+    // z forward, spectral operation, z inverse
     za.plan = pz.dev;
     const int nbuf = std::max(za.nin, za.nout);
     // The wide z family runs as the tensor-memory kernel unless
@@ -624,15 +671,6 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
 
     // y inverse (cropped to Ny) and x inverse (cropped to Nx) of the written outputs
     if (write_mask) {
-        ColArgs yi{};
-        for (int c = 0; c < 3; ++c)
-            if (write_mask >> c & 1) yi.data[yi.ncomp++] = work[c].p;
-        yi.L = P[1];
-        yi.n_in = P[1];
-        yi.n_out = n[1];
-        yi.Mx = Mx;
-        yi.axis_stride = Mx;
-        yi.outer_stride = (long long)P[1] * Mx;
         yi.plan = py.dev;
         yi.B = ya.B;
         if (wy) PS_CK(wide::launch_col(1, yi, n[2], stream));
@@ -640,20 +678,6 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         else PS_CK(launch_col(prec, 1, yi, n[2], stream));
         mark(4);
 
-        XInvArgs xi{};
-        for (int c = 0; c < 3; ++c)
-            if (write_mask >> c & 1) {
-                xi.in[xi.ncomp] = work[c].p;
-                xi.out[xi.ncomp] = Aout[c];
-                ++xi.ncomp;
-            }
-        xi.L = P[0];
-        xi.n_out = n[0];
-        xi.Mx = Mx;
-        xi.rows_y = n[1];
-        xi.rows_z = n[2];
-        xi.in_y = P[1];
-        xi.out_stride = n[0];
         xi.plan = px.dev;
         xi.B = xa.B;
         if (wx) PS_CK(wide::launch_xinv(xi, stream));

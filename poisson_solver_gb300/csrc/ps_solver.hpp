@@ -38,6 +38,17 @@ struct Plan {
     DevBuf table;
 };
 
+// Arguments of the five passes of one solve, all but the plans and the lines
+// per CTA (which depend on the kernel family that runs each pass).
+struct PassArgs {
+    XFwdArgs x{};
+    ColArgs y{};
+    ZArgs z{};
+    ColArgs yi{};
+    XInvArgs xi{};
+    int write_mask = 0;  // outputs written; 0 skips the inverse y and x passes
+};
+
 struct Solver {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -81,6 +92,9 @@ struct Solver {
     // Device-pointer pipeline. B: input components (NULL = absent); A: outputs.
     // Returns the mask of components written to A.
     int solve(const double *const Bin[3], double *const Aout[3], bool filter_only = false);
+    // The pass arguments of that solve (buffers and the kernel ensured);
+    // returns the mask of components written.
+    int prepare(const double *const Bin[3], double *const Aout[3], bool filter_only, PassArgs &pa);
     // Mask of outputs a solve produces for the given input mask (throws on a
     // combination the options reject).
     int output_mask(int in_mask) const;

@@ -117,6 +117,22 @@ cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaS
 cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st);
 cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st);
 
+// Batched passes (ps_kernels.cu): one launch runs the tiles of many problems.
+// Tile = (problem, bx, by, bz): x passes (line block, component); y passes
+// (column block, z slab, component); z pass (column block, ky row).
+struct BatchTile {
+    int p, bx, by, bz;
+};
+constexpr int BATCH_MAX_THREADS = 256;  // CTA size bound of the batched passes
+cudaError_t launch_xfwd_batch(int prec, const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                              cudaStream_t st);
+cudaError_t launch_col_batch(int prec, int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt,
+                             size_t smem, cudaStream_t st);
+cudaError_t launch_z_batch(int prec, const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                           cudaStream_t st);
+cudaError_t launch_xinv_batch(int prec, const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                              cudaStream_t st);
+
 // Shared-memory bytes each pass needs for a given line count (data, scratch
 // for direct-DFT stages, twiddle table).
 size_t smem_x(int prec, const FftPlanDev &p, int B);

@@ -178,6 +178,104 @@ class PoissonSolver:
         return tuple(int(self.info(w)) for w in (L.PS_INFO_PADDED_X, L.PS_INFO_PADDED_Y, L.PS_INFO_PADDED_Z))
 
 
+class PoissonBatch:
+    """Many independent problems solved together (no single reference call:
+    the reference holds one poisson_solver object per problem).
+
+    ``add`` stands for setup3d of one problem and returns its index;
+    ``push``/``pull``/``set_return_*`` take that index first. ``solve`` runs
+    every problem with one launch per pass, replayed through a CUDA graph.
+    """
+
+    def __init__(self, precision: str = "fp64"):
+        self._lib = L.load()
+        prec = {"fp64": L.PS_PREC_FP64, "fp32": L.PS_PREC_FP32}[precision]
+        h = ctypes.c_void_p()
+        st = self._lib.ps_batch_create(ctypes.byref(h), prec)
+        if st != L.PS_OK:
+            raise L.PSError(st, self._lib.ps_status_string(st).decode())
+        self._h = h
+        self._shapes: list[tuple] = []
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.ps_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self._shapes)
+
+    def _call(self, name, *args):
+        st = getattr(self._lib, name)(self._h, *args)
+        if st != L.PS_OK:
+            msg = self._lib.ps_batch_last_error(self._h)
+            raise L.PSError(st, msg.decode() if msg else self._lib.ps_status_string(st).decode())
+
+    def add(self, ncell, bc, dx, reg_order: int = 0) -> int:
+        nc = (ctypes.c_int * 3)(*[int(v) for v in ncell])
+        b = (ctypes.c_int * 3)(*[int(v) for v in bc])
+        d = (ctypes.c_double * 3)(*[float(v) for v in dx])
+        idx = ctypes.c_int()
+        self._call("ps_batch_add", nc, b, d, int(reg_order), ctypes.byref(idx))
+        self._shapes.append((int(ncell[2]), int(ncell[1]), int(ncell[0])))
+        return idx.value
+
+    def set_return_grad(self, i: int, toggle: bool):
+        self._call("ps_batch_set_option", int(i), L.PS_OPT_GRAD, int(bool(toggle)))
+
+    def set_return_div(self, i: int, toggle: bool):
+        self._call("ps_batch_set_option", int(i), L.PS_OPT_DIV, int(bool(toggle)))
+
+    def set_return_curl(self, i: int, toggle: bool):
+        self._call("ps_batch_set_option", int(i), L.PS_OPT_CURL, int(bool(toggle)))
+
+    def set_reprojection(self, i: int, toggle: bool):
+        self._call("ps_batch_set_option", int(i), L.PS_OPT_REPROJECT, int(bool(toggle)))
+
+    def push(self, i: int, bx, by=None, bz=None):
+        s = self._shapes[i]
+        self._call("ps_batch_push", int(i), _host_ptr(bx, s, "Bx"), _host_ptr(by, s, "By"), _host_ptr(bz, s, "Bz"))
+
+    def push_device(self, i: int, bx, by=0, bz=0):
+        self._call("ps_batch_push_device", int(i), bx or None, by or None, bz or None)
+
+    def solve(self):
+        self._call("ps_batch_solve")
+
+    def pull(self, i: int, ax=None, ay=None, az=None):
+        s = self._shapes[i]
+        self._call("ps_batch_pull", int(i), _host_ptr(ax, s, "Ax", True), _host_ptr(ay, s, "Ay", True),
+                   _host_ptr(az, s, "Az", True))
+
+    def pull_device(self, i: int, ax=0, ay=0, az=0):
+        self._call("ps_batch_pull_device", int(i), ax or None, ay or None, az or None)
+
+    def set_stream(self, stream_handle: int):
+        self._call("ps_batch_set_stream", ctypes.c_void_p(int(stream_handle)))
+
+    def synchronize(self):
+        self._call("ps_batch_synchronize")
+
+    def info(self, what: int) -> float:
+        v = ctypes.c_double()
+        st = self._lib.ps_batch_get_info(self._h, int(what), ctypes.byref(v))
+        if st != L.PS_OK:
+            raise L.PSError(st, self._lib.ps_status_string(st).decode())
+        return v.value
+
+
 def solve(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,
           reproject=False, precision="fp64", want_rhs=False):
     """One-shot host solve; returns (A, RB) lists of 3 arrays or None."""

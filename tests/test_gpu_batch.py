@@ -1,0 +1,174 @@
+"""Batched solves (ps_batch_*): many independent problems in one launch per pass.
+
+Every problem of a mixed batch -- odd and prime sizes, all four boundary
+families, 1-3 components, none/grad/div/curl -- is checked against the
+oracle. In FP64 the batched result must also equal the single-problem solve
+bit for bit: both run the same run-time transform kernels, whose per-line
+arithmetic does not depend on how many lines a CTA holds.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 5e-6
+
+# (ncell, bc, components, options)
+PROBLEMS = [
+    ((12, 10, 8), (0, 0, 0), (0,), dict()),
+    ((7, 11, 13), (1, 1, 1), (0, 1, 2), dict(curl=True)),
+    ((16, 9, 10), (1, 1, 0), (0, 1, 2), dict(div=True)),
+    ((10, 14, 6), (0, 0, 1), (0,), dict(grad=True)),
+    ((20, 6, 9), (0, 0, 0), (0, 1, 2), dict(grad=True)),
+    ((5, 5, 5), (0, 0, 0), (1, 2), dict()),
+    ((24, 16, 12), (0, 0, 0), (0, 1, 2), dict(curl=True)),
+    ((9, 13, 11), (1, 1, 1), (2,), dict()),
+    ((1, 8, 6), (0, 0, 0), (0,), dict()),
+    ((18, 20, 7), (1, 1, 0), (0, 1), dict()),
+    ((11, 11, 22), (0, 0, 1), (0, 1, 2), dict(curl=True)),
+]
+
+
+def _fields(nc, comps, seed, zero_mean):
+    rng = np.random.default_rng(seed)
+    shape = (nc[2], nc[1], nc[0])
+    out = []
+    for c in range(3):
+        if c not in comps:
+            out.append(None)
+            continue
+        f = rng.standard_normal(shape)
+        if zero_mean:
+            f -= f.mean(axis=(1, 2), keepdims=True)
+        out.append(f)
+    return out
+
+
+def _dx(nc):
+    return (2.0 / nc[0], 1.7 / nc[1], 2.3 / nc[2])
+
+
+def _make(psg, precision, seed=0):
+    b = psg.PoissonBatch(precision)
+    data = []
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS):
+        idx = b.add(nc, bc, _dx(nc), (0, 2, 6)[i % 3])
+        assert idx == i
+        if opts.get("grad"):
+            b.set_return_grad(i, True)
+        if opts.get("div"):
+            b.set_return_div(i, True)
+        if opts.get("curl"):
+            b.set_return_curl(i, True)
+        B = _fields(nc, comps, 100 * seed + i, zero_mean=bc == (1, 1, 0))
+        b.push(i, *B)
+        data.append(B)
+    return b, data
+
+
+def _pull(b, i):
+    nc = PROBLEMS[i][0]
+    shape = (nc[2], nc[1], nc[0])
+    A = [np.full(shape, np.nan) for _ in range(3)]
+    b.pull(i, *A)
+    return [a if not np.isnan(a).all() else None for a in A]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_vs_oracle(native, oracle, precision):
+    b, data = _make(native, precision)
+    b.solve()
+    tol = FP64_TOL if precision == "fp64" else FP32_TOL
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS):
+        ref, _ = oracle.solve3d(nc, bc, _dx(nc), data[i], (0, 2, 6)[i % 3], **opts)
+        got = _pull(b, i)
+        assert rel_l2(got, ref) < tol, (i, nc, bc, opts)
+    assert b.info(native._lib.PS_BATCH_INFO_LAUNCHES_PER_SOLVE) == 5
+    assert b.info(native._lib.PS_BATCH_INFO_POINTS) == sum(np.prod(p[0]) for p in PROBLEMS)
+    b.close()
+
+
+def test_batch_fp64_equals_single_solves(native):
+    b, data = _make(native, "fp64", seed=3)
+    b.solve()
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS):
+        single, _ = native.solve(nc, bc, _dx(nc), data[i], (0, 2, 6)[i % 3], **opts)
+        got = _pull(b, i)
+        for g, s in zip(got, single):
+            assert (g is None) == (s is None)
+            if g is not None:
+                assert np.array_equal(g, s), (i, nc, bc, opts)
+    b.close()
+
+
+def test_batch_replay_with_new_data_and_option_change(native, oracle):
+    b, data = _make(native, "fp64", seed=5)
+    b.solve()
+    # same components, new values: the captured graph is replayed
+    nc, bc, comps, opts = PROBLEMS[6]
+    B2 = _fields(nc, comps, 999, zero_mean=False)
+    b.push(6, *B2)
+    b.solve()
+    ref, _ = oracle.solve3d(nc, bc, _dx(nc), B2, (0, 2, 6)[6 % 3], **opts)
+    assert rel_l2(_pull(b, 6), ref) < FP64_TOL
+    # untouched problems keep their results
+    nc0, bc0, _, opts0 = PROBLEMS[0]
+    ref0, _ = oracle.solve3d(nc0, bc0, _dx(nc0), data[0], 0, **opts0)
+    assert rel_l2(_pull(b, 0), ref0) < FP64_TOL
+    # an option change forces a new capture
+    b.set_return_curl(6, False)
+    b.solve()
+    ref, _ = oracle.solve3d(nc, bc, _dx(nc), B2, (0, 2, 6)[6 % 3])
+    assert rel_l2(_pull(b, 6), ref) < FP64_TOL
+    b.close()
+
+
+def test_batch_errors(native):
+    from poisson_solver_gb300 import PSError
+    from poisson_solver_gb300 import _lib as L
+    b = native.PoissonBatch("fp64")
+    with pytest.raises(PSError) as e:
+        b.solve()
+    assert e.value.status == L.PS_ERR_STATE
+    b.add((8, 8, 8), (0, 0, 0), (0.1, 0.1, 0.1), 0)
+    b.add((6, 6, 6), (1, 1, 1), (0.1, 0.1, 0.1), 0)
+    b.push(0, np.ones((8, 8, 8)))
+    with pytest.raises(PSError) as e:
+        b.solve()  # problem 1 has nothing pushed
+    assert e.value.status == L.PS_ERR_STATE
+    with pytest.raises(PSError) as e:
+        b.set_return_curl(5, True)
+    assert e.value.status == L.PS_ERR_ARGUMENT
+    b.set_return_curl(0, True)
+    b.push(1, np.ones((6, 6, 6)))
+    with pytest.raises(PSError) as e:
+        b.solve()  # curl of a scalar
+    assert e.value.status == L.PS_ERR_COMPONENTS
+    b.close()
+
+
+def test_batch_device_pointers_on_a_stream(native, oracle):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    b = native.PoissonBatch("fp64")
+    st = torch.cuda.Stream()
+    b.set_stream(st.cuda_stream)
+    shapes = [((10, 8, 12), (0, 0, 0)), ((9, 9, 9), (1, 1, 1))]
+    fields = []
+    for i, (nc, bc) in enumerate(shapes):
+        b.add(nc, bc, _dx(nc), 2)
+        f = torch.randn((nc[2], nc[1], nc[0]), dtype=torch.float64, device=dev)
+        fields.append(f)
+        b.push_device(i, f.data_ptr())
+    b.solve()
+    outs = [torch.empty_like(f) for f in fields]
+    for i, o in enumerate(outs):
+        b.pull_device(i, o.data_ptr())
+    b.synchronize()
+    for (nc, bc), f, o in zip(shapes, fields, outs):
+        ref, _ = oracle.solve3d(nc, bc, _dx(nc), [f.cpu().numpy(), None, None], 2)
+        assert rel_l2([o.cpu().numpy()], [ref[0]]) < FP64_TOL
+    b.close()
