@@ -47,7 +47,13 @@ WORKLOADS = {
     "rings256": dict(n=256, reg=6, rings=1, seed=7,
                      desc="256^3 unbounded 3-component vector Poisson (padded 512^3), curl, reg 6, "
                           "one perturbed Gaussian-cored vortex ring"),
+    "batch64": dict(kind="batch", problems=64, seed=4, reg=2,
+                    desc="64 independent problems in one batched solve: sizes uniform in [32, 192] per axis, "
+                         "boundary conditions uniform over {000, 111, 110, 001}, 1-3 components, "
+                         "Gaussian-blob sources (random centres, sigma in [0.05, 0.2]), output A, reg 2"),
 }
+
+BATCH_BCS = [(0, 0, 0), (1, 1, 1), (1, 1, 0), (0, 0, 1)]
 
 
 def log(*a):
@@ -103,6 +109,35 @@ def make_source(w, device, dtype=None):
             out[1][z0:z0 + slab] += mag * ty
             out[2][z0:z0 + slab] += mag * tz
     return out
+
+
+def batch_problems(w):
+    """The seeded problem list of a batch workload: (ncell, bc, components, blobs)."""
+    rng = np.random.default_rng(w["seed"])
+    probs = []
+    for _ in range(w["problems"]):
+        nc = tuple(int(v) for v in rng.integers(32, 193, 3))
+        bc = BATCH_BCS[int(rng.integers(0, 4))]
+        ncomp = int(rng.integers(1, 4))
+        blobs = [(rng.uniform(-0.6, 0.6, 3), rng.uniform(0.05, 0.2), rng.standard_normal()) for _ in range(ncomp)]
+        probs.append((nc, bc, ncomp, blobs))
+    return probs
+
+
+def batch_source(nc, blobs, device):
+    """One Gaussian blob per component on [-1, 1]^3, cell-centred."""
+    import torch
+    axes = [-1.0 + (torch.arange(n, device=device, dtype=torch.float64) + 0.5) * (2.0 / n) for n in nc]
+    Z, Y, X = torch.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    out = []
+    for c, s, a in blobs:
+        r2 = (X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2
+        out.append((a * (2 * np.pi * s * s) ** -1.5 * torch.exp(-r2 / (2 * s * s))).contiguous())
+    return out
+
+
+def padded(nc, bc):
+    return tuple(n if b else 2 * n for n, b in zip(nc, bc))
 
 
 # ---------------------------------------------------------------------------
@@ -261,10 +296,56 @@ def _ref_worker(args):
     return times
 
 
+def _ref_batch_worker(args):
+    nc, bc, ncomp, blobs, reg, steps, warmup = args
+    from oracle import oracle
+    B = [b.numpy() for b in batch_source(nc, blobs, "cpu")] + [None] * (3 - ncomp)
+    dx = tuple(2.0 / n for n in nc)
+    times = []
+    for s in range(warmup + steps):
+        _, sec = oracle.solve3d_timed(nc, bc, dx, B, reg)
+        if s >= warmup:
+            times.append(sec[1])
+    return times
+
+
+def run_reference_batch(args, w, world):
+    import multiprocessing as mp
+    from oracle import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    probs = batch_problems(w)
+    # bounded sample: the smallest problems, one per host core
+    sample = sorted(probs, key=lambda p: np.prod(padded(p[0], p[1])))[:cores]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_batch_worker, [(nc, bc, nco, bl, w["reg"], args.steps, 1) for nc, bc, nco, bl in sample])
+    wall = time.perf_counter() - t0
+    slowest = max(sum(t) for t in res)
+    pts = sum(int(np.prod(p[0])) for p in sample)
+    value = pts * args.steps / slowest / 1e6
+    desc = (f"the {len(sample)} smallest of the {len(probs)} problems, one single-thread solve each on "
+            f"{cores} host cores at once, solve3d time only")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": 1, "ms_per_step": slowest / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": w["desc"]},
+        "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args, w):
     world, rank, _, pg = dist_setup()
     if rank != 0:
         return 0
+    if w.get("kind") == "batch":
+        return run_reference_batch(args, w, world)
     import multiprocessing as mp
     from oracle import oracle
     oracle.build()
@@ -427,6 +508,130 @@ def run_ours(args, w):
     return 0
 
 
+def run_batch(args, w):
+    """Batched workload: every problem of the list solved by one ps_batch_solve."""
+    import torch
+
+    import poisson_solver_gb300 as psg
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    K, W = args.steps, args.warmup
+    probs = batch_problems(w)
+    log(f"[rank {rank}] building {len(probs)} sources")
+    src = [batch_source(nc, bl, dev) for nc, bc, nco, bl in probs]
+    points = sum(int(np.prod(p[0])) for p in probs)
+    stream = torch.cuda.current_stream(dev)
+
+    def make(precision):
+        b = psg.PoissonBatch(precision)
+        b.set_stream(stream.cuda_stream)
+        outs = []
+        for (nc, bc, nco, bl), B in zip(probs, src):
+            i = b.add(nc, bc, tuple(2.0 / n for n in nc), w["reg"])
+            b.push_device(i, *[t.data_ptr() for t in B])
+            outs.append([torch.empty_like(t) for t in B])
+        return b, outs
+
+    def timed(b, steps, warm, sample_clocks=False):
+        for _ in range(warm):
+            b.solve()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local) if sample_clocks else None
+        barrier(pg)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            b.solve()
+        e1.record(stream)
+        e1.synchronize()
+        barrier(pg)
+        return e0.elapsed_time(e1), (clocks.stop() if clocks else None)
+
+    t0 = time.perf_counter()
+    b32, o32 = make("fp32")
+    b32.solve()
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ms32, clocks = timed(b32, K, W, sample_clocks=True)
+    ms32_max = max_over_ranks(pg, ms32)
+    value = replica_throughput(points, K, ms32_max / 1e3, world)
+    b64, o64 = make("fp64")
+    K64 = max(2, K // 3)
+    ms64, _ = timed(b64, K64, 1)
+    value64 = replica_throughput(points, K64, max_over_ranks(pg, ms64) / 1e3, world)
+    for i, (a32, a64) in enumerate(zip(o32, o64)):
+        b32.pull_device(i, *[t.data_ptr() for t in a32])
+        b64.pull_device(i, *[t.data_ptr() for t in a64])
+    torch.cuda.synchronize()
+    num = sum(float(torch.sum((x - y) ** 2)) for a, c in zip(o32, o64) for x, y in zip(a, c))
+    den = sum(float(torch.sum(y ** 2)) for c in o64 for y in c)
+    rel = (num / den) ** 0.5
+
+    # end to end: host push of every problem, one batched solve, host pull of every problem
+    hbt = [[t.cpu().pin_memory() for t in B] for B in src]  # pinned host buffers, kept alive
+    hat = [[torch.empty(t.shape, dtype=torch.float64).pin_memory() for t in B] for B in src]
+    hb = [[t.numpy() for t in B] for B in hbt]
+    ha = [[t.numpy() for t in A] for A in hat]
+
+    def e2e_step():
+        for i, B in enumerate(hb):
+            b32.push(i, *B)
+        b32.solve()
+        for i, A in enumerate(ha):
+            b32.pull(i, *A)
+
+    e2e_step()
+    Ke = max(2, min(K, 5))
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        e2e_step()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e = replica_throughput(points, Ke, e2e_s, world)
+    io_bytes = sum(int(np.prod(p[0])) * p[2] * 8 for p in probs)
+
+    byt = sum(sum(algorithmic_bytes(nc, padded(nc, bc), nco, nco, 8, 4)) for nc, bc, nco, bl in probs)
+    peak, peak_kind = measured_peaks()
+    achieved = byt / (ms32 / K * 1e-3) / 1e9
+    if rank != 0:
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        from oracle import oracle
+        nc, bc, nco, bl = min(probs, key=lambda p: np.prod(padded(p[0], p[1])))
+        B = [t.cpu().numpy() for t in batch_source(nc, bl, "cpu")] + [None] * (3 - nco)
+        _, sec = oracle.solve3d_timed(nc, bc, tuple(2.0 / n for n in nc), B, w["reg"])
+        cpu = {"value": int(np.prod(nc)) / sec[1] / 1e6, "unit": "Mpts/s", "cores": 1, "kind": "port",
+               "sample": f"the smallest problem of the batch ({nc[0]}x{nc[1]}x{nc[2]}, bc {bc}, {nco} components), "
+                         f"oracle/ps_oracle.c solve3d on one host thread: {sec[1]:.2f} s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms32_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "problems": len(probs), "points": points,
+                   "precision": "FP32 transforms; FP64 kernel build, FP64 field input/output",
+                   "l2": "the batch's fields and spectra total %.2f GB, larger than L2" % (
+                       (io_bytes * 2 + byt / 10) / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "whole batched solve (5 launches)", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "algorithmic_bytes": byt},
+        "fp64": {"value": value64, "ms_per_step": max_over_ranks(pg, ms64) / K64},
+        "mixed_vs_fp64_speedup": value / value64,
+        "rel_l2_fp32_vs_fp64": rel,
+        "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
+        "gpu_launches": K * int(b32.info(psg._lib.PS_BATCH_INFO_LAUNCHES_PER_SOLVE)),
+        "tiles_per_solve": int(b32.info(psg._lib.PS_BATCH_INFO_TILES_PER_SOLVE)),
+        "clocks": clocks,
+        "setup_s": setup_s,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,6 +647,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)
+    if w.get("kind") == "batch":
+        return run_batch(args, w)
     return run_ours(args, w)
 
 

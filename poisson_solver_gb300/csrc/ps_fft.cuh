@@ -305,36 +305,46 @@ __device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const 
     __syncthreads();
 }
 
-// A stage with a prime radix above 7: out of place into W, then copied back.
+// A stage with a prime radix above 7 (no unrolled butterfly): a direct
+// R-point DFT for every butterfly, out of place into W, then copied back. The
+// L outputs of a line (butterfly bf = o mod nbf, output k = o / nbf) are
+// spread over the line's threads, so the stage runs L R complex products on
+// tpl threads however few butterflies it has (a length-194 line has 2).
+// Twiddles are applied to the inputs in place first; each output then sums
+// R twiddled inputs in the order r = 0 .. R-1.
 template <bool INV, typename C>
 __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws, int4 sd)
 {
     const int L = P.L, R = sd.x, m = sd.y, nbf = L / R, tpl = P.tpl;
     const C *tw = tws + sd.z;
     const C *gw = tws + sd.w;
-    for (int bf = t; bf < nbf; bf += tpl) {
-        const int j = bf % m, q = bf / m;
-        const int base = q * R * m + j;
-        for (int k = 0; k < R; ++k) {
-            C acc = C{0, 0};
-            for (int r = 0; r < R; ++r) {
-                C x = S[(bf + r * nbf) * sn + b * sb];
-                if (m > 1 && r > 0) {
-                    const C w = tw[j * (R - 1) + r - 1];
-                    x = INV ? cmulc(x, w) : cmul(x, w);
-                }
-                const C g = gw[(r * k) % R];
-                acc = cadd(acc, INV ? cmulc(x, g) : cmul(x, g));
+    C *Sb = S + b * sb, *Wb = W + b * sb;
+    if (m > 1) {
+        for (int e = t; e < L; e += tpl) {
+            const int r = e / nbf, bf = e - r * nbf;
+            if (r > 0) {
+                const C w = tw[(bf % m) * (R - 1) + r - 1];
+                Sb[e * sn] = INV ? cmulc(Sb[e * sn], w) : cmul(Sb[e * sn], w);
             }
-            W[(base + k * m) * sn + b * sb] = acc;
         }
+        __syncthreads();
+    }
+    for (int o = t; o < L; o += tpl) {
+        const int k = o / nbf, bf = o - k * nbf;
+        const int j = bf % m, q = bf / m;
+        C acc = C{0, 0};
+        int idx = 0;  // (r k) mod R
+        for (int r = 0; r < R; ++r) {
+            const C x = Sb[(bf + r * nbf) * sn];
+            const C g = gw[idx];
+            acc = cadd(acc, INV ? cmulc(x, g) : cmul(x, g));
+            idx += k;
+            if (idx >= R) idx -= R;
+        }
+        Wb[(q * R * m + j + k * m) * sn] = acc;
     }
     __syncthreads();
-    for (int bf = t; bf < nbf; bf += tpl) {
-        const int j = bf % m, q = bf / m;
-        const int base = q * R * m + j;
-        for (int k = 0; k < R; ++k) S[(base + k * m) * sn + b * sb] = W[(base + k * m) * sn + b * sb];
-    }
+    for (int e = t; e < L; e += tpl) Sb[e * sn] = Wb[e * sn];
     __syncthreads();
 }
 

@@ -147,7 +147,7 @@ void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_t
             d.generic = 1;
             d.gw[s] = (int)(used - base);
             for (int q = 0; q < R; ++q) put(root(q, R));
-            const int g = nbf < 64 ? nbf : 64;
+            const int g = L < 64 ? L : 64;  // the direct DFT spreads a line's L outputs over its threads
             tpl = tpl > g ? tpl : g;
         }
         m *= R;

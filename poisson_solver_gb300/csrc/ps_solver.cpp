@@ -146,7 +146,8 @@ const Plan &Solver::plan(int L, int prec, int emax)
             d.generic = 1;
             d.gw[s] = (int)tab.size();
             for (int q = 0; q < R; ++q) tab.push_back(root(q, R));
-            tpl = std::max(tpl, std::min(nbf, 64));
+            // the direct DFT spreads a line's L outputs over its threads
+            tpl = std::max(tpl, std::min(L, 64));
         }
         m *= R;
     }
