@@ -47,6 +47,10 @@ WORKLOADS = {
     "rings256": dict(n=256, reg=6, rings=1, seed=7,
                      desc="256^3 unbounded 3-component vector Poisson (padded 512^3), curl, reg 6, "
                           "one perturbed Gaussian-cored vortex ring"),
+    "mixed512": dict(kind="mixed", n=(512, 512, 256), reg=2, modes=32, seed=11,
+                     desc="512x512x256 periodic-periodic-unbounded (z padded to 512), 32 seeded random-phase "
+                          "Fourier modes (k 1..16, amplitude N(0,1) k^-2) x Gaussian z envelope (sigma 0.15); "
+                          "one step = the grad solve of the scalar pushed in 3 components + the div solve of (B,B,B)"),
     "batch64": dict(kind="batch", problems=64, seed=4, reg=2,
                     desc="64 independent problems in one batched solve: sizes uniform in [32, 192] per axis, "
                          "boundary conditions uniform over {000, 111, 110, 001}, 1-3 components, "
@@ -134,6 +138,27 @@ def batch_source(nc, blobs, device):
         r2 = (X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2
         out.append((a * (2 * np.pi * s * s) ** -1.5 * torch.exp(-r2 / (2 * s * s))).contiguous())
     return out
+
+
+def mixed_source(w, device):
+    """Sum of seeded Fourier modes in x-y times a Gaussian envelope in z (x-y mean zero)."""
+    import torch
+    nx, ny, nz = w["n"]
+    d = 2.0 / nx
+    rng = np.random.default_rng(w["seed"])
+    modes = []
+    for _ in range(w["modes"]):
+        kx, ky = rng.integers(1, 17, 2)
+        modes.append((int(kx), int(ky), rng.standard_normal() / float(kx * kx + ky * ky), rng.uniform(0, 2 * np.pi)))
+    x = -1.0 + (torch.arange(nx, device=device, dtype=torch.float64) + 0.5) * d
+    y = -1.0 + (torch.arange(ny, device=device, dtype=torch.float64) + 0.5) * d
+    z = -0.5 * nz * d + (torch.arange(nz, device=device, dtype=torch.float64) + 0.5) * d
+    Y, X = torch.meshgrid(y, x, indexing="ij")
+    plane = torch.zeros((ny, nx), device=device, dtype=torch.float64)
+    for kx, ky, a, ph in modes:
+        plane += a * torch.cos(np.pi * (kx * X + ky * Y) + ph)  # wavelength 2 / k on the length-2 domain
+    env = torch.exp(-z * z / (2 * 0.15 ** 2))
+    return (env[:, None, None] * plane[None]).contiguous(), (d, d, d)
 
 
 def padded(nc, bc):
@@ -340,12 +365,58 @@ def run_reference_batch(args, w, world):
     return 0
 
 
+def _ref_mixed_worker(args):
+    nc, reg, steps, warmup, seed = args
+    from oracle import oracle
+    w = dict(WORKLOADS["mixed512"])
+    w["n"], w["seed"] = nc, seed
+    B, dx = mixed_source(w, "cpu")
+    B = B.numpy()
+    times = []
+    for s in range(warmup + steps):
+        _, s1 = oracle.solve3d_timed(nc, (1, 1, 0), dx, [B, B, B], reg, grad=True)
+        _, s2 = oracle.solve3d_timed(nc, (1, 1, 0), dx, [B, B, B], reg, div=True)
+        if s >= warmup:
+            times.append(s1[1] + s2[1])
+    return times
+
+
+def run_reference_mixed(args, w, world):
+    import multiprocessing as mp
+    from oracle import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    nc = (64, 64, 32)
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_mixed_worker, [(nc, w["reg"], args.steps, 1, w["seed"] + i) for i in range(cores)])
+    wall = time.perf_counter() - t0
+    slowest = max(sum(t) for t in res)
+    value = cores * 2 * int(np.prod(nc)) * args.steps / slowest / 1e6
+    desc = (f"{cores} concurrent single-thread grad + div steps of a {nc[0]}x{nc[1]}x{nc[2]} sample of the "
+            f"workload (z padded to {2 * nc[2]}), solve3d time only")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": 1, "ms_per_step": slowest / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": w["desc"], "sample_grid": list(nc)},
+        "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args, w):
     world, rank, _, pg = dist_setup()
     if rank != 0:
         return 0
     if w.get("kind") == "batch":
         return run_reference_batch(args, w, world)
+    if w.get("kind") == "mixed":
+        return run_reference_mixed(args, w, world)
     import multiprocessing as mp
     from oracle import oracle
     oracle.build()
@@ -508,6 +579,115 @@ def run_ours(args, w):
     return 0
 
 
+def run_mixed(args, w):
+    """The mixed-domain grad + div step on one handle, FP32 and FP64 transforms."""
+    import torch
+
+    import poisson_solver_gb300 as psg
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    K, W = args.steps, args.warmup
+    nc, bc = w["n"], (1, 1, 0)
+    Bs, dx = mixed_source(w, dev)
+    points = int(np.prod(nc))
+    stream = torch.cuda.current_stream(dev)
+    ps_g, ps_d = psg.PoissonSolver(), psg.PoissonSolver()
+    for ps in (ps_g, ps_d):
+        ps.setup3d(nc, bc, dx, w["reg"])
+        ps.set_stream(stream.cuda_stream)
+    ps_g.set_return_grad(True)
+    ps_d.set_return_div(True)
+    bp = [Bs.data_ptr()] * 3
+    G = [torch.empty_like(Bs) for _ in range(3)]
+    D = torch.empty_like(Bs)
+
+    def step():
+        ps_g.solve3d_device(bp, [g.data_ptr() for g in G])
+        ps_d.solve3d_device(bp, [D.data_ptr(), 0, 0])
+
+    def timed(precision, steps, warm, sample_clocks=False):
+        for ps in (ps_g, ps_d):
+            ps.set_precision(precision)
+        for _ in range(warm):
+            step()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local) if sample_clocks else None
+        barrier(pg)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+        barrier(pg)
+        return e0.elapsed_time(e1), (clocks.stop() if clocks else None)
+
+    ms64, _ = timed("fp64", max(2, K // 3), 1)
+    G64 = [g.clone() for g in G]
+    D64 = D.clone()
+    ms32, clocks = timed("fp32", K, W, sample_clocks=True)
+    K64 = max(2, K // 3)
+    ms32_max = max_over_ranks(pg, ms32)
+    value = replica_throughput(2 * points, K, ms32_max / 1e3, world)
+    value64 = replica_throughput(2 * points, K64, max_over_ranks(pg, ms64) / 1e3, world)
+    num = sum(float(torch.sum((a - b) ** 2)) for a, b in zip(G + [D], G64 + [D64]))
+    den = sum(float(torch.sum(b ** 2)) for b in G64 + [D64])
+    rel = (num / den) ** 0.5
+
+    # end to end: host push, solve, host pull for both solves
+    ps_g.set_precision("fp32")
+    ps_d.set_precision("fp32")
+    hb = Bs.cpu().pin_memory()
+    hg = [torch.empty(Bs.shape, dtype=torch.float64).pin_memory() for _ in range(3)]
+    hd = torch.empty(Bs.shape, dtype=torch.float64).pin_memory()
+    hbn = hb.numpy()
+
+    def e2e_step():
+        ps_g.push(hbn, hbn, hbn)
+        ps_g.solve3d()
+        ps_g.pull(*[t.numpy() for t in hg])
+        ps_d.push(hbn, hbn, hbn)
+        ps_d.solve3d()
+        ps_d.pull(hd.numpy())
+
+    e2e_step()
+    Ke = max(2, min(K, 5))
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        e2e_step()
+    e2e = replica_throughput(2 * points, Ke, max_over_ranks(pg, time.perf_counter() - t0), world)
+    P = padded(nc, bc)
+    byt = sum(algorithmic_bytes(nc, P, 3, 3, 8, 4)) + sum(algorithmic_bytes(nc, P, 3, 1, 8, 4))
+    peak, peak_kind = measured_peaks()
+    achieved = byt / (ms32 / K * 1e-3) / 1e9
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms32_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "grid": list(nc), "padded": list(P), "bc": list(bc),
+                   "solves_per_step": 2, "precision": "FP32 transforms; FP64 kernel build, FP64 field input/output",
+                   "l2": "inputs larger than L2 (%.2f GB a field)" % (points * 8 / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "whole step (2 solves, 10 launches)", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "algorithmic_bytes": byt},
+        "fp64": {"value": value64, "ms_per_step": max_over_ranks(pg, ms64) / K64},
+        "mixed_vs_fp64_speedup": value / value64,
+        "rel_l2_fp32_vs_fp64": rel,
+        "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": 6 * points * 8,
+                "d2h_bytes_per_step": 4 * points * 8},
+        "gpu_launches": K * 10,
+        "clocks": clocks,
+        "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_batch(args, w):
     """Batched workload: every problem of the list solved by one ps_batch_solve."""
     import torch
@@ -649,6 +829,8 @@ def main():
         return run_reference(args, w)
     if w.get("kind") == "batch":
         return run_batch(args, w)
+    if w.get("kind") == "mixed":
+        return run_mixed(args, w)
     return run_ours(args, w)
 
 

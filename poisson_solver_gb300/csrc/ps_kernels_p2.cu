@@ -31,51 +31,52 @@ template <typename T> __device__ __forceinline__ T wavenumber(int k, int P, T c,
 
 // ---------------------------------------------------------------------------
 // x forward: line l = rows 2l (re) and 2l+1 (im), then the two half spectra.
-template <typename T, int L, int EM>
-__global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+// BL lines a CTA is a template parameter, so the thread count NT = BL TPL is
+// a constant and the load, separation and store loops address global memory
+// as one row base plus immediate offsets.
+template <typename T, int L, int EM, int BL>
+__global__ void __launch_bounds__(BL *(L / EM)) k_xfwd(const XFwdArgs a)
 {
     using C = typename CxT<T>::type;
     using PL = Plan<L, EM>;
-    constexpr int TPL = PL::TPL, LT = ilog2(TPL);
+    constexpr int TPL = PL::TPL, LT = ilog2(TPL), NT = BL * TPL, PER = L / NT;
+    static_assert(PER * NT == L, "a CTA's threads divide the line");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, LDP = line_pitch<C>(L, B);
-    C *TW = S + B * LDP;
-    const int nt = blockDim.x, tid = threadIdx.x;
+    const int LDP = line_pitch<C>(L, BL);
+    C *TW = S + BL * LDP;
+    const int tid = threadIdx.x;
     load_twiddles<C, PL::NTW>(TW, a.plan.table);
     const int comp = blockIdx.y;
     const double *in = pick3(a.in, comp);
     C *out = reinterpret_cast<C *>(pick3(a.out, comp));
     const long long rows = (long long)a.rows_y * a.rows_z;
-    const long long row0 = (long long)blockIdx.x * 2 * B;
-    __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, L / 2 + 1);
+    const long long row0 = (long long)blockIdx.x * 2 * BL;
+    __shared__ long long rofs[2 * BL];
+    row_offsets(rofs, row0, 2 * BL, rows, a.rows_y, a.out_y, L / 2 + 1);
 
     // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last row
     if (!a.mirror) {
-        // B L = EM nt: EM (line, n) pairs a thread, every load issued before
-        // the first shared-memory store
-        constexpr int LL = PL::LL;
-        C v[EM];
+        // every load of the thread issued before the first shared-memory store
+        C v[BL][PER];
 #pragma unroll
-        for (int i = 0; i < EM; ++i) {
-            const int idx = tid + i * nt, line = idx >> LL, n = idx & (L - 1);
-            const long long ra = row0 + 2 * line;
-            T xa = (T)0, xb = (T)0;
-            if (n < a.n_in) {
-                if (ra < rows) xa = (T)in[ra * a.in_stride + n];
-                if (ra + 1 < rows) xb = (T)in[(ra + 1) * a.in_stride + n];
+        for (int l = 0; l < BL; ++l) {
+            const long long ra = row0 + 2 * l;
+            const double *pa = in + ra * a.in_stride + tid, *pb = pa + a.in_stride;
+            const bool va = ra < rows, vb = ra + 1 < rows;
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                const bool live = tid + j * NT < a.n_in;
+                v[l][j] = C{(live && va) ? (T)pa[j * NT] : (T)0, (live && vb) ? (T)pb[j * NT] : (T)0};
             }
-            v[i] = C{xa, xb};
         }
 #pragma unroll
-        for (int i = 0; i < EM; ++i) {
-            const int idx = tid + i * nt, line = idx >> LL, n = idx & (L - 1);
-            S[line * LDP + sk<C>(n)] = v[i];
-        }
+        for (int l = 0; l < BL; ++l)
+#pragma unroll
+            for (int j = 0; j < PER; ++j) S[l * LDP + sk<C>(tid + j * NT)] = v[l][j];
     } else {
         // rows of the kernel octant, mirrored: (z, y) -> (min(z, Pz-z), min(y, Py-y)), n -> min(n, L-n)
-        for (int line = 0; line < B; ++line) {
+        for (int line = 0; line < BL; ++line) {
             const long long ra = row0 + 2 * line;
             const bool va = ra < rows, vb = ra + 1 < rows;
             long long oa = 0, ob = 0;
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
                 ob = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
             }
             C *ln = S + line * LDP;
-            for (int n = tid; n < L; n += nt) {
+            for (int n = tid; n < L; n += NT) {
                 T xa = (T)0, xb = (T)0;
                 if (n < a.n_in) {
                     const int nn = imin(n, L - n);
@@ -102,16 +103,22 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     __syncthreads();
     run<L, EM, false>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
 
-    constexpr int Mx = L / 2 + 1;
-    for (int line = 0; line < B; ++line) {
+    constexpr int Mx = L / 2 + 1, KPER = (Mx + NT - 1) / NT;
+#pragma unroll
+    for (int line = 0; line < BL; ++line) {
         const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
         if (oa < 0) break;
         const C *ln = S + line * LDP;
-        for (int k = tid; k < Mx; k += nt) {
-            const C z = ln[sk<C>(k)], w = ln[sk<C>((L - k) & (L - 1))];
-            const T h = (T)0.5;
-            out[oa + k] = C{h * (z.x + w.x), h * (z.y - w.y)};
-            if (ob >= 0) out[ob + k] = C{h * (z.y + w.y), h * (w.x - z.x)};
+        C *outa = out + oa + tid, *outb = out + ob + tid;
+#pragma unroll
+        for (int j = 0; j < KPER; ++j) {
+            const int k = tid + j * NT;
+            if (k < Mx) {
+                const C z = ln[sk<C>(k)], w = ln[sk<C>((L - k) & (L - 1))];
+                const T h = (T)0.5;
+                outa[j * NT] = C{h * (z.x + w.x), h * (z.y - w.y)};
+                if (ob >= 0) outb[j * NT] = C{h * (z.y + w.y), h * (w.x - z.x)};
+            }
         }
     }
 }
@@ -263,37 +270,54 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
 
 // ---------------------------------------------------------------------------
 // x inverse: half spectra of row pairs -> real rows, cropped.
-template <typename T, int L, int EM>
-__global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+template <typename T, int L, int EM, int BL>
+__global__ void __launch_bounds__(BL *(L / EM)) k_xinv(const XInvArgs a)
 {
     using C = typename CxT<T>::type;
     using PL = Plan<L, EM>;
-    constexpr int TPL = PL::TPL, LT = ilog2(TPL);
-    constexpr int Mx = L / 2 + 1;
+    constexpr int TPL = PL::TPL, LT = ilog2(TPL), NT = BL * TPL;
+    constexpr int Mx = L / 2 + 1, KPER = (Mx + NT - 1) / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, LDP = line_pitch<C>(L, B);
-    C *TW = S + B * LDP;
-    const int nt = blockDim.x, tid = threadIdx.x;
+    const int LDP = line_pitch<C>(L, BL);
+    C *TW = S + BL * LDP;
+    const int tid = threadIdx.x;
     load_twiddles<C, PL::NTW>(TW, a.plan.table);
     const int comp = blockIdx.y;
     const C *in = reinterpret_cast<const C *>(pick3(a.in, comp));
     double *out = pick3(a.out, comp);
     const long long rows = (long long)a.rows_y * a.rows_z;
-    const long long row0 = (long long)blockIdx.x * 2 * B;
-    __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
+    const long long row0 = (long long)blockIdx.x * 2 * BL;
+    __shared__ long long rofs[2 * BL];
+    row_offsets(rofs, row0, 2 * BL, rows, a.rows_y, a.in_y, Mx);
     __syncthreads();
 
-    for (int line = 0; line < B; ++line) {
-        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
-        C *ln = S + line * LDP;
-        for (int k = tid; k < Mx; k += nt) {
-            C xa = C{0, 0}, xb = C{0, 0};
-            if (oa >= 0) xa = in[oa + k];
-            if (ob >= 0) xb = in[ob + k];
-            ln[sk<C>(k)] = C{xa.x - xb.y, xa.y + xb.x};
-            if (k >= 1 && k <= L - Mx) ln[sk<C>(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
+    // Z = Xa + i Xb over the full line from the two half spectra
+    {
+        C va[BL][KPER], vb[BL][KPER];
+#pragma unroll
+        for (int l = 0; l < BL; ++l) {
+            const long long oa = rofs[2 * l], ob = rofs[2 * l + 1];
+            const C *ia = in + oa + tid, *ib = in + ob + tid;
+#pragma unroll
+            for (int j = 0; j < KPER; ++j) {
+                const bool live = tid + j * NT < Mx;
+                va[l][j] = (live && oa >= 0) ? ia[j * NT] : C{0, 0};
+                vb[l][j] = (live && ob >= 0) ? ib[j * NT] : C{0, 0};
+            }
+        }
+#pragma unroll
+        for (int l = 0; l < BL; ++l) {
+            C *ln = S + l * LDP;
+#pragma unroll
+            for (int j = 0; j < KPER; ++j) {
+                const int k = tid + j * NT;
+                if (k < Mx) {
+                    const C xa = va[l][j], xb = vb[l][j];
+                    ln[sk<C>(k)] = C{xa.x - xb.y, xa.y + xb.x};
+                    if (k >= 1 && k <= L - Mx) ln[sk<C>(L - k)] = C{xa.x + xb.y, xb.x - xa.y};
+                }
+            }
         }
     }
     __syncthreads();
@@ -301,16 +325,21 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
 
     // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;
-    for (int line = 0; line < B; ++line) {
+    constexpr int NPER = (L + NT - 1) / NT;
+#pragma unroll
+    for (int line = 0; line < BL; ++line) {
         const long long ra = row0 + 2 * line;
         if (ra >= rows) break;
         const bool vb = ra + 1 < rows;
-        double *oa = out + ra * a.out_stride, *ob = oa + a.out_stride;
+        double *oa = out + ra * a.out_stride + tid, *ob = oa + a.out_stride;
         const C *ln = S + line * LDP;
-        for (int n = tid; n < no; n += nt) {
-            const C v = ln[sk<C>(n)];
-            oa[n] = (double)v.x;
-            if (vb) ob[n] = (double)v.y;
+#pragma unroll
+        for (int j = 0; j < NPER; ++j) {
+            if (tid + j * NT < no) {
+                const C v = ln[sk<C>(tid + j * NT)];
+                oa[j * NT] = (double)v.x;
+                if (vb) ob[j * NT] = (double)v.y;
+            }
         }
     }
 }
@@ -337,25 +366,58 @@ size_t smem_lines(int prec, int L, int B, int nbuf, int ntw_entries)
     return c * ((size_t)nbuf * B * ldp + ntw_entries);
 }
 
+// The x kernels are compiled for 1, 2, 4 or 8 lines a CTA.
+template <int L, int BL> cudaError_t launch_xfwd_t(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    const cudaError_t e = prep(k_xfwd<float, L, 16, BL>, sm);
+    if (e != cudaSuccess) return e;
+    k_xfwd<float, L, 16, BL><<<grid, nt, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L, int BL> cudaError_t launch_xinv_t(const XInvArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    const cudaError_t e = prep(k_xinv<float, L, 16, BL>, sm);
+    if (e != cudaSuccess) return e;
+    k_xinv<float, L, 16, BL><<<grid, nt, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L> cudaError_t launch_xfwd_len(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    switch (a.B) {
+    case 1: return launch_xfwd_t<L, 1>(a, grid, nt, sm, st);
+    case 2: return launch_xfwd_t<L, 2>(a, grid, nt, sm, st);
+    case 4: return launch_xfwd_t<L, 4>(a, grid, nt, sm, st);
+    case 8: return launch_xfwd_t<L, 8>(a, grid, nt, sm, st);
+    default: return cudaErrorInvalidConfiguration;
+    }
+}
+
+template <int L> cudaError_t launch_xinv_len(const XInvArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    switch (a.B) {
+    case 1: return launch_xinv_t<L, 1>(a, grid, nt, sm, st);
+    case 2: return launch_xinv_t<L, 2>(a, grid, nt, sm, st);
+    case 4: return launch_xinv_t<L, 4>(a, grid, nt, sm, st);
+    case 8: return launch_xinv_t<L, 8>(a, grid, nt, sm, st);
+    default: return cudaErrorInvalidConfiguration;
+    }
+}
+
 cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st)
 {
-    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
     const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);
     const int nt = a.B * (a.L / e_max(PREC_FP32));
-    cudaError_t e;
     switch (a.L) {
-#define X(LV)                                                                   \
-    case LV:                                                                    \
-        if ((e = prep(k_xfwd<float, LV, 16>, sm)) != cudaSuccess) return e;     \
-        k_xfwd<float, LV, 16><<<grid, nt, sm, st>>>(a);                         \
-        break;
+#define X(LV) \
+    case LV: return launch_xfwd_len<LV>(a, grid, nt, sm, st);
         PS_P2_LENGTHS(X)
 #undef X
     default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st)
@@ -423,23 +485,17 @@ cudaError_t launch_z(const ZArgs &a, int ny, int em, cudaStream_t st)
 
 cudaError_t launch_xinv(const XInvArgs &a, cudaStream_t st)
 {
-    if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
     const long long rows = (long long)a.rows_y * a.rows_z;
     dim3 grid((unsigned)(((rows + 1) / 2 + a.B - 1) / a.B), a.ncomp);
     const size_t sm = smem_lines(PREC_FP32, a.L, a.B, 1, a.plan.ntw);
     const int nt = a.B * (a.L / e_max(PREC_FP32));
-    cudaError_t e;
     switch (a.L) {
-#define X(LV)                                                                   \
-    case LV:                                                                    \
-        if ((e = prep(k_xinv<float, LV, 16>, sm)) != cudaSuccess) return e;     \
-        k_xinv<float, LV, 16><<<grid, nt, sm, st>>>(a);                         \
-        break;
+#define X(LV) \
+    case LV: return launch_xinv_len<LV>(a, grid, nt, sm, st);
         PS_P2_LENGTHS(X)
 #undef X
     default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 }  // namespace p2

@@ -616,9 +616,9 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
                           "PS_LINES_X", 4);
         PS_CK(wide::launch_xfwd(xa, stream));
     } else if (p2x) {
-        // two lines (four rows) per CTA measured fastest for the x passes
+        // two lines (four rows) per CTA measured fastest for the forward x pass
         xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[0], B, 1, px.dev.ntw); },
-                          "PS_LINES_X", 2);
+                          "PS_LINES_X", 2, 8 * px.dev.tpl);  // compiled for 1, 2, 4 or 8 lines
         PS_CK(p2::launch_xfwd(xa, stream));
     } else {
         xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return smem_x(prec, px.dev, B); }, "PS_LINES_X");
@@ -681,6 +681,12 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
 
         xi.plan = px.dev;
         xi.B = xa.B;
+        if (p2x) {
+            // four lines a CTA measured fastest for the inverse (1.47 against
+            // 1.53 ms with two at 512^3)
+            xi.B = pick_lines(prec, px.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[0], B, 1, px.dev.ntw); },
+                              "PS_LINES_XI", 4, 8 * px.dev.tpl);
+        }
         if (wx) PS_CK(wide::launch_xinv(xi, stream));
         else if (p2x) PS_CK(p2::launch_xinv(xi, stream));
         else PS_CK(launch_xinv(prec, xi, stream));
