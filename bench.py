@@ -38,7 +38,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mpts/s per solve, mixed-prec vs FP64 on GPU at ≤1e-6 rel L2; HBM GB/s"
 PASS_NAMES = ["x_forward", "y_forward", "z_fused", "y_inverse", "x_inverse"]
-KERNEL_NAMES = ["k_xfwd", "k_col<fwd>", "k_zt<curl>", "k_col<inv>", "k_xinv"]
 
 WORKLOADS = {
     "rings512": dict(n=512, reg=10, rings=16, seed=2024,
@@ -473,6 +472,15 @@ def run_ours(args, w):
     bp = [b.data_ptr() for b in B]
     P = ps.padded
     launches = int(ps.info(psg._lib.PS_INFO_LAUNCHES_PER_SOLVE))
+    tune_s = None
+    if not args.no_autotune:
+        # pick each pass's kernel family and lines per CTA by timing (not in the timed region)
+        ps.set_precision("fp32")
+        t0 = time.perf_counter()
+        ps.autotune(7)
+        tune_s = time.perf_counter() - t0
+    ps.set_precision("fp32")
+    pass_config = ps.pass_config(7)
 
     def timed_loop(precision, steps, warm, out, sample_clocks=False):
         ps.set_precision(precision)
@@ -560,7 +568,9 @@ def run_ours(args, w):
                    "precision": "FP32 transforms; FP64 kernel build, FP64 field input/output",
                    "l2": "inputs larger than L2 (3 x %.2f GB in, 3 x %.2f GB out)" % (points * 8 / 1e9, points * 8 / 1e9),
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[top], "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "%s pass: %s family, %d lines a CTA" % (
+                         PASS_NAMES[top], pass_config[top][0], pass_config[top][1]),
+                     "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": byt[top], "ms": pass32[top]},
         "passes_ms": dict(zip(PASS_NAMES, pass32)),
@@ -573,6 +583,8 @@ def run_ours(args, w):
         "gpu_launches": K * launches,
         "clocks": clocks,
         "setup_s": setup_s,
+        "autotune_s": tune_s,
+        "pass_config": dict(zip(PASS_NAMES, [f"{f} x{b}" for f, b in pass_config])),
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -820,6 +832,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rings512")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-autotune", action="store_true", help="run the measured default kernel choices")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to the minimum of 3 steps")

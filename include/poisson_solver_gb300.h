@@ -159,6 +159,23 @@ int ps_get_info(const ps_solver *h, int what, double *value);
 enum { PS_NUM_PASSES = 5 };
 int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset);
 
+/* Autotuning (no reference counterpart: the reference has one FFT code path).
+ * Each pass of a solve -- x forward, y forward, fused z, y inverse, x inverse
+ * -- can run one of several kernel families with a choice of lines per CTA.
+ * ps_autotune times every choice that fits each pass for the handle's grid,
+ * boundary conditions, precision and output option, with the components of
+ * component_mask (bit c = component c) pushed, on zero-filled scratch buffers
+ * (pushed fields are not touched), and keeps the fastest. Tuned choices are
+ * kept for the process and appended to a text cache file ($PS_TUNE_CACHE,
+ * else $XDG_CACHE_HOME or $HOME/.cache, poisson_solver_gb300/tune.txt;
+ * PS_TUNE_CACHE="" disables the file), so later handles and runs of the same
+ * configuration on the same GPU model reuse them. Without tuning a measured
+ * default is used. ps_get_pass_config reports the family and lines a solve
+ * with component_mask would run for pass 0..4. */
+enum { PS_FAMILY_RUNTIME = 0, PS_FAMILY_P2 = 1, PS_FAMILY_WIDE = 2, PS_FAMILY_TMEM = 3 };
+int ps_autotune(ps_solver *h, int component_mask);
+int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, int *lines);
+
 /* Copy the FP64 kernel octant K = G * zeta / (Px Py Pz), layout
  * [Pz/2+1][Py/2+1][Px/2+1] (x fastest), to a HOST array. */
 int ps_get_kernel(const ps_solver *h, double *out, long long capacity);

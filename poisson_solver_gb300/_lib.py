@@ -37,6 +37,12 @@ PS_INFO_LAUNCHES_PER_SOLVE = 3
 PS_INFO_DEVICE_BYTES = 4
 PS_INFO_KERNEL_OCTANT = 5
 
+PS_FAMILY_RUNTIME = 0
+PS_FAMILY_P2 = 1
+PS_FAMILY_WIDE = 2
+PS_FAMILY_TMEM = 3
+FAMILY_NAMES = {0: "runtime", 1: "p2", 2: "wide", 3: "tmem"}
+
 PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0
 PS_BATCH_INFO_TILES_PER_SOLVE = 1
 PS_BATCH_INFO_POINTS = 2
@@ -70,6 +76,8 @@ SIGNATURES = {
     "ps_get_info": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_double)]),
     "ps_get_kernel": (_i, [_vp, _dp, ctypes.c_longlong]),
     "ps_get_pass_times": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _ip, _i]),
+    "ps_autotune": (_i, [_vp, _i]),
+    "ps_get_pass_config": (_i, [_vp, _i, _i, _ip, _ip]),
     "ps_batch_create": (_i, [ctypes.POINTER(_vp), _i]),
     "ps_batch_destroy": (_i, [_vp]),
     "ps_batch_add": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_double), _i, _ip]),

@@ -214,6 +214,22 @@ int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset)
     });
 }
 
+int ps_autotune(ps_solver *h, int component_mask)
+{
+    return guarded(h, [&](ps::Solver &s) { s.autotune(component_mask); });
+}
+
+int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, int *lines)
+{
+    if (!family || !lines) return PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) {
+        const ps::PassChoice c = s.current_choice(pass, component_mask);
+        *family = c.fam == 'p' ? PS_FAMILY_P2 : c.fam == 'w' ? PS_FAMILY_WIDE : c.fam == 't' ? PS_FAMILY_TMEM
+                                                                                             : PS_FAMILY_RUNTIME;
+        *lines = c.B;
+    });
+}
+
 int ps_get_kernel(const ps_solver *h, double *out, long long capacity)
 {
     if (!out) return PS_ERR_ARGUMENT;

@@ -5,12 +5,17 @@
 // that replaces the reference's pencil FFTs and MPI remaps (solve3d.cpp:8-635).
 #include "ps_solver.hpp"
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <functional>
+#include <mutex>
+#include <sstream>
 #include <vector>
 
 #include "poisson_solver_gb300.h"
@@ -554,45 +559,253 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     return write_mask;
 }
 
+// ---------------------------------------------------------------------------
+// Kernel family and lines per CTA of each pass.
+//
+// Families: 'r' run-time kernels (any length, FP64 and FP32), 'p' length-
+// specialised FP32 kernels (powers of two 64..2048), 'w' wide FP32 kernels
+// (256..2048; for z the shared-memory fused kernel), 't' the fused z kernel
+// with tensor-memory staging (z only). Defaults, measured at 512^3 (FP32
+// curl): x forward p2 with 2 lines a CTA (2.3 against 3.4 ms for wide),
+// x inverse p2 with 4, y wide with 8, z tensor-memory with 8. PS_KERNELS,
+// PS_KERNELS_X/_Y/_Z (= wide, p2 or runtime), PS_LINES_X/_XI/_Y/_Z and PS_Z_EM
+// override the defaults; ps_autotune replaces them for one configuration.
+
+static int axis_of(int pass) { return pass == 0 || pass == 4 ? 0 : pass == 2 ? 2 : 1; }
+
+bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
+{
+    const int prec = precision, L = P[axis_of(pass)], op = pa.z.op;
+    switch (fam) {
+    case 'r': return true;
+    case 'p': return p2::supported(prec, L) && (pass != 2 || p2::supports_op(op));
+    case 'w': return wide::supported(prec, L) && (pass != 2 || p2::supports_op(op));
+    case 't': return pass == 2 && wide::zt_supported(prec, L, op, pa.z.nin, pa.z.nout);
+    default: return false;
+    }
+}
+
+int Solver::family_emax(int pass, char fam) const
+{
+    if (fam == 'w' || fam == 't') return 32;
+    if (pass == 2) {
+        if (fam == 'p') {
+            const char *v = getenv("PS_Z_EM");  // 16 measured faster than 8 (13.4 vs 15.4 ms at 512^3)
+            return v && atoi(v) == 8 ? 8 : 16;
+        }
+        return e_max_z(precision);
+    }
+    return e_max(precision);
+}
+
+// Shared memory of a CTA of B lines and the largest B the family allows.
+size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Plan &pl) const
+{
+    const int prec = precision, L = pl.dev.L, ntw = pl.dev.ntw;
+    const int nbuf = std::max(pa.z.nin, pa.z.nout);
+    if (pass == 2) {
+        if (fam == 't') return wide::smem_lines_zt(L, B, ntw);
+        if (fam == 'w') return wide::smem_lines(L, B, nbuf, ntw, true);
+        if (fam == 'p') return p2::smem_lines(prec, L, B, nbuf, ntw);
+        return smem_z(prec, pl.dev, B, nbuf);
+    }
+    const bool x = pass == 0 || pass == 4;
+    if (fam == 'w') return wide::smem_lines(L, B, 1, ntw, !x);
+    if (fam == 'p') return p2::smem_lines(prec, L, B, 1, ntw);
+    return x ? smem_x(prec, pl.dev, B) : smem_col(prec, pl.dev, B);
+}
+
+bool Solver::pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan &pl) const
+{
+    static int limit = 0;
+    if (!limit) limit = max_smem_per_block() - 1024;  // room for static shared data
+    const int tpl = pl.dev.tpl, nt = B * tpl;
+    int max_threads = MAX_THREADS;
+    if (pass == 2 && fam == 't') max_threads = wide::ZT_MAX_THREADS;
+    if (pass == 2 && fam == 'w') max_threads = wide::Z_MAX_THREADS;
+    if ((pass == 0 || pass == 4) && fam == 'p' && B > 8) return false;  // compiled for 1, 2, 4, 8 lines
+    if ((pass == 0 || pass == 4) && B > MAX_LINES) return false;
+    if (pass == 2 && fam == 't' && nt % 32 != 0) return false;           // whole warps
+    return nt <= max_threads && pass_smem(pass, fam, B, pa, pl) <= (size_t)limit;
+}
+
+PassChoice Solver::default_choice(int pass, const PassArgs &pa)
+{
+    static const char *fam_env[3] = {"PS_KERNELS_X", "PS_KERNELS_Y", "PS_KERNELS_Z"};
+    static const char *line_env[5] = {"PS_LINES_X", "PS_LINES_Y", "PS_LINES_Z", "PS_LINES_Y", "PS_LINES_XI"};
+    const int axis = axis_of(pass);
+    const char *f = getenv(fam_env[axis]);
+    if (!f) f = getenv("PS_KERNELS");
+    char fam;
+    if (f && strcmp(f, "runtime") == 0) fam = 'r';
+    else if (f && strcmp(f, "p2") == 0) fam = family_ok(pass, 'p', pa) ? 'p' : 'r';
+    else if (f && strcmp(f, "wide") == 0)
+        fam = family_ok(pass, 'w', pa) ? 'w' : family_ok(pass, 'p', pa) ? 'p' : 'r';
+    else if (pass == 2 && family_ok(pass, 't', pa)) fam = 't';
+    else if (axis > 0 && family_ok(pass, 'w', pa)) fam = 'w';
+    else fam = family_ok(pass, 'p', pa) ? 'p' : 'r';
+
+    int pref = precision == PREC_FP64 ? 8 : 16;
+    if (fam == 'w') pref = pass == 0 || pass == 4 ? 4 : 8;
+    if (fam == 't') pref = 8;  // 64-byte rows: 8.7 against 10.0 ms with 4 for the 512^3 curl pass
+    if (fam == 'p' && pass == 0) pref = 2;
+    if (fam == 'p' && pass == 4) pref = 4;  // 1.47 against 1.53 ms with 2 at 512^3
+    if (const char *v = getenv(line_env[pass])) {
+        const int want = atoi(v);
+        if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) pref = want;
+    }
+    const Plan &pl = plan(P[axis], precision, family_emax(pass, fam));
+    int B = pref;
+    while (B > 1 && !pass_fits(pass, fam, B, pa, pl)) B >>= 1;
+    if (fam == 't')
+        while (B * pl.dev.tpl < 32 && pass_fits(pass, fam, 2 * B, pa, pl)) B *= 2;
+    if (!pass_fits(pass, fam, B, pa, pl)) throw Error(PS_ERR_UNSUPPORTED, "transform length too large for one CTA");
+    return PassChoice{fam, B};
+}
+
+void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
+{
+    const int prec = precision, axis = axis_of(pass);
+    const Plan &pl = plan(P[axis], prec, family_emax(pass, c.fam));
+    switch (pass) {
+    case 0: {
+        XFwdArgs &a = pa.x;
+        a.plan = pl.dev;
+        a.B = c.B;
+        if (c.fam == 'w') PS_CK(wide::launch_xfwd(a, stream));
+        else if (c.fam == 'p') PS_CK(p2::launch_xfwd(a, stream));
+        else PS_CK(launch_xfwd(prec, a, stream));
+        break;
+    }
+    case 1:
+    case 3: {
+        ColArgs &a = pass == 1 ? pa.y : pa.yi;
+        const int inv = pass == 3;
+        a.plan = pl.dev;
+        a.B = c.B;
+        if (c.fam == 'w') PS_CK(wide::launch_col(inv, a, n[2], stream));
+        else if (c.fam == 'p') PS_CK(p2::launch_col(inv, a, n[2], stream));
+        else PS_CK(launch_col(prec, inv, a, n[2], stream));
+        break;
+    }
+    case 2: {
+        ZArgs &a = pa.z;
+        a.plan = pl.dev;
+        a.B = c.B;
+        if (c.fam == 't') PS_CK(wide::launch_zt(a, P[1], stream));
+        else if (c.fam == 'w') PS_CK(wide::launch_z(a, P[1], stream));
+        else if (c.fam == 'p') PS_CK(p2::launch_z(a, P[1], family_emax(2, 'p'), stream));
+        else PS_CK(launch_z(prec, a, P[1], stream));
+        break;
+    }
+    default: {
+        XInvArgs &a = pa.xi;
+        a.plan = pl.dev;
+        a.B = c.B;
+        if (c.fam == 'w') PS_CK(wide::launch_xinv(a, stream));
+        else if (c.fam == 'p') PS_CK(p2::launch_xinv(a, stream));
+        else PS_CK(launch_xinv(prec, a, stream));
+        break;
+    }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tuned choices: in memory for the process, and in a text file (one
+// "key family lines" line a pass) at $PS_TUNE_CACHE, else
+// $XDG_CACHE_HOME/poisson_solver_gb300/tune.txt or
+// $HOME/.cache/poisson_solver_gb300/tune.txt; PS_TUNE_CACHE="" keeps them in
+// memory only.
+namespace {
+
+std::mutex tune_mu;
+std::map<std::string, PassChoice> tune_table;
+bool tune_loaded = false;
+
+std::string tune_path()
+{
+    if (const char *p = getenv("PS_TUNE_CACHE")) return p;
+    std::string base;
+    if (const char *x = getenv("XDG_CACHE_HOME")) base = x;
+    else if (const char *h = getenv("HOME")) base = std::string(h) + "/.cache";
+    else return "";
+    return base + "/poisson_solver_gb300/tune.txt";
+}
+
+void tune_load_locked()
+{
+    if (tune_loaded) return;
+    tune_loaded = true;
+    const std::string path = tune_path();
+    if (path.empty()) return;
+    std::ifstream f(path);
+    std::string key, fam;
+    int B;
+    while (f >> key >> fam >> B)
+        if (fam.size() == 1 && B >= 1 && B <= 64) tune_table[key] = PassChoice{fam[0], B};
+}
+
+void tune_store_locked(const std::string &key, const PassChoice &c)
+{
+    tune_table[key] = c;
+    const std::string path = tune_path();
+    if (path.empty()) return;
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        // create the directory chain (best effort)
+        for (size_t i = 1; i <= slash; ++i)
+            if (path[i] == '/' || i == slash) mkdir(path.substr(0, i == slash ? slash : i).c_str(), 0755);
+    }
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << ' ' << c.fam << ' ' << c.B << '\n';
+}
+
+}  // namespace
+
+std::string Solver::tune_key(int pass, const PassArgs &pa)
+{
+    if (device_tag.empty()) {
+        cudaDeviceProp prop{};
+        PS_CK(cudaGetDeviceProperties(&prop, device));
+        std::ostringstream d;
+        for (const char *c = prop.name; *c; ++c) d << (*c == ' ' ? '_' : *c);
+        d << ":sm" << prop.multiProcessorCount;
+        device_tag = d.str();
+    }
+    std::ostringstream k;
+    k << device_tag << ":" << (precision == PREC_FP64 ? "fp64" : "fp32") << ":N" << n[0] << 'x'
+      << n[1] << 'x' << n[2] << ":P" << P[0] << 'x' << P[1] << 'x' << P[2] << ":op" << pa.z.op << ":in" << pa.x.ncomp
+      << ":out" << pa.xi.ncomp << ":z" << pa.z.nin << pa.z.nout << ":pass" << pass;
+    return k.str();
+}
+
+// Any PS_KERNELS* or PS_LINES* setting bypasses the tuned choices.
+static bool env_override()
+{
+    for (const char *v : {"PS_KERNELS", "PS_KERNELS_X", "PS_KERNELS_Y", "PS_KERNELS_Z", "PS_LINES_X", "PS_LINES_XI",
+                          "PS_LINES_Y", "PS_LINES_Z"})
+        if (getenv(v)) return true;
+    return false;
+}
+
+PassChoice Solver::choice(int pass, const PassArgs &pa)
+{
+    if (!env_override()) {
+        std::lock_guard<std::mutex> lock(tune_mu);
+        tune_load_locked();
+        auto it = tune_table.find(tune_key(pass, pa));
+        if (it != tune_table.end() && family_ok(pass, it->second.fam, pa)) {
+            const Plan &pl = plan(P[axis_of(pass)], precision, family_emax(pass, it->second.fam));
+            if (pass_fits(pass, it->second.fam, it->second.B, pa, pl)) return it->second;
+        }
+    }
+    return default_choice(pass, pa);
+}
+
 int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter_only)
 {
     PassArgs pa;
     const int write_mask = prepare(Bin, Aout, filter_only, pa);
-    const int prec = precision, op = pa.z.op;
-    XFwdArgs &xa = pa.x;
-    ColArgs &ya = pa.y, &yi = pa.yi;
-    ZArgs &za = pa.z;
-    XInvArgs &xi = pa.xi;
-
-    // Kernel family per axis. FP32: the wide kernels for the y and z passes
-    // (lengths 256..2048), the length-specialised ones for x (measured faster
-    // there: 2.3 vs 3.4 ms for the 512^3 forward x pass) and for other
-    // power-of-two lengths 64..2048; the run-time kernels for the rest and
-    // for FP64. PS_KERNELS (all axes) or PS_KERNELS_X/_Y/_Z = wide, p2 or
-    // runtime override the choice (PS_KERNELS_Z=wide: the shared-memory fused
-    // z kernel instead of the tensor-memory one).
-    auto family = [&](int axis, int L, bool op_ok) -> char {
-        static const char *names[3] = {"PS_KERNELS_X", "PS_KERNELS_Y", "PS_KERNELS_Z"};
-        const char *f = getenv(names[axis]);
-        if (!f) f = getenv("PS_KERNELS");
-        const bool force = f != nullptr;
-        const bool w_ok = wide::supported(prec, L) && op_ok, p_ok = p2::supported(prec, L) && op_ok;
-        if (force && strcmp(f, "runtime") == 0) return 'r';
-        if (force && strcmp(f, "p2") == 0) return p_ok ? 'p' : 'r';
-        if (force && strcmp(f, "wide") == 0) return w_ok ? 'w' : p_ok ? 'p' : 'r';
-        if (w_ok && axis > 0) return 'w';
-        return p_ok ? 'p' : 'r';
-    };
-    const char fx = family(0, P[0], true), fy = family(1, P[1], true), fz = family(2, P[2], p2::supports_op(op));
-    const bool wx = fx == 'w', wy = fy == 'w', wz = fz == 'w';
-    const bool p2x = fx == 'p', p2y = fy == 'p', p2z = fz == 'p';
-    int emz = e_max_z(prec);
-    if (p2z) {
-        emz = 16;  // measured faster than 8 at 512^3 (13.4 vs 15.4 ms for the curl pass)
-        if (const char *v = getenv("PS_Z_EM")) emz = atoi(v) == 8 ? 8 : 16;
-    }
-    if (wz) emz = 32;
-    const Plan &px = plan(P[0], prec, wx ? 32 : 0), &py = plan(P[1], prec, wy ? 32 : 0), &pz = plan(P[2], prec, emz);
 
     std::array<cudaEvent_t, NPASS + 1> ev{};
     if (opt_timing) {
@@ -608,93 +821,103 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         if (opt_timing) PS_CK(cudaEventRecord(ev[i], stream));
     };
     mark(0);
-
-    // x forward over the pushed components
-    xa.plan = px.dev;
-    if (wx) {
-        xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return wide::smem_lines(P[0], B, 1, px.dev.ntw, false); },
-                          "PS_LINES_X", 4);
-        PS_CK(wide::launch_xfwd(xa, stream));
-    } else if (p2x) {
-        // two lines (four rows) per CTA measured fastest for the forward x pass
-        xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[0], B, 1, px.dev.ntw); },
-                          "PS_LINES_X", 2, 8 * px.dev.tpl);  // compiled for 1, 2, 4 or 8 lines
-        PS_CK(p2::launch_xfwd(xa, stream));
-    } else {
-        xa.B = pick_lines(prec, px.dev.tpl, [&](int B) { return smem_x(prec, px.dev, B); }, "PS_LINES_X");
-        PS_CK(launch_xfwd(prec, xa, stream));
+    // x forward, y forward, z (forward, spectral operation, inverse), then
+    // y inverse and x inverse of the written outputs
+    for (int pass = 0; pass < NPASS; ++pass) {
+        if (pass < 3 || write_mask) launch_pass(pass, choice(pass, pa), pa);
+        mark(pass + 1);
     }
-    mark(1);
-
-    // y forward
-    ya.plan = py.dev;
-    if (wy) {
-        ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return wide::smem_lines(P[1], B, 1, py.dev.ntw, true); },
-                          "PS_LINES_Y", 8);
-        PS_CK(wide::launch_col(0, ya, n[2], stream));
-    } else if (p2y) {
-        ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[1], B, 1, py.dev.ntw); },
-                          "PS_LINES_Y");
-        PS_CK(p2::launch_col(0, ya, n[2], stream));
-    } else {
-        ya.B = pick_lines(prec, py.dev.tpl, [&](int B) { return smem_col(prec, py.dev, B); }, "PS_LINES_Y");
-        PS_CK(launch_col(prec, 0, ya, n[2], stream));
-    }
-    mark(2);
-
-    // z forward, spectral operation, z inverse
-    za.plan = pz.dev;
-    const int nbuf = std::max(za.nin, za.nout);
-    // The wide z family runs as the tensor-memory kernel unless
-    // PS_KERNELS_Z=wide asks for the shared-memory one.
-    const char *zfam = getenv("PS_KERNELS_Z");
-    const bool zt = wz && !(zfam && strcmp(zfam, "wide") == 0) && wide::zt_supported(prec, P[2], op, za.nin, za.nout);
-    if (zt) {
-        // 8 columns a CTA (64-byte rows in global memory): measured 8.7 ms
-        // against 10.0 ms with 4 for the 512^3 curl pass (Pz = 1024)
-        za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return wide::smem_lines_zt(P[2], B, pz.dev.ntw); },
-                          "PS_LINES_Z", 8, wide::ZT_MAX_THREADS);
-        while (za.B * pz.dev.tpl < 32) za.B *= 2;  // whole warps (tcgen05 is warp-collective)
-        PS_CK(wide::launch_zt(za, P[1], stream));
-    } else if (wz) {
-        za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return wide::smem_lines(P[2], B, nbuf, pz.dev.ntw, true); },
-                          "PS_LINES_Z", 8, wide::Z_MAX_THREADS);
-        PS_CK(wide::launch_z(za, P[1], stream));
-    } else if (p2z) {
-        za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[2], B, nbuf, pz.dev.ntw); },
-                          "PS_LINES_Z");
-        PS_CK(p2::launch_z(za, P[1], emz, stream));
-    } else {
-        za.B = pick_lines(prec, pz.dev.tpl, [&](int B) { return smem_z(prec, pz.dev, B, nbuf); }, "PS_LINES_Z");
-        PS_CK(launch_z(prec, za, P[1], stream));
-    }
-    mark(3);
-
-    // y inverse (cropped to Ny) and x inverse (cropped to Nx) of the written outputs
-    if (write_mask) {
-        yi.plan = py.dev;
-        yi.B = ya.B;
-        if (wy) PS_CK(wide::launch_col(1, yi, n[2], stream));
-        else if (p2y) PS_CK(p2::launch_col(1, yi, n[2], stream));
-        else PS_CK(launch_col(prec, 1, yi, n[2], stream));
-        mark(4);
-
-        xi.plan = px.dev;
-        xi.B = xa.B;
-        if (p2x) {
-            // four lines a CTA measured fastest for the inverse (1.47 against
-            // 1.53 ms with two at 512^3)
-            xi.B = pick_lines(prec, px.dev.tpl, [&](int B) { return p2::smem_lines(prec, P[0], B, 1, px.dev.ntw); },
-                              "PS_LINES_XI", 4, 8 * px.dev.tpl);
-        }
-        if (wx) PS_CK(wide::launch_xinv(xi, stream));
-        else if (p2x) PS_CK(p2::launch_xinv(xi, stream));
-        else PS_CK(launch_xinv(prec, xi, stream));
-    } else {
-        mark(4);
-    }
-    mark(5);
     return write_mask;
+}
+
+void Solver::autotune(int in_mask)
+{
+    check_setup();
+    if (in_mask <= 0 || in_mask > 7) throw Error(PS_ERR_ARGUMENT, "component mask must be 1..7");
+    const int out_mask = output_mask(in_mask);
+    // zero-filled scratch fields: the tuning runs leave every buffer at zero
+    DevBuf tb[3], ta[3];
+    const size_t bytes = field_elems() * sizeof(double);
+    const double *Bin[3];
+    double *Aout[3];
+    for (int c = 0; c < 3; ++c) {
+        Bin[c] = nullptr;
+        Aout[c] = nullptr;
+        if (in_mask >> c & 1) {
+            tb[c].ensure(bytes);
+            PS_CK(cudaMemsetAsync(tb[c].p, 0, bytes, stream));
+            Bin[c] = (const double *)tb[c].p;
+        }
+        if (out_mask >> c & 1) {
+            ta[c].ensure(bytes);
+            Aout[c] = (double *)ta[c].p;
+        }
+    }
+    PassArgs pa;
+    const int write_mask = prepare(Bin, Aout, false, pa);
+    for (int c = 0; c < 3; ++c)
+        if (work[c].p) PS_CK(cudaMemsetAsync(work[c].p, 0, work[c].bytes, stream));
+    cudaEvent_t e0, e1;
+    PS_CK(cudaEventCreate(&e0));
+    PS_CK(cudaEventCreate(&e1));
+    try {
+        for (int pass = 0; pass < NPASS; ++pass) {
+            if (pass >= 3 && !write_mask) continue;
+            PassChoice best{0, 0};
+            float best_ms = 0.f;
+            for (char fam : {'t', 'w', 'p', 'r'}) {
+                if (!family_ok(pass, fam, pa)) continue;
+                const Plan &pl = plan(P[axis_of(pass)], precision, family_emax(pass, fam));
+                for (int B = 1; B <= 64; B *= 2) {
+                    if (!pass_fits(pass, fam, B, pa, pl)) continue;
+                    const PassChoice c{fam, B};
+                    PassArgs run = pa;
+                    launch_pass(pass, c, run);  // warm-up (and the one-time attribute setup)
+                    PS_CK(cudaEventRecord(e0, stream));
+                    const int reps = 3;
+                    for (int r = 0; r < reps; ++r) launch_pass(pass, c, run);
+                    PS_CK(cudaEventRecord(e1, stream));
+                    PS_CK(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    PS_CK(cudaEventElapsedTime(&ms, e0, e1));
+                    ms /= reps;
+                    if (!best.fam || ms < best_ms) {
+                        best = c;
+                        best_ms = ms;
+                    }
+                }
+            }
+            if (best.fam) {
+                std::lock_guard<std::mutex> lock(tune_mu);
+                tune_load_locked();
+                tune_store_locked(tune_key(pass, pa), best);
+            }
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    PS_CK(cudaStreamSynchronize(stream));
+}
+
+PassChoice Solver::current_choice(int pass, int in_mask)
+{
+    check_setup();
+    if (pass < 0 || pass >= NPASS) throw Error(PS_ERR_ARGUMENT, "pass must be 0..4");
+    const int out_mask = output_mask(in_mask);
+    // arguments only: no buffer is touched (pointers are placeholders)
+    const double *Bin[3];
+    double *Aout[3];
+    for (int c = 0; c < 3; ++c) {
+        Bin[c] = (in_mask >> c & 1) ? reinterpret_cast<const double *>(16) : nullptr;
+        Aout[c] = (out_mask >> c & 1) ? reinterpret_cast<double *>(16) : nullptr;
+    }
+    PassArgs pa;
+    prepare(Bin, Aout, false, pa);
+    return choice(pass, pa);
 }
 
 // ---------------------------------------------------------------------------

@@ -38,6 +38,13 @@ struct Plan {
     DevBuf table;
 };
 
+// Kernel family and lines per CTA of one pass: 'r' run-time, 'p' length-
+// specialised, 'w' wide, 't' tensor-memory fused z.
+struct PassChoice {
+    char fam;
+    int B;
+};
+
 // Arguments of the five passes of one solve, all but the plans and the lines
 // per CTA (which depend on the kernel family that runs each pass).
 struct PassArgs {
@@ -103,6 +110,13 @@ struct Solver {
     void solve_internal();
     void pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind);
 
+    // Time every kernel family and line count that fits each pass of this
+    // configuration (options + in_mask) on zero-filled scratch buffers and
+    // keep the fastest (tuned choices outlive the handle; see ps_solver.cpp).
+    void autotune(int in_mask);
+    // The family and lines a solve of in_mask would run on a pass.
+    PassChoice current_choice(int pass, int in_mask);
+
     size_t device_bytes() const;
     void copy_kernel(double *host, long long capacity) const;
 
@@ -111,6 +125,15 @@ struct Solver {
     void ensure_zeta(int prec);
 
 private:
+    bool family_ok(int pass, char fam, const PassArgs &pa) const;
+    int family_emax(int pass, char fam) const;
+    size_t pass_smem(int pass, char fam, int B, const PassArgs &pa, const Plan &pl) const;
+    bool pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan &pl) const;
+    PassChoice default_choice(int pass, const PassArgs &pa);
+    PassChoice choice(int pass, const PassArgs &pa);
+    std::string tune_key(int pass, const PassArgs &pa);
+    std::string device_tag;  // device name and SM count, for the tuning key
+    void launch_pass(int pass, const PassChoice &c, PassArgs &pa);
     void build_kernel();
     void check_setup() const;
     size_t field_elems() const { return (size_t)n[0] * n[1] * n[2]; }

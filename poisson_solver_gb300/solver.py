@@ -157,6 +157,19 @@ class PoissonSolver:
         self._call("ps_get_pass_times", ms, ctypes.byref(n), int(reset))
         return list(ms), n.value
 
+    def autotune(self, component_mask: int = 7):
+        """Time each pass's kernel families and lines per CTA; keep the fastest."""
+        self._call("ps_autotune", int(component_mask))
+
+    def pass_config(self, component_mask: int = 7):
+        """[(family name, lines per CTA)] of the five passes a solve would run."""
+        out = []
+        for p in range(5):
+            f, b = ctypes.c_int(), ctypes.c_int()
+            self._call("ps_get_pass_config", p, int(component_mask), ctypes.byref(f), ctypes.byref(b))
+            out.append((L.FAMILY_NAMES[f.value], b.value))
+        return out
+
     def synchronize(self):
         self._call("ps_synchronize")
 
