@@ -364,8 +364,8 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
 __device__ __forceinline__ bool is_generic_radix(int R) { return R > 8 && R != 16; }
 
 template <bool INV, int EM, typename C>
-__device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws,
-                                          const StageInfo &si, int ncomp = 1, int cstride = 0)
+__device__ __forceinline__ void fft_stages(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+                                           const C *tws, const StageInfo &si, int ncomp, int cstride)
 {
     const int ns = P.nstages;
     int s = 0;
@@ -390,6 +390,59 @@ __device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int
         for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
         ++s;
     }
+}
+
+// Line-thread index of a thread that must only join the barriers: past every
+// butterfly and every element of any plan.
+constexpr int IDLE_T = 1 << 28;
+
+// Bluestein's algorithm for a length lb with a large prime factor, on lines
+// of M = P.L >= 2 lb - 1 elements: with c[n] = e^{-i pi n^2 / lb},
+// X[k] = c[k] sum_n (x[n] c[n]) conj(c[k - n]), a circular convolution of
+// length M done by the power-of-two stages (forward, times the precomputed
+// spectrum K of the wrapped conj(c) scaled by 1/M, unnormalised inverse). The
+// inverse DFT conjugates the chirp and reads K at -k, which is the spectrum of
+// the wrapped c. The chirp and K are read from the plan's global table (each
+// entry once a line), the stage twiddles from shared memory.
+template <bool INV, int EM, typename C>
+__device__ __forceinline__ void bluestein_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+                                                const C *tws, const StageInfo &si, int ncomp, int cstride)
+{
+    const int M = P.L, Lb = P.lb, tpl = P.tpl;
+    const C *g = reinterpret_cast<const C *>(P.table);  // global table: chirp and K are not staged
+    const C *ch = g + P.chirp, *K = g + P.kspec;
+    for (int c = 0; c < ncomp; ++c) {
+        C *Sb = S + c * cstride + b * sb;
+        for (int n = t; n < M; n += tpl) {
+            C v = C{0, 0};
+            if (n < Lb) v = INV ? cmulc(Sb[n * sn], ch[n]) : cmul(Sb[n * sn], ch[n]);
+            Sb[n * sn] = v;
+        }
+    }
+    __syncthreads();
+    fft_stages<false, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    for (int c = 0; c < ncomp; ++c) {
+        C *Sb = S + c * cstride + b * sb;
+        for (int k = t; k < M; k += tpl) {
+            const C kk = INV ? C{K[(M - k) & (M - 1)].x, -K[(M - k) & (M - 1)].y} : K[k];
+            Sb[k * sn] = cmul(Sb[k * sn], kk);
+        }
+    }
+    __syncthreads();
+    fft_stages<true, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    for (int c = 0; c < ncomp; ++c) {
+        C *Sb = S + c * cstride + b * sb;
+        for (int k = t; k < Lb; k += tpl) Sb[k * sn] = INV ? cmulc(Sb[k * sn], ch[k]) : cmul(Sb[k * sn], ch[k]);
+    }
+    __syncthreads();
+}
+
+template <bool INV, int EM, typename C>
+__device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws,
+                                          const StageInfo &si, int ncomp = 1, int cstride = 0)
+{
+    if (P.blue) bluestein_lines<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    else fft_stages<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
 }
 
 // Component c of a three-entry parameter array, read with constant indices.

@@ -39,7 +39,7 @@ __device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, i
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, ld = L + 1;
+    const int B = a.B, L = a.L, ld = a.plan.L + 1;  // lines as long as the plan's working length
     C *W = a.plan.generic ? S + B * ld : nullptr;
     const FftPlanDev &plan = a.plan;
     const C *tws = stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
@@ -83,7 +83,7 @@ __device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, i
         }
     }
     __syncthreads();
-    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : L, plan, tws, si);
+    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
 
     // separate the two half spectra and store
     const int Mx = a.Mx;
@@ -113,11 +113,11 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L;
-    C *W = a.plan.generic ? S + L * B : nullptr;
+    const int B = a.B, L = a.L, Lw = a.plan.L;  // Lw: the plan's working length
+    C *W = a.plan.generic ? S + Lw * B : nullptr;
     const int lb = __ffs(B) - 1;
     const FftPlanDev &plan = a.plan;
-    const C *tws = stage_twiddles(plan, S + L * B * (a.plan.generic ? 2 : 1));
+    const C *tws = stage_twiddles(plan, S + Lw * B * (a.plan.generic ? 2 : 1));
     __shared__ StageInfo si;
     load_stages(si, a.plan);
     const int x0 = bx * B;
@@ -126,7 +126,7 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int
     const int tid = threadIdx.x;
 
     // each thread keeps one column b and walks rows n = t, t + nt/B, ...
-    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : L, rstep = nt >> lb;
+    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : IDLE_T, rstep = nt >> lb;
     const long long gstep = (long long)rstep * a.axis_stride;
     {
         const C *src = base + (long long)t * a.axis_stride + b;
@@ -174,7 +174,7 @@ __device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, LB = L * B;
+    const int B = a.B, L = a.L, LB = a.plan.L * B;  // buffers as long as the plan's working length
     const int nbuf = a.nin > a.nout ? a.nin : a.nout;
     C *W = a.plan.generic ? S + nbuf * LB : nullptr;
     const int lb = __ffs(B) - 1;
@@ -183,7 +183,7 @@ __device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
     const int nb = imin(B, a.Mx - x0);
     const long long off = (long long)ky * a.row_stride + x0;
     const int tid = threadIdx.x;
-    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : L;
+    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : IDLE_T;
     const FftPlanDev &plan = a.plan;
     const C *tws = stage_twiddles(plan, S + (nbuf + (a.plan.generic ? 1 : 0)) * LB);
     __shared__ StageInfo si;
@@ -300,7 +300,7 @@ __device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, i
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, ld = L + 1, Mx = a.Mx;
+    const int B = a.B, L = a.L, ld = a.plan.L + 1, Mx = a.Mx;
     C *W = a.plan.generic ? S + B * ld : nullptr;
     const FftPlanDev &plan = a.plan;
     const C *tws = stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
@@ -327,7 +327,7 @@ __device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, i
         }
     }
     __syncthreads();
-    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : L, plan, tws, si);
+    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
 
     // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;

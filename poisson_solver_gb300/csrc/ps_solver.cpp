@@ -120,6 +120,44 @@ static std::complex<long double> root(long long e, long long N)
     return {cosl(a), -sinl(a)};
 }
 
+static int largest_prime_factor(int x)
+{
+    int f = 1;
+    for (int p = 2; (long long)p * p <= x; ++p)
+        while (x % p == 0) {
+            f = p;
+            x /= p;
+        }
+    return x > 1 ? std::max(f, x) : f;
+}
+
+// In-place DFT (e^{-2 pi i nk / M}) of a power-of-two length in extended
+// precision: the Bluestein kernel spectrum.
+static void host_fft_pow2(std::vector<std::complex<long double>> &a)
+{
+    const size_t M = a.size();
+    for (size_t i = 1, j = 0; i < M; ++i) {
+        size_t bit = M >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(a[i], a[j]);
+    }
+    for (size_t len = 2; len <= M; len <<= 1) {
+        for (size_t i = 0; i < M; i += len)
+            for (size_t k = 0; k < len / 2; ++k) {
+                const std::complex<long double> w = root((long long)k, (long long)len);
+                const std::complex<long double> u = a[i + k], v = a[i + k + len / 2] * w;
+                a[i + k] = u + v;
+                a[i + k + len / 2] = u - v;
+            }
+    }
+}
+
+// Lengths with a prime factor of at least this take Bluestein's algorithm
+// (two power-of-two FFTs of M >= 2L - 1 points) instead of a direct prime-
+// radix stage (about R complex products an element).
+constexpr int BLUESTEIN_MIN_PRIME = 17;
+
 const Plan &Solver::plan(int L, int prec, int emax)
 {
     if (emax <= 0) emax = e_max(prec);
@@ -128,7 +166,15 @@ const Plan &Solver::plan(int L, int prec, int emax)
     if (it != plans.end()) return *it->second;
     auto pl = std::make_unique<Plan>();
     FftPlanDev &d = pl->dev;
+    const int Lt = L;  // the transform length
+    const bool blue = L > 16 && largest_prime_factor(L) >= BLUESTEIN_MIN_PRIME && !getenv("PS_NO_BLUESTEIN");
+    if (blue) {
+        L = 1;
+        while (L < 2 * Lt - 1) L <<= 1;
+    }
     d.L = L;
+    d.blue = blue ? 1 : 0;
+    d.lb = Lt;
     std::vector<int> rad = L > 1 ? factorize(L, emax) : std::vector<int>{};
     if ((int)rad.size() > MAX_STAGES) throw Error(PS_ERR_UNSUPPORTED, "transform length has too many factors");
     d.nstages = (int)rad.size();
@@ -157,8 +203,23 @@ const Plan &Solver::plan(int L, int prec, int emax)
         m *= R;
     }
     d.tpl = tpl;
-    d.ntw = (int)tab.size();
-    if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length " + std::to_string(L) + " too large");
+    d.ntw = (int)tab.size();  // the part copied to shared memory
+    if (blue) {
+        // chirp c[n] = e^{-i pi n^2 / Lt} and the spectrum of its conjugate
+        // wrapped onto M = L points, scaled by 1/M (read through the cache)
+        d.chirp = (int)tab.size();
+        for (long long k = 0; k < Lt; ++k) tab.push_back(root((k * k) % (2LL * Lt), 2LL * Lt));
+        std::vector<std::complex<long double>> b(L, {0.0L, 0.0L});
+        for (int k = 0; k < Lt; ++k) {
+            const std::complex<long double> cc = std::conj(tab[d.chirp + k]);
+            b[k] = cc;
+            if (k > 0) b[L - k] = cc;
+        }
+        host_fft_pow2(b);
+        d.kspec = (int)tab.size();
+        for (int k = 0; k < L; ++k) tab.push_back(b[k] / (long double)L);
+    }
+    if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length " + std::to_string(Lt) + " too large");
     if (!tab.empty()) {
         if (prec == PREC_FP64) {
             std::vector<double2> h(tab.size());

@@ -31,6 +31,13 @@ struct FftPlanDev {
     int lm[MAX_STAGES];  // log2(m) when m is a power of two, else -1
     int ntw;             // complex entries in the table
     const void *table;   // complex twiddles in the pass precision (copied to shared memory per CTA)
+    // Bluestein plans (a prime factor of the transform length of 17 or more):
+    // the stages above transform length L = M, a power of two >= 2 lb - 1,
+    // and the length-lb DFT is chirp x FFT_M^-1(K FFT_M(chirp x)).
+    int blue;   // 1 for a Bluestein plan
+    int lb;     // the transform length (L for other plans)
+    int chirp;  // table offset of c[n] = e^{-i pi n^2 / lb}, n < lb
+    int kspec;  // table offset of K[k] = FFT_M(conj c, wrapped)[k] / M, k < M
 };
 
 // Spectral operation of the fused z pass.
