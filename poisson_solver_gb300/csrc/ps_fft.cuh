@@ -88,14 +88,38 @@ template <bool INV, typename C> __device__ __forceinline__ void dft8(C *x)
     for (int i = 0; i < 8; ++i) x[i] = y[i];
 }
 
+// The twiddles and second layer of the 16-point DFT (after the first layer of
+// four 4-point DFTs over n2, n = 4 n2 + n1).
+template <bool INV, typename C> __device__ __forceinline__ void dft16_layer2(C *x);
+
 template <bool INV, typename C> __device__ __forceinline__ void dft16(C *x)
+{
+    // n = 4 n2 + n1: four 4-point DFTs over n2 for each n1
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) dft4<INV>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
+    dft16_layer2<INV>(x);
+}
+
+// The 16-point DFT of an input whose upper half x[8..15] is zero: the first
+// layer's 4-point DFTs see (x[n1], x[n1 + 4], 0, 0).
+template <bool INV, typename C> __device__ __forceinline__ void dft16_half(C *x)
+{
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) {
+        const C a = x[n1], b = x[n1 + 4], rb = rot<INV>(b);
+        x[n1] = cadd(a, b);
+        x[n1 + 8] = csub(a, b);
+        x[n1 + 4] = cadd(a, rb);
+        x[n1 + 12] = csub(a, rb);
+    }
+    dft16_layer2<INV>(x);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft16_layer2(C *x)
 {
     using S = decltype(x[0].x);
     const S c1 = (S)0.92387953251128675613, s1 = (S)0.38268343236508977173;
     const S h = (S)0.70710678118654752440;
-    // n = 4 n2 + n1: four 4-point DFTs over n2 for each n1
-#pragma unroll
-    for (int n1 = 0; n1 < 4; ++n1) dft4<INV>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
     // x[n1 + 4 k1] now holds A[n1][k1]; multiply by w16^{n1 k1}
     x[5] = crot<INV>(x[5], c1, s1);                // w^1
     x[9] = crot<INV>(x[9], h, h);                  // w^2
@@ -191,6 +215,35 @@ template <bool INV, typename C> __device__ __forceinline__ void dft32(C *x)
     }
     dft16<INV>(e);
     dft16<INV>(o);
+    const S c[8] = {(S)1.0, (S)0.98078528040323044913, (S)0.92387953251128675613, (S)0.83146961230254523708,
+                    (S)0.70710678118654752440, (S)0.55557023301960222474, (S)0.38268343236508977173,
+                    (S)0.19509032201612826785};
+#pragma unroll
+    for (int k = 1; k < 16; ++k) {
+        if (k < 8) o[k] = crot<INV>(o[k], c[k], c[8 - k]);
+        else if (k == 8) o[k] = rot<INV>(o[k]);
+        else o[k] = rot<INV>(crot<INV>(o[k], c[k - 8], c[16 - k]));
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        x[k] = cadd(e[k], o[k]);
+        x[k + 16] = csub(e[k], o[k]);
+    }
+}
+
+// The 32-point DFT of an input whose upper half x[16..31] is zero (the
+// zero-padded half of an unbounded axis): both 16-point halves are half zero.
+template <bool INV, typename C> __device__ __forceinline__ void dft32_half(C *x)
+{
+    using S = decltype(x[0].x);
+    C e[16], o[16];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        e[i] = x[2 * i];
+        o[i] = x[2 * i + 1];
+    }
+    dft16_half<INV>(e);
+    dft16_half<INV>(o);
     const S c[8] = {(S)1.0, (S)0.98078528040323044913, (S)0.92387953251128675613, (S)0.83146961230254523708,
                     (S)0.70710678118654752440, (S)0.55557023301960222474, (S)0.38268343236508977173,
                     (S)0.19509032201612826785};

@@ -9,7 +9,11 @@ namespace wide {
 
 // ---------------------------------------------------------------------------
 // y pass: strided columns, in place.
-template <int L, bool INV>
+// HALF: the y axis is unbounded. Forward: n_in = L / 2, so the first stage
+// (one radix-32 butterfly a thread over n = t + r L/32) has data only for
+// r < 16. Inverse: n_out = L / 2, so the last stage writes only its first
+// R/2 outputs (positions r M + bf < L / 2).
+template <int L, bool INV, bool HALF>
 __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
 {
     using C = float2;
@@ -31,15 +35,22 @@ __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
     {   // first stage from global
         using T0 = St<L, 0>;
         C v[T0::U][T0::R];
-        const int n_in = active ? a.n_in : 0;
+        if constexpr (HALF && !INV) {
+            static_assert(T0::U == 1 && T0::R == 32, "one radix-32 butterfly a thread in the first stage");
 #pragma unroll
-        for (int u = 0; u < T0::U; ++u)
+            for (int r = 0; r < 16; ++r) v[0][r] = active ? col[T0::in_pos(t, 0, r) * as] : C{0.f, 0.f};
+            dft32_half<INV>(v[0]);
+        } else {
+            const int n_in = active ? a.n_in : 0;
 #pragma unroll
-            for (int r = 0; r < T0::R; ++r) {
-                const int n = T0::in_pos(t, u, r);
-                v[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
-            }
-        twiddle_dft<L, 0, INV>(v, TW, t);
+            for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+                for (int r = 0; r < T0::R; ++r) {
+                    const int n = T0::in_pos(t, u, r);
+                    v[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
+                }
+            twiddle_dft<L, 0, INV>(v, TW, t);
+        }
         write_line<L, 0>(line, t, v);
     }
     __syncthreads();
@@ -50,12 +61,14 @@ __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
         read_line<L, LAST>(line, t, v);
         twiddle_dft<L, LAST, INV>(v, TW, t);
         if (active) {
+            // HALF inverse: out_pos = r M + bf with bf < M = L / R, so r < R/2 is the cropped half
+            constexpr int RW = (HALF && INV) ? TL::R / 2 : TL::R;
 #pragma unroll
             for (int u = 0; u < TL::U; ++u)
 #pragma unroll
-                for (int r = 0; r < TL::R; ++r) {
+                for (int r = 0; r < RW; ++r) {
                     const int n = TL::out_pos(t, u, r);
-                    if (n < a.n_out) col[n * as] = v[u][r];
+                    if ((HALF && INV) || n < a.n_out) col[n * as] = v[u][r];
                 }
         }
     }
@@ -366,28 +379,38 @@ cudaError_t launch_xfwd(const XFwdArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+template <int L, bool INV, bool HALF>
+static cudaError_t launch_col_t(const ColArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    const cudaError_t e = prep(k_col<L, INV, HALF>, sm);
+    if (e != cudaSuccess) return e;
+    k_col<L, INV, HALF><<<grid, nt, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L> static cudaError_t launch_col_len(int inverse, const ColArgs &a, dim3 grid, int nt, size_t sm,
+                                                   cudaStream_t st)
+{
+    // the zero-padded half of an unbounded axis: forward input, inverse output
+    if (inverse)
+        return 2 * a.n_out == L ? launch_col_t<L, true, true>(a, grid, nt, sm, st)
+                                : launch_col_t<L, true, false>(a, grid, nt, sm, st);
+    return 2 * a.n_in == L ? launch_col_t<L, false, true>(a, grid, nt, sm, st)
+                           : launch_col_t<L, false, false>(a, grid, nt, sm, st);
+}
+
 cudaError_t launch_col(int inverse, const ColArgs &a, int outer, cudaStream_t st)
 {
     dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), outer, a.ncomp);
     const size_t sm = smem_lines(a.L, a.B, 1, a.plan.ntw, true);
     const int nt = a.B * (a.L / 32);
-    cudaError_t e;
     switch (a.L) {
-#define X(LV)                                                                      \
-    case LV:                                                                       \
-        if (inverse) {                                                             \
-            if ((e = prep(k_col<LV, true>, sm)) != cudaSuccess) return e;          \
-            k_col<LV, true><<<grid, nt, sm, st>>>(a);                              \
-        } else {                                                                   \
-            if ((e = prep(k_col<LV, false>, sm)) != cudaSuccess) return e;         \
-            k_col<LV, false><<<grid, nt, sm, st>>>(a);                             \
-        }                                                                          \
-        break;
+#define X(LV) \
+    case LV: return launch_col_len<LV>(inverse, a, grid, nt, sm, st);
         PS_WIDE_LENGTHS(X)
 #undef X
     default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 template <int L> cudaError_t launch_z_len(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)

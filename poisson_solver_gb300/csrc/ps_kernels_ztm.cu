@@ -116,7 +116,11 @@ __device__ __forceinline__ void unstash(uint32_t taddr, float2 (&v)[U][R])
 
 constexpr int SLOT_COLUMNS = 64;  // 32 complex values
 
-template <int L, int OP>
+// HALF: the z axis is unbounded (n_in = n_out = L / 2). The first forward
+// stage (one radix-32 butterfly a thread over n = t + r L/32) then has data
+// only for r < 16, and the last inverse stage writes only r < 16: the loads,
+// stores and the zero half of the DFT arithmetic drop out.
+template <int L, int OP, bool HALF>
 __global__ void __launch_bounds__(ZT_MAX_THREADS) k_zt(const ZArgs a, const int tm_cols)
 {
     using C = float2;
@@ -158,14 +162,21 @@ __global__ void __launch_bounds__(ZT_MAX_THREADS) k_zt(const ZArgs a, const int 
         {
             const C *col = reinterpret_cast<const C *>(pick3(a.in, c)) + off;
             C v0[T0::U][T0::R];
+            if constexpr (HALF) {
+                static_assert(T0::U == 1 && T0::R == 32, "one radix-32 butterfly a thread in the first stage");
 #pragma unroll
-            for (int u = 0; u < T0::U; ++u)
+                for (int r = 0; r < 16; ++r) v0[0][r] = active ? col[T0::in_pos(t, 0, r) * as] : C{0.f, 0.f};
+                dft32_half<false>(v0[0]);
+            } else {
 #pragma unroll
-                for (int r = 0; r < T0::R; ++r) {
-                    const int n = T0::in_pos(t, u, r);
-                    v0[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
-                }
-            twiddle_dft<L, 0, false>(v0, TW, t);
+                for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+                    for (int r = 0; r < T0::R; ++r) {
+                        const int n = T0::in_pos(t, u, r);
+                        v0[u][r] = n < n_in ? col[n * as] : C{0.f, 0.f};
+                    }
+                twiddle_dft<L, 0, false>(v0, TW, t);
+            }
             write_line<L, 0>(line, t, v0);
         }
         __syncthreads();
@@ -268,13 +279,18 @@ __global__ void __launch_bounds__(ZT_MAX_THREADS) k_zt(const ZArgs a, const int 
         adjoint_dft<L, 0>(v0, TW, t);
         if (active) {
             C *col = col0 + off;
+            if constexpr (HALF) {
 #pragma unroll
-            for (int u = 0; u < T0::U; ++u)
+                for (int r = 0; r < 16; ++r) col[T0::in_pos(t, 0, r) * as] = v0[0][r];
+            } else {
 #pragma unroll
-                for (int r = 0; r < T0::R; ++r) {
-                    const int n = T0::in_pos(t, u, r);
-                    if (n < a.n_out) col[n * as] = v0[u][r];
-                }
+                for (int u = 0; u < T0::U; ++u)
+#pragma unroll
+                    for (int r = 0; r < T0::R; ++r) {
+                        const int n = T0::in_pos(t, u, r);
+                        if (n < a.n_out) col[n * as] = v0[u][r];
+                    }
+            }
         }
         ++ph;
     }
@@ -333,16 +349,23 @@ template <typename K> size_t smem_for_columns(K kernel, int threads, size_t sm, 
     return out;
 }
 
-template <int L, int OP> cudaError_t launch_zt_op(const ZArgs &a, dim3 grid, int nt, cudaStream_t st)
+template <int L, int OP, bool HALF> cudaError_t launch_zt_half(const ZArgs &a, dim3 grid, int nt, cudaStream_t st)
 {
     const int cols = columns_zt(nt);
-    const size_t sm = smem_for_columns(k_zt<L, OP>, nt, smem_zt(L, a.B, a.plan.ntw), cols);
+    const size_t sm = smem_for_columns(k_zt<L, OP, HALF>, nt, smem_zt(L, a.B, a.plan.ntw), cols);
     if (!sm) return cudaErrorInvalidConfiguration;
     // the attribute is per kernel: another configuration may have lowered it
-    const cudaError_t e = cudaFuncSetAttribute(k_zt<L, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_zt<L, OP, HALF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_zt<L, OP><<<grid, nt, sm, st>>>(a, cols);
+    k_zt<L, OP, HALF><<<grid, nt, sm, st>>>(a, cols);
     return cudaGetLastError();
+}
+
+template <int L, int OP> cudaError_t launch_zt_op(const ZArgs &a, dim3 grid, int nt, cudaStream_t st)
+{
+    if (2 * a.n_in == L && 2 * a.n_out == L) return launch_zt_half<L, OP, true>(a, grid, nt, st);
+    return launch_zt_half<L, OP, false>(a, grid, nt, st);
 }
 
 template <int L> cudaError_t launch_zt_len(const ZArgs &a, dim3 grid, int nt, cudaStream_t st)

@@ -83,3 +83,24 @@ def test_tmem_z_lines_per_cta(native, oracle, monkeypatch, lines):
     monkeypatch.setenv("PS_LINES_Z", str(lines))
     got, _ = native.solve(nc, bc, dx, B, 2, precision="fp32", **opts)
     assert rel_l2(got, ref) < FP32_TOL
+
+
+# tall y extents: the wide y kernels at P_y = 256 .. 1024, unbounded (the
+# zero-padded half pruned) and periodic
+Y_SHAPES = [
+    ((6, 128, 8), (0, 0, 0)),
+    ((4, 256, 6), (0, 0, 0)),
+    ((4, 512, 4), (0, 0, 0)),
+    ((6, 256, 6), (1, 1, 1)),
+    ((5, 512, 7), (0, 0, 1)),
+]
+
+
+@pytest.mark.parametrize("yi", range(len(Y_SHAPES)))
+def test_fp32_wide_y_vs_oracle(native, oracle, yi):
+    nc, bc = Y_SHAPES[yi]
+    dx = (2.0 / nc[0], 1.5 / nc[1], 2.5 / nc[2])
+    B = _fields(nc, (0, 1, 2), 500 + yi)
+    ref, _ = oracle.solve3d(nc, bc, dx, B, 2, curl=True)
+    got, _ = native.solve(nc, bc, dx, B, 2, precision="fp32", curl=True)
+    assert rel_l2(got, ref) < FP32_TOL
