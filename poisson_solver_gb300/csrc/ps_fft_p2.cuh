@@ -147,14 +147,56 @@ __device__ __forceinline__ void stage_sets(C *line, const C *tws, int t, int nco
     __syncthreads();
 }
 
-// All stages over ncomp line sets.
-template <int L, int EM, bool INV, typename C, int S = 0>
+// Stages S .. SEND-1 over ncomp line sets.
+template <int L, int EM, bool INV, typename C, int S = 0, int SEND = Plan<L, EM>::NST>
 __device__ __forceinline__ void run(C *line, const C *tws, int t, int ncomp = 1, int cstride = 0)
 {
-    if constexpr (S < Plan<L, EM>::NST) {
+    if constexpr (S < SEND) {
         stage_sets<L, EM, S, INV>(line, tws, t, ncomp, cstride);
-        run<L, EM, INV, C, S + 1>(line, tws, t, ncomp, cstride);
+        run<L, EM, INV, C, S + 1, SEND>(line, tws, t, ncomp, cstride);
     }
+}
+
+// Stage 0 of a transform whose inputs n >= L/2 are zero (the padded half of an
+// unbounded axis): a radix-16 stage (bf + r NBF, M = 1) reads r < 8 and runs
+// the half-input DFT; the zero half is never read, so it need not be stored.
+template <int L, int EM, bool INV, typename C> __device__ __forceinline__ void stage0_half(C *line, int t)
+{
+    using PL = Plan<L, EM>;
+    constexpr int R = PL::radix(0), U = EM / R, NBF = L / R, TPL = PL::TPL;
+    static_assert(R == 16, "a radix-16 first stage");
+    C v[U][R];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int bf = t + u * TPL;
+#pragma unroll
+        for (int r = 0; r < R / 2; ++r) v[u][r] = line[sk<C>(bf + r * NBF)];
+        dft16_half<INV>(v[u]);
+    }
+    __syncthreads();
+    stage_write<L, EM, 0>(line, t, v);
+    __syncthreads();
+}
+
+// The last stage of a transform whose outputs n >= L/2 are cropped: it writes
+// positions r M + bf (bf < M = L / R) for r < R/2 only; the other outputs of
+// its DFT are dead code.
+template <int L, int EM, bool INV, typename C>
+__device__ __forceinline__ void last_stage_half(C *line, const C *tws, int t)
+{
+    using PL = Plan<L, EM>;
+    constexpr int S = PL::NST - 1, R = PL::radix(S), M = PL::mm(S), U = EM / R, TPL = PL::TPL;
+    static_assert(M * R == L, "the last stage");
+    C v[U][R];
+    stage_read<L, EM, S, INV>(line, tws, t, v);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int bf = t + u * TPL;
+#pragma unroll
+        for (int r = 0; r < R / 2; ++r) line[sk<C>(r * M + bf)] = v[u][r];
+    }
+    __syncthreads();
 }
 
 }  // namespace p2

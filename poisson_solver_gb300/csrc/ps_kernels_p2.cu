@@ -34,7 +34,9 @@ template <typename T> __device__ __forceinline__ T wavenumber(int k, int P, T c,
 // BL lines a CTA is a template parameter, so the thread count NT = BL TPL is
 // a constant and the load, separation and store loops address global memory
 // as one row base plus immediate offsets.
-template <typename T, int L, int EM, int BL>
+// HALF: the x axis is unbounded (n_in = L / 2): the padded half is neither
+// stored nor read (stage0_half).
+template <typename T, int L, int EM, int BL, bool HALF>
 __global__ void __launch_bounds__(BL *(L / EM)) k_xfwd(const XFwdArgs a)
 {
     using C = typename CxT<T>::type;
@@ -58,22 +60,23 @@ __global__ void __launch_bounds__(BL *(L / EM)) k_xfwd(const XFwdArgs a)
     // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last row
     if (!a.mirror) {
         // every load of the thread issued before the first shared-memory store
-        C v[BL][PER];
+        constexpr int JN = HALF ? PER / 2 : PER;  // HALF: n < L/2 = n_in exactly
+        C v[BL][JN];
 #pragma unroll
         for (int l = 0; l < BL; ++l) {
             const long long ra = row0 + 2 * l;
             const double *pa = in + ra * a.in_stride + tid, *pb = pa + a.in_stride;
             const bool va = ra < rows, vb = ra + 1 < rows;
 #pragma unroll
-            for (int j = 0; j < PER; ++j) {
-                const bool live = tid + j * NT < a.n_in;
+            for (int j = 0; j < JN; ++j) {
+                const bool live = HALF || tid + j * NT < a.n_in;
                 v[l][j] = C{(live && va) ? (T)pa[j * NT] : (T)0, (live && vb) ? (T)pb[j * NT] : (T)0};
             }
         }
 #pragma unroll
         for (int l = 0; l < BL; ++l)
 #pragma unroll
-            for (int j = 0; j < PER; ++j) S[l * LDP + sk<C>(tid + j * NT)] = v[l][j];
+            for (int j = 0; j < JN; ++j) S[l * LDP + sk<C>(tid + j * NT)] = v[l][j];
     } else {
         // rows of the kernel octant, mirrored: (z, y) -> (min(z, Pz-z), min(y, Py-y)), n -> min(n, L-n)
         for (int line = 0; line < BL; ++line) {
@@ -101,7 +104,13 @@ __global__ void __launch_bounds__(BL *(L / EM)) k_xfwd(const XFwdArgs a)
         }
     }
     __syncthreads();
-    run<L, EM, false>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    if constexpr (HALF) {
+        // the mirrored kernel rows (a.mirror) are never HALF: the launcher checks
+        stage0_half<L, EM, false>(S + (tid >> LT) * LDP, tid & (TPL - 1));
+        run<L, EM, false, C, 1>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    } else {
+        run<L, EM, false>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    }
 
     constexpr int Mx = L / 2 + 1, KPER = (Mx + NT - 1) / NT;
 #pragma unroll
@@ -270,7 +279,8 @@ __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
 
 // ---------------------------------------------------------------------------
 // x inverse: half spectra of row pairs -> real rows, cropped.
-template <typename T, int L, int EM, int BL>
+// HALF: n_out = L / 2 (unbounded x): the last stage writes only the kept half.
+template <typename T, int L, int EM, int BL, bool HALF>
 __global__ void __launch_bounds__(BL *(L / EM)) k_xinv(const XInvArgs a)
 {
     using C = typename CxT<T>::type;
@@ -321,7 +331,12 @@ __global__ void __launch_bounds__(BL *(L / EM)) k_xinv(const XInvArgs a)
         }
     }
     __syncthreads();
-    run<L, EM, true>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    if constexpr (HALF) {
+        run<L, EM, true, C, 0, Plan<L, EM>::NST - 1>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+        last_stage_half<L, EM, true>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    } else {
+        run<L, EM, true>(S + (tid >> LT) * LDP, TW, tid & (TPL - 1));
+    }
 
     // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;
@@ -367,20 +382,35 @@ size_t smem_lines(int prec, int L, int B, int nbuf, int ntw_entries)
 }
 
 // The x kernels are compiled for 1, 2, 4 or 8 lines a CTA.
+template <int L, int BL, bool HALF>
+cudaError_t launch_xfwd_h(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    const cudaError_t e = prep(k_xfwd<float, L, 16, BL, HALF>, sm);
+    if (e != cudaSuccess) return e;
+    k_xfwd<float, L, 16, BL, HALF><<<grid, nt, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
 template <int L, int BL> cudaError_t launch_xfwd_t(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    const cudaError_t e = prep(k_xfwd<float, L, 16, BL>, sm);
+    // the zero-padded half of an unbounded axis (never for mirrored kernel rows)
+    if (!a.mirror && 2 * a.n_in == L && L >= 256) return launch_xfwd_h<L, BL, true>(a, grid, nt, sm, st);
+    return launch_xfwd_h<L, BL, false>(a, grid, nt, sm, st);
+}
+
+template <int L, int BL, bool HALF>
+cudaError_t launch_xinv_h(const XInvArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
+{
+    const cudaError_t e = prep(k_xinv<float, L, 16, BL, HALF>, sm);
     if (e != cudaSuccess) return e;
-    k_xfwd<float, L, 16, BL><<<grid, nt, sm, st>>>(a);
+    k_xinv<float, L, 16, BL, HALF><<<grid, nt, sm, st>>>(a);
     return cudaGetLastError();
 }
 
 template <int L, int BL> cudaError_t launch_xinv_t(const XInvArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    const cudaError_t e = prep(k_xinv<float, L, 16, BL>, sm);
-    if (e != cudaSuccess) return e;
-    k_xinv<float, L, 16, BL><<<grid, nt, sm, st>>>(a);
-    return cudaGetLastError();
+    if (2 * a.n_out == L && L >= 256) return launch_xinv_h<L, BL, true>(a, grid, nt, sm, st);
+    return launch_xinv_h<L, BL, false>(a, grid, nt, sm, st);
 }
 
 template <int L> cudaError_t launch_xfwd_len(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
