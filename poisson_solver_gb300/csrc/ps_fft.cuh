@@ -504,15 +504,15 @@ template <typename T> __device__ __forceinline__ T pick3(const T (&a)[3], int c)
     return c == 0 ? a[0] : (c == 1 ? a[1] : a[2]);
 }
 
-// Element offsets of the rows row0 .. row0 + nrows - 1 of a [rows_z][ystride][Mx]
+// Element offsets of the rows row0 .. row0 + nrows - 1 of a [rows_z][ystride][ld]
 // half-spectrum array (row r = (z, y) with y = r mod rows_y), -1 past the last
 // row. The x passes compute them once per CTA instead of dividing per element.
 __device__ __forceinline__ void row_offsets(long long *ofs, long long row0, int nrows, long long rows, int rows_y,
-                                            int ystride, int Mx)
+                                            int ystride, int ld)
 {
     for (int i = threadIdx.x; i < nrows; i += blockDim.x) {
         const long long r = row0 + i;
-        ofs[i] = r < rows ? ((r / rows_y) * ystride + r % rows_y) * Mx : -1;
+        ofs[i] = r < rows ? ((r / rows_y) * ystride + r % rows_y) * ld : -1;
     }
 }
 

@@ -52,7 +52,7 @@ __device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, i
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)bx * 2 * B;
     __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, a.Mx);
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, a.ld);
 
     // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last
     // row. With the mirror flag the rows are those of the kernel octant,
@@ -313,7 +313,7 @@ __device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, i
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)bx * 2 * B;
     __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, a.ld);
     __syncthreads();
 
     for (int line = 0; line < B; ++line) {

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(BL *(L / EM)) k_xfwd(const XFwdArgs a)
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * BL;
     __shared__ long long rofs[2 * BL];
-    row_offsets(rofs, row0, 2 * BL, rows, a.rows_y, a.out_y, L / 2 + 1);
+    row_offsets(rofs, row0, 2 * BL, rows, a.rows_y, a.out_y, a.ld);
 
     // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last row
     if (!a.mirror) {
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(BL *(L / EM)) k_xinv(const XInvArgs a)
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long row0 = (long long)blockIdx.x * 2 * BL;
     __shared__ long long rofs[2 * BL];
-    row_offsets(rofs, row0, 2 * BL, rows, a.rows_y, a.in_y, Mx);
+    row_offsets(rofs, row0, 2 * BL, rows, a.rows_y, a.in_y, a.ld);
     __syncthreads();
 
     // Z = Xa + i Xb over the full line from the two half spectra

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
     const long long rows = (long long)a.rows_y * a.rows_z;
     const long long ra = (long long)blockIdx.x * 2 * B + 2 * b, rb = ra + 1;
     __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, (long long)blockIdx.x * 2 * B, 2 * B, rows, a.rows_y, a.out_y, L / 2 + 1);
+    row_offsets(rofs, (long long)blockIdx.x * 2 * B, 2 * B, rows, a.rows_y, a.out_y, a.ld);
     C *line = S + b * LDP;
     {
         using T0 = St<L, 0>;
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
     const long long row0 = (long long)blockIdx.x * 2 * B;
     const int nt = blockDim.x;
     __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, Mx);
+    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, a.ld);
     __syncthreads();
     for (int idx = threadIdx.x; idx < B * Mx; idx += nt) {
         const int l = idx / Mx, k = idx - l * Mx;

@@ -232,6 +232,7 @@ int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
     xa.rows_z = n[2];
     xa.out_y = P[1];
     xa.Mx = Mx;
+    xa.ld = Mx;  // the scratch spectra are unpadded
     xa.plan = px;
     xa.B = lines_per_cta(px.tpl, [&](int B) { return smem_x(prec, px, B); });
     PS_NA_CK(launch_xfwd(prec, xa, s.stream));
@@ -317,6 +318,7 @@ int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
         xi.L = P[0];
         xi.n_out = n[0];
         xi.Mx = Mx;
+        xi.ld = Mx;
         xi.rows_y = n[1];
         xi.rows_z = n[2];
         xi.in_y = P[1];

@@ -297,6 +297,7 @@ void Solver::setup3d(const int ncell[3], const int bcs[3], const double dxs[3], 
     }
     reg = reg_order;
     Mx = P[0] / 2 + 1;
+    ldx = (Mx + 1) & ~1;  // even: rows of the spectra are whole 16-byte units
     oy = P[1] / 2 + 1;
     oz = P[2] / 2 + 1;
     pushed = produced = rhs_ready = 0;
@@ -393,6 +394,7 @@ void Solver::build_kernel()
         xa.rows_z = pz;
         xa.out_y = P[1];
         xa.Mx = Mx;
+        xa.ld = Mx;  // the kernel-build spectrum is unpadded
         xa.mirror = 1;
         xa.oct_x = ox;
         xa.oct_y = oy;
@@ -536,6 +538,7 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     xa.rows_z = n[2];
     xa.out_y = P[1];
     xa.Mx = Mx;
+    xa.ld = ldx;
 
     // y forward (zero-padded from Ny to Py)
     ColArgs &ya = pa.y;
@@ -545,8 +548,8 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     ya.n_in = n[1];
     ya.n_out = P[1];
     ya.Mx = Mx;
-    ya.axis_stride = Mx;
-    ya.outer_stride = (long long)P[1] * Mx;
+    ya.axis_stride = ldx;
+    ya.outer_stride = (long long)P[1] * ldx;
 
     // z: forward (zero-padded from Nz to Pz), spectral operation, inverse (cropped)
     ZArgs &za = pa.z;
@@ -578,8 +581,8 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     za.n_in = n[2];
     za.n_out = n[2];
     za.Mx = Mx;
-    za.axis_stride = (long long)P[1] * Mx;
-    za.row_stride = Mx;
+    za.axis_stride = (long long)P[1] * ldx;
+    za.row_stride = ldx;
     za.op = op;
     za.reproject = op == OP_FILTER && opt_reproject && in_mask == 7;
     za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
@@ -600,8 +603,8 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     yi.n_in = P[1];
     yi.n_out = n[1];
     yi.Mx = Mx;
-    yi.axis_stride = Mx;
-    yi.outer_stride = (long long)P[1] * Mx;
+    yi.axis_stride = ldx;
+    yi.outer_stride = (long long)P[1] * ldx;
 
     XInvArgs &xi = pa.xi;
     for (int c = 0; c < 3; ++c)
@@ -613,6 +616,7 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     xi.L = P[0];
     xi.n_out = n[0];
     xi.Mx = Mx;
+    xi.ld = ldx;
     xi.rows_y = n[1];
     xi.rows_z = n[2];
     xi.in_y = P[1];

@@ -65,6 +65,7 @@ struct Solver {
     double dx[3] = {0, 0, 0};
     int reg = 0;
     int Mx = 0, oy = 0, oz = 0;  // half-spectrum length and kernel octant extents
+    int ldx = 0;                 // row pitch of the spectra work[c] (Mx rounded up to even)
 
     int opt_grad = 0, opt_div = 0, opt_curl = 0, opt_reproject = 0;
     int precision = PREC_FP64;
@@ -137,7 +138,7 @@ private:
     void build_kernel();
     void check_setup() const;
     size_t field_elems() const { return (size_t)n[0] * n[1] * n[2]; }
-    size_t work_elems() const { return (size_t)n[2] * P[1] * Mx; }
+    size_t work_elems() const { return (size_t)n[2] * P[1] * ldx; }
 };
 
 // The FP64 solve in fixed, library-owned device memory (ps_noalloc.cu).

@@ -62,6 +62,7 @@ struct XFwdArgs {
     int rows_y, rows_z;  // row r = k * rows_y + j
     int out_y;           // y extent of the output array
     int Mx;              // L/2 + 1
+    int ld;              // row pitch of the output array (>= Mx)
     int mirror;          // input is the octant of an even function
     int oct_x, oct_y;    // octant extents (x, y) when mirrored
     int Py, Pz;          // full extents the octant is reflected onto
@@ -113,6 +114,7 @@ struct XInvArgs {
     int Mx;
     int rows_y, rows_z;
     int in_y;             // y extent of the input array
+    int ld;               // row pitch of the input array (>= Mx)
     long long out_stride; // row stride of the output rows
     int B;
     FftPlanDev plan;
