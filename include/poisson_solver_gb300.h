@@ -38,7 +38,10 @@ enum {
     PS_ERR_MEMORY = 4,      /* device or host allocation failed */
     PS_ERR_CUDA = 5,        /* a CUDA call failed */
     PS_ERR_STATE = 6,       /* call out of order (e.g. solve before setup/push) */
-    PS_ERR_UNSUPPORTED = 7  /* outside what this build implements (e.g. 2D) */
+    PS_ERR_UNSUPPORTED = 7, /* outside what this build implements (e.g. 2D) */
+    PS_ERR_TIMEOUT = 8      /* a kernel's bounded wait for an asynchronous copy ran
+                               out (reported by the next synchronising call:
+                               ps_pull, ps_pull_device, ps_synchronize) */
 };
 
 /* Options for ps_set_option. */
@@ -172,7 +175,7 @@ int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset);
  * configuration on the same GPU model reuse them. Without tuning a measured
  * default is used. ps_get_pass_config reports the family and lines a solve
  * with component_mask would run for pass 0..4. */
-enum { PS_FAMILY_RUNTIME = 0, PS_FAMILY_P2 = 1, PS_FAMILY_WIDE = 2, PS_FAMILY_TMEM = 3 };
+enum { PS_FAMILY_RUNTIME = 0, PS_FAMILY_P2 = 1, PS_FAMILY_WIDE = 2, PS_FAMILY_TMEM = 3, PS_FAMILY_TMA = 4 };
 int ps_autotune(ps_solver *h, int component_mask);
 int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, int *lines);
 

@@ -19,6 +19,7 @@ PS_ERR_MEMORY = 4
 PS_ERR_CUDA = 5
 PS_ERR_STATE = 6
 PS_ERR_UNSUPPORTED = 7
+PS_ERR_TIMEOUT = 8
 
 PS_OPT_GRAD = 0
 PS_OPT_DIV = 1
@@ -41,7 +42,8 @@ PS_FAMILY_RUNTIME = 0
 PS_FAMILY_P2 = 1
 PS_FAMILY_WIDE = 2
 PS_FAMILY_TMEM = 3
-FAMILY_NAMES = {0: "runtime", 1: "p2", 2: "wide", 3: "tmem"}
+PS_FAMILY_TMA = 4
+FAMILY_NAMES = {0: "runtime", 1: "p2", 2: "wide", 3: "tmem", 4: "tma"}
 
 PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0
 PS_BATCH_INFO_TILES_PER_SOLVE = 1

@@ -161,10 +161,7 @@ int ps_set_stream(ps_solver *h, void *stream)
 
 int ps_synchronize(ps_solver *h)
 {
-    return guarded(h, [&](ps::Solver &s) {
-        cudaError_t e = cudaStreamSynchronize(s.stream);
-        if (e != cudaSuccess) throw ps::Error(PS_ERR_CUDA, cudaGetErrorString(e));
-    });
+    return guarded(h, [&](ps::Solver &s) { s.synchronize(); });
 }
 
 const char *ps_last_error(const ps_solver *h) { return h ? h->s.last_error.c_str() : "NULL handle"; }
@@ -224,8 +221,11 @@ int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, 
     if (!family || !lines) return PS_ERR_ARGUMENT;
     return guarded(h, [&](ps::Solver &s) {
         const ps::PassChoice c = s.current_choice(pass, component_mask);
-        *family = c.fam == 'p' ? PS_FAMILY_P2 : c.fam == 'w' ? PS_FAMILY_WIDE : c.fam == 't' ? PS_FAMILY_TMEM
-                                                                                             : PS_FAMILY_RUNTIME;
+        *family = c.fam == 'p'   ? PS_FAMILY_P2
+                  : c.fam == 'w' ? PS_FAMILY_WIDE
+                  : c.fam == 't' ? PS_FAMILY_TMEM
+                  : c.fam == 'q' ? PS_FAMILY_TMA
+                                 : PS_FAMILY_RUNTIME;
         *lines = c.B;
     });
 }

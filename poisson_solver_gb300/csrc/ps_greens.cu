@@ -307,4 +307,29 @@ cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t 
     return cudaGetLastError();
 }
 
+// 32 x 32 (x, z) tiles of one y row through shared memory: reads along x,
+// writes along z, both coalesced.
+__global__ void k_kernel_zfast(const double *__restrict__ kern, float *__restrict__ out, int Mx, int oy, int oz,
+                               int kzp)
+{
+    __shared__ float tile[32][33];
+    const int y = blockIdx.z, x0 = blockIdx.x * 32, z0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int z = z0 + r, x = x0 + threadIdx.x;
+        tile[r][threadIdx.x] = (z < oz && x < Mx) ? (float)kern[((long long)z * oy + y) * Mx + x] : 0.f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int x = x0 + r, z = z0 + threadIdx.x;
+        if (x < Mx && z < kzp) out[((long long)y * Mx + x) * kzp + z] = tile[threadIdx.x][r];
+    }
+}
+
+cudaError_t launch_kernel_zfast(const double *kern, float *out, int Mx, int oy, int oz, int kzp, cudaStream_t st)
+{
+    const dim3 grid((unsigned)((Mx + 31) / 32), (unsigned)((kzp + 31) / 32), (unsigned)oy);
+    k_kernel_zfast<<<grid, dim3(32, 8), 0, st>>>(kern, out, Mx, oy, oz, kzp);
+    return cudaGetLastError();
+}
+
 }  // namespace ps

@@ -300,8 +300,10 @@ void Solver::setup3d(const int ncell[3], const int bcs[3], const double dxs[3], 
     ldx = (Mx + 1) & ~1;  // even: rows of the spectra are whole 16-byte units
     oy = P[1] / 2 + 1;
     oz = P[2] / 2 + 1;
+    kzp = (oz + 3) & ~3;
     pushed = produced = rhs_ready = 0;
     kern32.release();
+    kernzf32.release();
     zeta64.release();
     zeta32.release();
     for (int c = 0; c < 3; ++c) {
@@ -311,6 +313,11 @@ void Solver::setup3d(const int ncell[3], const int bcs[3], const double dxs[3], 
         fr[c].release();
     }
     build_kernel();
+    if (!status.p) {
+        status.ensure(sizeof(int));
+        PS_CK(cudaMemsetAsync(status.p, 0, sizeof(int), stream));
+        PS_CK(cudaStreamSynchronize(stream));
+    }
     is_setup = true;
 }
 
@@ -448,9 +455,15 @@ void Solver::ensure_kernel(int prec)
 {
     if (prec == PREC_FP64) return;
     const size_t nk = (size_t)Mx * oy * oz;
-    if (kern32.p && kern32.bytes >= nk * sizeof(float)) return;
-    kern32.ensure(nk * sizeof(float));
-    PS_CK(launch_to_fp32((const double *)kern64.p, (float *)kern32.p, nk, stream));
+    if (!kern32.p) {
+        kern32.ensure(nk * sizeof(float));
+        PS_CK(launch_to_fp32((const double *)kern64.p, (float *)kern32.p, nk, stream));
+    }
+    // the z-fastest copy for the bulk-copy z kernel, on the z extents it runs
+    if (!kernzf32.p && bc[2] == 0 && (P[2] == 256 || P[2] == 512 || P[2] == 1024)) {
+        kernzf32.ensure((size_t)Mx * oy * kzp * sizeof(float));
+        PS_CK(launch_kernel_zfast((const double *)kern64.p, (float *)kernzf32.p, Mx, oy, oz, kzp, stream));
+    }
 }
 
 void Solver::ensure_zeta(int prec)
@@ -588,6 +601,8 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
     za.zeta = op == OP_FILTER ? (prec == PREC_FP64 ? zeta64.p : zeta32.p) : nullptr;
     za.oct_y = oy;
+    za.kern_zf = prec == PREC_FP32 ? static_cast<const float *>(kernzf32.p) : nullptr;
+    za.kzp = kzp;
     za.Px = P[0];
     za.Py = P[1];
     za.Pz = P[2];
@@ -630,7 +645,8 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
 // Families: 'r' run-time kernels (any length, FP64 and FP32), 'p' length-
 // specialised FP32 kernels (powers of two 64..2048), 'w' wide FP32 kernels
 // (256..2048; for z the shared-memory fused kernel), 't' the fused z kernel
-// with tensor-memory staging (z only). Defaults, measured at 512^3 (FP32
+// with tensor-memory staging (z only), 'q' the fused z kernel with a warp per
+// column group fed by tiled bulk copies (z only, unbounded z of 256..1024). Defaults, measured at 512^3 (FP32
 // curl): x forward p2 with 2 lines a CTA (2.3 against 3.4 ms for wide),
 // x inverse p2 with 4, y wide with 8, z tensor-memory with 8. PS_KERNELS,
 // PS_KERNELS_X/_Y/_Z (= wide, p2 or runtime), PS_LINES_X/_XI/_Y/_Z and PS_Z_EM
@@ -646,13 +662,15 @@ bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
     case 'p': return p2::supported(prec, L) && (pass != 2 || p2::supports_op(op));
     case 'w': return wide::supported(prec, L) && (pass != 2 || p2::supports_op(op));
     case 't': return pass == 2 && wide::zt_supported(prec, L, op, pa.z.nin, pa.z.nout);
+    case 'q':
+        return pass == 2 && pa.z.kern_zf && wide::zq_supported(prec, L, op, pa.z.nin, pa.z.nout, pa.z.n_in, pa.z.n_out);
     default: return false;
     }
 }
 
 int Solver::family_emax(int pass, char fam) const
 {
-    if (fam == 'w' || fam == 't') return 32;
+    if (fam == 'w' || fam == 't' || fam == 'q') return 32;
     if (pass == 2) {
         if (fam == 'p') {
             const char *v = getenv("PS_Z_EM");  // 16 measured faster than 8 (13.4 vs 15.4 ms at 512^3)
@@ -670,6 +688,7 @@ size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Pl
     const int nbuf = std::max(pa.z.nin, pa.z.nout);
     if (pass == 2) {
         if (fam == 't') return wide::smem_lines_zt(L, B, ntw);
+        if (fam == 'q') return wide::smem_lines_zq(L, ntw);
         if (fam == 'w') return wide::smem_lines(L, B, nbuf, ntw, true);
         if (fam == 'p') return p2::smem_lines(prec, L, B, nbuf, ntw);
         return smem_z(prec, pl.dev, B, nbuf);
@@ -691,6 +710,8 @@ bool Solver::pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan
     if ((pass == 0 || pass == 4) && fam == 'p' && B > 8) return false;  // compiled for 1, 2, 4, 8 lines
     if ((pass == 0 || pass == 4) && B > MAX_LINES) return false;
     if (pass == 2 && fam == 't' && nt % 32 != 0) return false;           // whole warps
+    if (pass == 2 && fam == 'q')  // fixed lines per length; no static shared memory
+        return B == wide::zq_lines(pl.dev.L) && pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
     return nt <= max_threads && pass_smem(pass, fam, B, pa, pl) <= (size_t)limit;
 }
 
@@ -706,6 +727,7 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     else if (f && strcmp(f, "p2") == 0) fam = family_ok(pass, 'p', pa) ? 'p' : 'r';
     else if (f && strcmp(f, "wide") == 0)
         fam = family_ok(pass, 'w', pa) ? 'w' : family_ok(pass, 'p', pa) ? 'p' : 'r';
+    else if (f && strcmp(f, "tma") == 0 && family_ok(pass, 'q', pa)) fam = 'q';
     else if (pass == 2 && family_ok(pass, 't', pa)) fam = 't';
     else if (axis > 0 && family_ok(pass, 'w', pa)) fam = 'w';
     else fam = family_ok(pass, 'p', pa) ? 'p' : 'r';
@@ -720,6 +742,7 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
         if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) pref = want;
     }
     const Plan &pl = plan(P[axis], precision, family_emax(pass, fam));
+    if (fam == 'q') pref = wide::zq_lines(pl.dev.L);  // fixed by the length
     int B = pref;
     while (B > 1 && !pass_fits(pass, fam, B, pa, pl)) B >>= 1;
     if (fam == 't')
@@ -757,7 +780,8 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
         ZArgs &a = pa.z;
         a.plan = pl.dev;
         a.B = c.B;
-        if (c.fam == 't') PS_CK(wide::launch_zt(a, P[1], stream));
+        if (c.fam == 'q') PS_CK(wide::launch_zq(a, P[1], static_cast<int *>(status.p), stream));
+        else if (c.fam == 't') PS_CK(wide::launch_zt(a, P[1], stream));
         else if (c.fam == 'w') PS_CK(wide::launch_z(a, P[1], stream));
         else if (c.fam == 'p') PS_CK(p2::launch_z(a, P[1], family_emax(2, 'p'), stream));
         else PS_CK(launch_z(prec, a, P[1], stream));
@@ -930,7 +954,7 @@ void Solver::autotune(int in_mask)
             if (pass >= 3 && !write_mask) continue;
             PassChoice best{0, 0};
             float best_ms = 0.f;
-            for (char fam : {'t', 'w', 'p', 'r'}) {
+            for (char fam : {'q', 't', 'w', 'p', 'r'}) {
                 if (!family_ok(pass, fam, pa)) continue;
                 const Plan &pl = plan(P[axis_of(pass)], precision, family_emax(pass, fam));
                 for (int B = 1; B <= 64; B *= 2) {
@@ -965,7 +989,7 @@ void Solver::autotune(int in_mask)
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    PS_CK(cudaStreamSynchronize(stream));
+    synchronize();
 }
 
 PassChoice Solver::current_choice(int pass, int in_mask)
@@ -1053,12 +1077,31 @@ void Solver::pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind)
             if (RB[c] && (pushed >> c & 1))
                 PS_CK(cudaMemcpyAsync(RB[c], filtered ? fr[c].p : fb[c].p, bytes, kind, stream));
     }
+    synchronize();
+}
+
+void Solver::synchronize()
+{
     PS_CK(cudaStreamSynchronize(stream));
+    check_status();
+}
+
+void Solver::check_status()
+{
+    if (!status.p) return;
+    int word = 0;
+    PS_CK(cudaMemcpyAsync(&word, status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    PS_CK(cudaStreamSynchronize(stream));
+    if (word) {
+        PS_CK(cudaMemsetAsync(status.p, 0, sizeof(int), stream));
+        PS_CK(cudaStreamSynchronize(stream));
+        throw Error(PS_ERR_TIMEOUT, "a pass kernel's wait for an asynchronous copy timed out; results are invalid");
+    }
 }
 
 size_t Solver::device_bytes() const
 {
-    size_t s = kern64.bytes + kern32.bytes + zeta64.bytes + zeta32.bytes;
+    size_t s = kern64.bytes + kern32.bytes + kernzf32.bytes + zeta64.bytes + zeta32.bytes;
     for (int c = 0; c < 3; ++c) s += work[c].bytes + fb[c].bytes + fa[c].bytes + fr[c].bytes;
     for (auto &kv : plans) s += kv.second->table.bytes;
     return s;

@@ -39,7 +39,8 @@ struct Plan {
 };
 
 // Kernel family and lines per CTA of one pass: 'r' run-time, 'p' length-
-// specialised, 'w' wide, 't' tensor-memory fused z.
+// specialised, 'w' wide, 't' tensor-memory fused z, 'q' fused z fed by tiled
+// bulk copies.
 struct PassChoice {
     char fam;
     int B;
@@ -66,14 +67,17 @@ struct Solver {
     int reg = 0;
     int Mx = 0, oy = 0, oz = 0;  // half-spectrum length and kernel octant extents
     int ldx = 0;                 // row pitch of the spectra work[c] (Mx rounded up to even)
+    int kzp = 0;                 // z pitch of kernzf32 (oz rounded up to a multiple of 4)
 
     int opt_grad = 0, opt_div = 0, opt_curl = 0, opt_reproject = 0;
     int precision = PREC_FP64;
 
     DevBuf kern64, kern32;  // octant K = G zeta / (Px Py Pz)
+    DevBuf kernzf32;        // FP32 K with z fastest, [oy][Mx][kzp] (unbounded z of 256..1024 points)
     DevBuf zeta64, zeta32;  // octant zeta / (Px Py Pz), built on first use
     DevBuf work[3];         // per-component spectra [Nz][Py][Mx], pass precision
     DevBuf fb[3], fa[3], fr[3];  // handle-owned fields: pushed B, solution A, returned B
+    DevBuf status;               // int: bit 0 set by a kernel whose bounded wait timed out
 
     int pushed = 0;    // component mask held in fb
     int produced = 0;  // component mask of fa from the last solve
@@ -110,6 +114,10 @@ struct Solver {
     void push(const double *const B[3], cudaMemcpyKind kind);
     void solve_internal();
     void pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind);
+    // After the stream has drained: throws PS_ERR_TIMEOUT (and clears the
+    // word) if a kernel reported a timed-out wait.
+    void check_status();
+    void synchronize();
 
     // Time every kernel family and line count that fits each pass of this
     // configuration (options + in_mask) on zero-filled scratch buffers and

@@ -98,6 +98,8 @@ struct ZArgs {
     const void *kern;  // octant K = G zeta / (Px Py Pz), [oz][oy][Mx]
     const void *zeta;  // octant zeta / (Px Py Pz) for OP_FILTER
     int oct_y;         // Py/2 + 1
+    const float *kern_zf;  // FP32 octant of K with z fastest, [oy][Mx][kzp] (null if not built)
+    int kzp;               // z pitch of kern_zf: Pz/2 + 1 rounded up to a multiple of 4
     int Px, Py, Pz;
     double kxc, kyc, kzc;  // 2 pi / (P dx) per axis
     int B;
@@ -178,6 +180,15 @@ constexpr int ZT_MAX_THREADS = 256;
 bool zt_supported(int prec, int L, int op, int nin, int nout);
 size_t smem_lines_zt(int L, int B, int ntw_entries);
 cudaError_t launch_zt(const ZArgs &a, int ny, cudaStream_t st);
+// fused z pass, a warp per column group, tiled bulk copies in and out
+// (ps_kernels_zq.cu): unbounded z (n_in = n_out = L / 2), L = 256..1024, a
+// persistent CTA per SM of ZQ_THREADS threads holding zq_lines(L) columns.
+// A wait that times out sets bit 0 of *status.
+constexpr int ZQ_THREADS = 256;
+bool zq_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_out);
+int zq_lines(int L);
+size_t smem_lines_zq(int L, int ntw_entries);
+cudaError_t launch_zq(const ZArgs &a, int ny, int *status, cudaStream_t st);
 }  // namespace wide
 
 // Kernel-build helpers (ps_greens.cu), all FP64.
@@ -204,5 +215,8 @@ struct KernelFillArgs {
 };
 cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st);
 cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t st);
+// FP32 copy of the octant [oz][oy][Mx] with z fastest: out[(y Mx + x) kzp + z],
+// zero for oz <= z < kzp (each column a whole number of 16-byte units).
+cudaError_t launch_kernel_zfast(const double *kern, float *out, int Mx, int oy, int oz, int kzp, cudaStream_t st);
 
 }  // namespace ps

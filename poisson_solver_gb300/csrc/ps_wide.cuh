@@ -35,15 +35,15 @@ template <int L> using WP = p2::Plan<L, 32>;
 
 __device__ __forceinline__ int skw(int n) { return n + (n >> 5); }
 
-__host__ __device__ inline int pitch_to(int L, int target)
+__host__ __device__ constexpr int pitch_to(int L, int target)
 {
     const int base = L + L / 32;
     return base + (((target - base) % 16) + 16) % 16;
 }
 // lines of a column pass (lane-fast over the B lines)
-__host__ __device__ inline int pitch_col(int L, int B) { return pitch_to(L, (16 / B) % 16); }
+__host__ __device__ constexpr int pitch_col(int L, int B) { return pitch_to(L, (16 / B) % 16); }
 // lines of a row pass (lane-fast along the line)
-__host__ __device__ inline int pitch_row(int L) { return pitch_to(L, (L / 32) % 16); }
+__host__ __device__ constexpr int pitch_row(int L) { return pitch_to(L, (L / 32) % 16); }
 
 // Stage S of the length-L plan: butterfly bf = t + u TPL reads positions
 // bf + r NBF and writes (q R + r) M + j, j = bf mod M, q = bf / M.
@@ -96,9 +96,17 @@ __device__ __forceinline__ void write_line(C *line, int t, const C (&v)[St<L, S>
         for (int r = 0; r < T::R; ++r) line[skw(T::out_pos(t, u, r))] = v[u][r];
 }
 
+// Barrier between the exchanges of a line: the CTA's, or (WARP) the warp's
+// when all threads of the line are one warp's.
+template <bool WARP> __device__ __forceinline__ void line_sync()
+{
+    if constexpr (WARP) __syncwarp();
+    else __syncthreads();
+}
+
 // Shared-memory stages from S up to (excluding) the last, in place: read,
 // barrier, write, barrier. nsets line sets cstride elements apart.
-template <int L, int S, bool INV, typename C>
+template <int L, int S, bool INV, bool WARP = false, typename C>
 __device__ __forceinline__ void middle_stages(C *line, const C *tws, int t, int nsets, int cstride)
 {
     if constexpr (S < WP<L>::NST - 1) {
@@ -107,11 +115,11 @@ __device__ __forceinline__ void middle_stages(C *line, const C *tws, int t, int 
             C v[T::U][T::R];
             read_line<L, S>(line + c * cstride, t, v);
             twiddle_dft<L, S, INV>(v, tws, t);
-            __syncthreads();
+            line_sync<WARP>();
             write_line<L, S>(line + c * cstride, t, v);
         }
-        __syncthreads();
-        middle_stages<L, S + 1, INV>(line, tws, t, nsets, cstride);
+        line_sync<WARP>();
+        middle_stages<L, S + 1, INV, WARP>(line, tws, t, nsets, cstride);
     }
 }
 

@@ -16,7 +16,7 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-FAMILIES = {"runtime", "p2", "wide", "tmem"}
+FAMILIES = {"runtime", "p2", "wide", "tmem", "tma"}
 
 
 def _solver(psg, nc, bc, precision, curl=True):

@@ -2,8 +2,10 @@
 wide kernels cover (Pz = 256 .. 2048), for every spectral operation.
 
 The families: the tensor-memory fused kernel (default), the shared-memory
-fused kernel (PS_KERNELS_Z=wide) and the length-specialised one
-(PS_KERNELS_Z=p2). Narrow x-y extents keep the oracle fast while the z
+fused kernel (PS_KERNELS_Z=wide), the length-specialised one
+(PS_KERNELS_Z=p2) and the warp-per-column kernel fed by tiled bulk copies
+(PS_KERNELS_Z=tma; unbounded z of 256..1024 points, the other shapes fall
+back to the default). Narrow x-y extents keep the oracle fast while the z
 columns reach the long lengths; the narrow x extent also leaves part of each
 CTA's columns inactive.
 """
@@ -36,7 +38,7 @@ OPS = [
     (dict(curl=True), (0, 1, 2)),
 ]
 
-FAMILIES = ["tmem", "wide", "p2"]
+FAMILIES = ["tmem", "wide", "p2", "tma"]
 
 
 def _fields(nc, comps, seed):
