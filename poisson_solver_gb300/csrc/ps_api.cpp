@@ -177,6 +177,7 @@ const char *ps_status_string(int status)
     case PS_ERR_CUDA: return "CUDA error";
     case PS_ERR_STATE: return "call out of order";
     case PS_ERR_UNSUPPORTED: return "unsupported";
+    case PS_ERR_TIMEOUT: return "a kernel's wait for an asynchronous copy timed out";
     default: return "unknown status";
     }
 }

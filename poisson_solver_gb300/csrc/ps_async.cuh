@@ -74,7 +74,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 
 // Wait for the completion of the barrier phase of the given parity; false
 // once WAIT_LIMIT_NS have passed (or 2^26 polls) without it.
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+static __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer();

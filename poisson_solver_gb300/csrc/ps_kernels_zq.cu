@@ -26,12 +26,11 @@
 //
 // Every mbarrier wait is bounded; on a timeout the warp stops, the CTA drains
 // its copies, frees its tensor memory and sets bit 0 of *status.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
-#include <mutex>
+#include <cstdlib>
+#include <cstring>
 
 #include "ps_async.cuh"
+#include "ps_tma_host.hpp"
 #include "ps_zt.cuh"
 
 namespace ps {
@@ -55,12 +54,14 @@ template <int L> struct Zq {
     static constexpr int CPW = 32 / TPL;                // columns a warp
     static constexpr int KP = (L / 2 + 1 + 3) & ~3;     // z pitch of the z-fastest kernel octant
     // byte offsets from the 1024-aligned base: in staging 0/1, out staging
-    // 0/1, lines, kernel columns, twiddles, 8 + 8 mbarriers, TMEM address slot
+    // 0/1, lines, kernel columns, twiddles, mbarriers (full, empty, out-full,
+    // out-empty pairs; one a warp for its kernel columns; the test probe),
+    // TMEM address slot
     static constexpr int IN0 = 0, OUT0 = 2 * STAGE_BYTES, LINES = 4 * STAGE_BYTES;
     static constexpr int GBUF = LINES + B * LDP * 8;
     static constexpr int TWO = GBUF + B * KP * 4;
     __host__ __device__ static constexpr int bars(int ntw) { return (TWO + ntw * 8 + 15) & ~15; }
-    __host__ __device__ static constexpr int bytes(int ntw) { return bars(ntw) + 16 * 8 + 16 + 1024; }  // + alignment slack
+    __host__ __device__ static constexpr int bytes(int ntw) { return bars(ntw) + 24 * 8 + 16 + 1024; }  // + alignment slack
     static_assert(G >= 1 && G * 8 == B, "whole 64-byte column groups");
     static_assert(GROUP_BYTES % 1024 == 0 && (BOXZ * 64) % 1024 == 0, "boxes keep the swizzle phase");
 };
@@ -77,7 +78,7 @@ __device__ __forceinline__ bool warp_ok(bool ok) { return __all_sync(0xffffffffu
 
 template <int L, int OP>
 __global__ void __launch_bounds__(ZQ_THREADS, 1)
-    k_zq(const ZArgs a, const __grid_constant__ ZqMaps maps, const int nxt, const int ntiles, int *status)
+    k_zq(const ZArgs a, const __grid_constant__ ZqMaps maps, const int nxt, const int ntiles, int *status, const int probe)
 {
     using C = float2;
     using PL = WP<L>;
@@ -94,7 +95,8 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
     C *TW = reinterpret_cast<C *>(base + Q::TWO);
     const int boff = Q::bars(PL::NTW);
     const uint32_t full0 = sb + boff, empty0 = full0 + 16, ofull0 = full0 + 32, oempty0 = full0 + 48;
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(base + boff + 128);
+    const uint32_t probe_bar = full0 + 128;  // never arrived at
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(base + boff + 192);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t gbar = full0 + 64 + 8 * warp;  // this warp's kernel-column barrier
@@ -106,6 +108,7 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
             mbar_init(oempty0 + 8 * s, 1);
         }
         for (int w = 0; w < ZQ_THREADS / 32; ++w) mbar_init(full0 + 64 + 8 * w, 1);
+        mbar_init(probe_bar, 1);
         fence_mbar_init();
     }
     if (warp == 0) {
@@ -160,7 +163,9 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
     };
     if (lane == 0 && nloc > 0) issue_g(0);
 
-    bool ok = true;
+    // test hook: a wait on a barrier nothing arrives at runs out, and the
+    // kernel winds down as after any timed-out wait
+    bool ok = !probe || mbar_wait(probe_bar, 0);
     int qo = 0;        // output boxes of this CTA so far
     int consumed = 0;  // loads thread 0 has waited for
     for (int i = 0; i < nloc && ok; ++i) {
@@ -258,70 +263,29 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
     }
 }
 
-// cuTensorMapEncodeTiled from the driver, looked up once.
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-    static std::once_flag once;
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    std::call_once(once, [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        cudaGetLastError();
-    });
-    return fn;
-}
-
-// Spectrum array [n_in z][Py y][ld x] of complex floats as floats: x extent
-// 2 Mx (the row pitch padding lies outside the tensor), boxes of 8 columns x
-// 1 row x boxz planes, 64-byte swizzle.
-bool encode_map(CUtensorMap *m, const void *p, const ZArgs &a, int boxz)
-{
-    const auto fn = encode_fn();
-    if (!fn || !p || (reinterpret_cast<uintptr_t>(p) & 15)) return false;
-    const long long rs = a.row_stride * 8, zs = a.axis_stride * 8;
-    if (rs % 16 || zs % 16) return false;
-    cuuint64_t dims[3] = {(cuuint64_t)(2 * a.Mx), (cuuint64_t)a.Py, (cuuint64_t)a.n_in};
-    cuuint64_t strides[2] = {(cuuint64_t)rs, (cuuint64_t)zs};
-    cuuint32_t box[3] = {16, 1, (cuuint32_t)boxz};
-    cuuint32_t estr[3] = {1, 1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(p), dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-int sm_count()
-{
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            n = 1;
-        cudaGetLastError();
-    }
-    return n;
-}
-
 template <int L, int OP> cudaError_t launch_zq_op(const ZArgs &a, int ny, int *status, cudaStream_t st)
 {
     using Q = Zq<L>;
     if (!a.kern_zf || a.kzp != Q::KP || (reinterpret_cast<uintptr_t>(a.kern_zf) & 15)) return cudaErrorInvalidValue;
     ZqMaps maps;
     memset(&maps, 0, sizeof(maps));
+    // [n_in z][Py y][ld x]: boxes of 8 columns x 1 y row x BOXZ planes
+    auto map = [&](CUtensorMap *m, const void *p) {
+        return tma::encode_spectrum(m, p, a.Mx, a.Py, a.n_in, a.row_stride * 8, a.axis_stride * 8, 1, Q::BOXZ);
+    };
     for (int c = 0; c < a.nin; ++c)
-        if (!encode_map(&maps.in[c], a.in[c], a, Q::BOXZ)) return cudaErrorInvalidValue;
+        if (!map(&maps.in[c], a.in[c])) return cudaErrorInvalidValue;
     for (int c = 0; c < a.nout; ++c)
-        if (a.out[c] && !encode_map(&maps.out[c], a.out[c], a, Q::BOXZ)) return cudaErrorInvalidValue;
+        if (a.out[c] && !map(&maps.out[c], a.out[c])) return cudaErrorInvalidValue;
     const int nxt = (a.Mx + Q::B - 1) / Q::B, ntiles = nxt * ny;
     if (ntiles <= 0) return cudaSuccess;
-    const int grid = ntiles < sm_count() ? ntiles : sm_count();
+    const int grid = ntiles < tma::sm_count() ? ntiles : tma::sm_count();
     const size_t sm = Q::bytes(a.plan.ntw);
     cudaError_t e = cudaFuncSetAttribute(k_zq<L, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_zq<L, OP><<<grid, ZQ_THREADS, sm, st>>>(a, maps, nxt, ntiles, status);
+    // PS_TEST_WAIT_TIMEOUT=1: every warp's first wait runs out (failure-path test)
+    const char *probe = getenv("PS_TEST_WAIT_TIMEOUT");
+    k_zq<L, OP><<<grid, ZQ_THREADS, sm, st>>>(a, maps, nxt, ntiles, status, probe && atoi(probe) == 1);
     return cudaGetLastError();
 }
 
@@ -342,7 +306,7 @@ bool zq_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_ou
 {
     return prec == PREC_FP32 && (L == 256 || L == 512 || L == 1024) && 2 * n_in == L && 2 * n_out == L &&
            (op == OP_NONE || op == OP_GRAD || op == OP_DIV || op == OP_CURL) && nin >= 1 && nin <= 3 && nout >= 1 &&
-           nout <= 3 && encode_fn() != nullptr;
+           nout <= 3 && tma::encode_fn() != nullptr;
 }
 
 int zq_lines(int L) { return L >= 32 ? ZQ_THREADS / (L / 32) : 0; }

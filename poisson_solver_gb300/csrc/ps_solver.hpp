@@ -77,7 +77,8 @@ struct Solver {
     DevBuf zeta64, zeta32;  // octant zeta / (Px Py Pz), built on first use
     DevBuf work[3];         // per-component spectra [Nz][Py][Mx], pass precision
     DevBuf fb[3], fa[3], fr[3];  // handle-owned fields: pushed B, solution A, returned B
-    DevBuf status;               // int: bit 0 set by a kernel whose bounded wait timed out
+    DevBuf status;               // int[4]: [0] bit 0 set by a kernel whose bounded wait timed out,
+                                 // [1] tile counter of the dynamically scheduled kernels
 
     int pushed = 0;    // component mask held in fb
     int produced = 0;  // component mask of fa from the last solve

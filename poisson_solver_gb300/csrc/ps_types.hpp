@@ -189,6 +189,15 @@ bool zq_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_ou
 int zq_lines(int L);
 size_t smem_lines_zq(int L, int ntw_entries);
 cudaError_t launch_zq(const ZArgs &a, int ny, int *status, cudaStream_t st);
+// y passes, a warp per column group, tiled bulk copies (ps_kernels_yq.cu):
+// unbounded y (forward n_in = L / 2, inverse n_out = L / 2), L = 256..1024, a
+// persistent CTA per SM holding yq_lines(L) columns, tiles handed out by a
+// counter at status[1] (reset by the launch). A wait that times out sets bit
+// 0 of status[0].
+bool yq_supported(int prec, int inverse, int L, int n_in, int n_out);
+int yq_lines(int L);
+size_t smem_lines_yq(int inverse, int L, int ntw_entries);
+cudaError_t launch_yq(int inverse, const ColArgs &a, int nplanes, int *status, cudaStream_t st);
 }  // namespace wide
 
 // Kernel-build helpers (ps_greens.cu), all FP64.

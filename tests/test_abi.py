@@ -42,6 +42,7 @@ def test_status_strings_and_null_handles(native):
     lib = _lib.load()
     assert lib.ps_status_string(0) == b"ok"
     assert lib.ps_status_string(3).startswith(b"pushed components")
+    assert b"timed out" in lib.ps_status_string(_lib.PS_ERR_TIMEOUT)
     assert lib.ps_solve3d(None) == _lib.PS_ERR_ARGUMENT
     assert lib.ps_destroy(None) == _lib.PS_OK
     assert lib.ps_setup2d(None, None, None, None, 0) == _lib.PS_ERR_UNSUPPORTED

@@ -1,11 +1,12 @@
 """Every FP32 z-pass kernel family against the oracle, at the z lengths the
 wide kernels cover (Pz = 256 .. 2048), for every spectral operation.
 
-The families: the tensor-memory fused kernel (default), the shared-memory
-fused kernel (PS_KERNELS_Z=wide), the length-specialised one
-(PS_KERNELS_Z=p2) and the warp-per-column kernel fed by tiled bulk copies
-(PS_KERNELS_Z=tma; unbounded z of 256..1024 points, the other shapes fall
-back to the default). Narrow x-y extents keep the oracle fast while the z
+The families: the warp-per-column kernel fed by tiled bulk copies
+(PS_KERNELS_Z=tma, the default on unbounded z of 256..1024 points), the
+tensor-memory fused kernel (PS_KERNELS_Z=tmem, the default elsewhere), the
+shared-memory fused kernel (PS_KERNELS_Z=wide) and the length-specialised
+one (PS_KERNELS_Z=p2). A family that does not cover a shape falls back to
+the default. Narrow x-y extents keep the oracle fast while the z
 columns reach the long lengths; the narrow x extent also leaves part of each
 CTA's columns inactive.
 """
@@ -88,7 +89,8 @@ def test_tmem_z_lines_per_cta(native, oracle, monkeypatch, lines):
 
 
 # tall y extents: the wide y kernels at P_y = 256 .. 1024, unbounded (the
-# zero-padded half pruned) and periodic
+# zero-padded half pruned) and periodic, and the bulk-copy y kernels
+# (PS_KERNELS_Y=tma: unbounded only, the periodic shapes fall back)
 Y_SHAPES = [
     ((6, 128, 8), (0, 0, 0)),
     ((4, 256, 6), (0, 0, 0)),
@@ -98,9 +100,11 @@ Y_SHAPES = [
 ]
 
 
+@pytest.mark.parametrize("family", ["wide", "tma"])
 @pytest.mark.parametrize("yi", range(len(Y_SHAPES)))
-def test_fp32_wide_y_vs_oracle(native, oracle, yi):
+def test_fp32_y_family_vs_oracle(native, oracle, monkeypatch, yi, family):
     nc, bc = Y_SHAPES[yi]
+    monkeypatch.setenv("PS_KERNELS_Y", family)
     dx = (2.0 / nc[0], 1.5 / nc[1], 2.5 / nc[2])
     B = _fields(nc, (0, 1, 2), 500 + yi)
     ref, _ = oracle.solve3d(nc, bc, dx, B, 2, curl=True)
