@@ -136,5 +136,10 @@ __device__ __forceinline__ int swizzle64(int row, int c8)
     return off ^ (((off >> 7) & 3) << 4);
 }
 
+// For rows congruent to t modulo 8 the swizzle term depends on t only:
+// swizzle64(row, c8) = row * 64 + swizzle64_col(t, c8), a per-thread constant
+// plus an offset the compiler folds into the access.
+__device__ __forceinline__ int swizzle64_col(int t, int c8) { return (c8 * 8) ^ (((t >> 1) & 3) << 4); }
+
 }  // namespace async
 }  // namespace ps

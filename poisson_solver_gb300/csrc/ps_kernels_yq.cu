@@ -87,6 +87,10 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
     using TL = St<L, LAST>;
     static_assert(T0::U == 1 && T0::R == 32, "one radix-32 butterfly a thread in the first stage");
     static_assert(PL::NST == 2, "two stages: one exchange");
+    // staged rows t + r NBF (first stage) and out_pos(t, u, r) = r M + t + u TPL
+    // (last stage) are congruent to t modulo 8: one swizzle term a thread
+    static_assert(T0::NBF % 8 == 0 && TL::M % 8 == 0 && TL::TPL % 8 == 0 && TL::U * TL::TPL <= TL::M,
+                  "staged rows share t's swizzle term");
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -181,7 +185,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
     } else {
         const int b = tid / Q::TPL, t = tid % Q::TPL;
         C *line = reinterpret_cast<C *>(base + Q::LINES) + b * Q::LDP;  // forward only
-        const int c8 = b & 7;
+        const int c8 = b & 7, sw = swizzle64_col(t, c8);
         int q = 0;
         for (;; ++q) {
             const int s = q % Q::NIN;
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
                 // rows >= L/2 are the zero padding
 #pragma unroll
                 for (int r = 0; r < 16; ++r)
-                    v0[0][r] = *reinterpret_cast<const C *>(stg + swizzle64(T0::in_pos(t, 0, r), c8));
+                    v0[0][r] = *reinterpret_cast<const C *>(stg + sw + T0::in_pos(t, 0, r) * 64);
                 mbar_arrive(empty0 + 8 * s);
                 dft32_half<false>(v0[0]);
                 write_line<L, 0>(line, t, v0);
@@ -210,7 +214,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
                 C v0[1][32];
 #pragma unroll
                 for (int r = 0; r < 32; ++r)
-                    v0[0][r] = *reinterpret_cast<const C *>(stg + swizzle64(T0::in_pos(t, 0, r), c8));
+                    v0[0][r] = *reinterpret_cast<const C *>(stg + sw + T0::in_pos(t, 0, r) * 64);
                 twiddle_dft<L, 0, true>(v0, TW, t);
                 __syncwarp();  // the column's lanes have read its rows
 #pragma unroll
@@ -236,7 +240,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
             for (int u = 0; u < TL::U; ++u)
 #pragma unroll
                 for (int r = 0; r < RW; ++r)
-                    *reinterpret_cast<C *>(ostg + swizzle64(TL::out_pos(t, u, r), c8)) = v[u][r];
+                    *reinterpret_cast<C *>(ostg + sw + TL::out_pos(t, u, r) * 64) = v[u][r];
             if (tid == 0) otile[so] = j;
             fence_proxy_async_smem();
             mbar_arrive(ofull0 + 8 * so);

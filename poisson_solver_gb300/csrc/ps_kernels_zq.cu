@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
     using TL = St<L, LAST>;
     static_assert(T0::U == 1 && T0::R == 32, "one radix-32 butterfly a thread in the first stage");
     static_assert(TL::U * TL::R == 32, "32 values per thread");
+    static_assert(T0::NBF % 8 == 0, "staged rows t + r NBF share t's swizzle term");
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
 
     const int b = tid / Q::TPL, t = tid % Q::TPL;  // column of the CTA, thread of the column
     C *line = reinterpret_cast<C *>(base + Q::LINES) + b * Q::LDP;
-    const int goff = (b >> 3) * Q::GROUP_BYTES, c8 = b & 7;
+    const int goff = (b >> 3) * Q::GROUP_BYTES + swizzle64_col(t, b & 7);
     const int nin = a.nin;
     const int nloc = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
     const int nq = nloc * nin;  // component loads of this CTA
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
             const unsigned char *stg = base + Q::IN0 + s * Q::STAGE_BYTES + goff;
             C v0[1][32];
 #pragma unroll
-            for (int r = 0; r < 16; ++r) v0[0][r] = *reinterpret_cast<const C *>(stg + swizzle64(T0::in_pos(t, 0, r), c8));
+            for (int r = 0; r < 16; ++r) v0[0][r] = *reinterpret_cast<const C *>(stg + T0::in_pos(t, 0, r) * 64);
             mbar_arrive(empty0 + 8 * s);
             dft32_half<false>(v0[0]);
             write_line<L, 0>(line, t, v0);
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
             unsigned char *ostg = base + Q::OUT0 + so * Q::STAGE_BYTES + goff;
             // rows < L / 2 (the cropped half is dropped)
 #pragma unroll
-            for (int r = 0; r < 16; ++r) *reinterpret_cast<C *>(ostg + swizzle64(T0::in_pos(t, 0, r), c8)) = v0[0][r];
+            for (int r = 0; r < 16; ++r) *reinterpret_cast<C *>(ostg + T0::in_pos(t, 0, r) * 64) = v0[0][r];
             fence_proxy_async_smem();
             mbar_arrive(ofull0 + 8 * so);
             if (tid == 0) {
