@@ -645,11 +645,13 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
 // Families: 'r' run-time kernels (any length, FP64 and FP32), 'p' length-
 // specialised FP32 kernels (powers of two 64..2048), 'w' wide FP32 kernels
 // (256..2048; for z the shared-memory fused kernel), 't' the fused z kernel
-// with tensor-memory staging (z only), 'q' a warp per column group fed by
-// tiled bulk copies (y and z, unbounded axes of 256..1024 points).
-// Defaults, measured at 512^3 (FP32 curl): x forward p2 with 2 lines a CTA
-// (2.3 against 3.4 ms for wide), x inverse p2 with 4; y and z bulk-copy
-// ('q') where it applies, else y wide with 8 and z tensor-memory with 8.
+// with tensor-memory staging (z only), 'q' a warp per line or column group
+// (x: L = 256..1024; y and z: unbounded axes of 256..1024 points, fed by
+// tiled bulk copies).
+// Defaults, measured at 512^3 (FP32 curl): the 'q' kernels where they apply
+// (x: a warp per line; y, z: bulk copies), else x forward p2 with 2 lines a
+// CTA (2.3 against 3.4 ms for wide), x inverse p2 with 4, y wide with 8 and
+// z tensor-memory with 8.
 // PS_KERNELS, PS_KERNELS_X/_Y/_Z (= tma, tmem, wide, p2 or runtime),
 // PS_LINES_X/_XI/_Y/_Z and PS_Z_EM override the defaults; ps_autotune
 // replaces them for one configuration.
@@ -665,6 +667,8 @@ bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
     case 'w': return wide::supported(prec, L) && (pass != 2 || p2::supports_op(op));
     case 't': return pass == 2 && wide::zt_supported(prec, L, op, pa.z.nin, pa.z.nout);
     case 'q':
+        if (pass == 0) return wide::xq_supported(prec, 0, L, pa.x.n_in, pa.x.mirror);
+        if (pass == 4) return wide::xq_supported(prec, 1, L, pa.xi.n_out, 0);
         if (pass == 1 || pass == 3) {
             const ColArgs &c = pass == 1 ? pa.y : pa.yi;
             return wide::yq_supported(prec, pass == 3, L, c.n_in, c.n_out);
@@ -700,7 +704,7 @@ size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Pl
         return smem_z(prec, pl.dev, B, nbuf);
     }
     const bool x = pass == 0 || pass == 4;
-    if (fam == 'q') return x ? 0 : wide::smem_lines_yq(pass == 3, L, ntw);
+    if (fam == 'q') return x ? wide::smem_lines_xq(L, ntw) : wide::smem_lines_yq(pass == 3, L, ntw);
     if (fam == 'w') return wide::smem_lines(L, B, 1, ntw, !x);
     if (fam == 'p') return p2::smem_lines(prec, L, B, 1, ntw);
     return x ? smem_x(prec, pl.dev, B) : smem_col(prec, pl.dev, B);
@@ -718,7 +722,7 @@ bool Solver::pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan
     if ((pass == 0 || pass == 4) && B > MAX_LINES) return false;
     if (pass == 2 && fam == 't' && nt % 32 != 0) return false;           // whole warps
     if (fam == 'q')  // fixed lines per length; no static shared memory
-        return B == (pass == 2 ? wide::zq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L)) &&
+        return B == (pass == 2 ? wide::zq_lines(pl.dev.L) : axis_of(pass) == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L)) &&
                pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
     return nt <= max_threads && pass_smem(pass, fam, B, pa, pl) <= (size_t)limit;
 }
@@ -737,8 +741,9 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
         fam = family_ok(pass, 'w', pa) ? 'w' : family_ok(pass, 'p', pa) ? 'p' : 'r';
     else if (f && strcmp(f, "tmem") == 0 && family_ok(pass, 't', pa)) fam = 't';
     else if (f && strcmp(f, "tma") == 0 && family_ok(pass, 'q', pa)) fam = 'q';
-    // 'q' at 512^3: z 6.0 against 7.7 ms for 't'; y 1.67 / 2.01 against 2.51 / 2.31 ms for 'w'
-    else if (axis > 0 && family_ok(pass, 'q', pa)) fam = 'q';
+    // 'q' at 512^3: z 6.0 against 7.7 ms for 't'; y 1.67 / 2.01 against 2.51 / 2.31 ms for 'w';
+    // x 1.25 / 1.20 against 1.33 / 1.45 ms for 'p'
+    else if (family_ok(pass, 'q', pa)) fam = 'q';
     else if (pass == 2 && family_ok(pass, 't', pa)) fam = 't';
     else if (axis > 0 && family_ok(pass, 'w', pa)) fam = 'w';
     else fam = family_ok(pass, 'p', pa) ? 'p' : 'r';
@@ -753,7 +758,8 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
         if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) pref = want;
     }
     const Plan &pl = plan(P[axis], precision, family_emax(pass, fam));
-    if (fam == 'q') pref = pass == 2 ? wide::zq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L);  // fixed by the length
+    if (fam == 'q')  // fixed by the length
+        pref = pass == 2 ? wide::zq_lines(pl.dev.L) : axis == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L);
     int B = pref;
     while (B > 1 && !pass_fits(pass, fam, B, pa, pl)) B >>= 1;
     if (fam == 't')
@@ -771,7 +777,8 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
         XFwdArgs &a = pa.x;
         a.plan = pl.dev;
         a.B = c.B;
-        if (c.fam == 'w') PS_CK(wide::launch_xfwd(a, stream));
+        if (c.fam == 'q') PS_CK(wide::launch_xfq(a, stream));
+        else if (c.fam == 'w') PS_CK(wide::launch_xfwd(a, stream));
         else if (c.fam == 'p') PS_CK(p2::launch_xfwd(a, stream));
         else PS_CK(launch_xfwd(prec, a, stream));
         break;
@@ -803,7 +810,8 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
         XInvArgs &a = pa.xi;
         a.plan = pl.dev;
         a.B = c.B;
-        if (c.fam == 'w') PS_CK(wide::launch_xinv(a, stream));
+        if (c.fam == 'q') PS_CK(wide::launch_xiq(a, stream));
+        else if (c.fam == 'w') PS_CK(wide::launch_xinv(a, stream));
         else if (c.fam == 'p') PS_CK(p2::launch_xinv(a, stream));
         else PS_CK(launch_xinv(prec, a, stream));
         break;

@@ -198,6 +198,13 @@ bool yq_supported(int prec, int inverse, int L, int n_in, int n_out);
 int yq_lines(int L);
 size_t smem_lines_yq(int inverse, int L, int ntw_entries);
 cudaError_t launch_yq(int inverse, const ColArgs &a, int nplanes, int *status, cudaStream_t st);
+// x passes, a warp per line group (ps_kernels_xq.cu): L = 256..1024, not
+// mirrored; xq_lines(L) lines a CTA. n = n_in (forward) or n_out (inverse).
+bool xq_supported(int prec, int inverse, int L, int n, int mirror);
+int xq_lines(int L);
+size_t smem_lines_xq(int L, int ntw_entries);
+cudaError_t launch_xfq(const XFwdArgs &a, cudaStream_t st);
+cudaError_t launch_xiq(const XInvArgs &a, cudaStream_t st);
 }  // namespace wide
 
 // Kernel-build helpers (ps_greens.cu), all FP64.

@@ -112,8 +112,10 @@ def test_fp32_y_family_vs_oracle(native, oracle, monkeypatch, yi, family):
     assert rel_l2(got, ref) < FP32_TOL
 
 
-# long x extents: the length-specialised x kernels at P_x = 256 .. 1024,
-# unbounded (the zero-padded half pruned) and periodic
+# long x extents: the length-specialised x kernels (PS_KERNELS_X=p2) and the
+# warp-per-line x kernels (PS_KERNELS_X=tma) at P_x = 256 .. 1024, unbounded
+# (the zero-padded half pruned) and periodic; odd row counts leave a lone
+# last row
 X_SHAPES = [
     ((128, 6, 8), (0, 0, 0)),
     ((256, 5, 4), (0, 0, 0)),
@@ -123,9 +125,11 @@ X_SHAPES = [
 ]
 
 
+@pytest.mark.parametrize("family", ["p2", "tma"])
 @pytest.mark.parametrize("xi", range(len(X_SHAPES)))
-def test_fp32_p2_x_vs_oracle(native, oracle, xi):
+def test_fp32_x_family_vs_oracle(native, oracle, monkeypatch, xi, family):
     nc, bc = X_SHAPES[xi]
+    monkeypatch.setenv("PS_KERNELS_X", family)
     dx = (2.0 / nc[0], 1.5 / nc[1], 2.5 / nc[2])
     rng = np.random.default_rng(600 + xi)
     B = [rng.standard_normal((nc[2], nc[1], nc[0])) for _ in range(3)]
