@@ -1,6 +1,7 @@
 // y passes, one warp per column group, fed by tiled bulk copies (FP32;
-// L = 256, 512, 1024 on an unbounded y axis: the forward pass reads L/2
-// rows and writes L, the inverse reads L and writes L/2).
+// L = 256, 512, 1024; on an unbounded y axis the forward pass reads L/2
+// rows and writes L, the inverse reads L and writes L/2; on a periodic one
+// both read and write L).
 //
 // A tile is one z plane x 8 (32 / TPL) columns x one component. A column's
 // L/32 threads are consecutive lanes of one warp, so the exchange between the
@@ -46,12 +47,15 @@ constexpr int YQ_COMPUTE = 256;                // compute threads (8 warps)
 constexpr int YQ_THREADS = YQ_COMPUTE + 64;     // + load warp + store warp
 constexpr int LOAD_WARP = YQ_COMPUTE / 32, STORE_WARP = LOAD_WARP + 1;
 
-template <int L, bool INV> struct Yq {
+// HALF: the y axis is unbounded (forward n_in = L/2, inverse n_out = L/2);
+// else periodic (n_in = n_out = L).
+template <int L, bool INV, bool HALF> struct Yq {
     static constexpr int TPL = L / 32;          // threads a column
     static constexpr int B = YQ_COMPUTE / TPL;  // columns a CTA
     static constexpr int G = B / 8;             // 64-byte column groups
-    static constexpr int IN_ROWS = INV ? L : L / 2, OUT_ROWS = INV ? L / 2 : L;
-    static constexpr int NIN = 2, NOUT = INV ? 2 : 1;  // staging buffers
+    static constexpr int IN_ROWS = (HALF && !INV) ? L / 2 : L, OUT_ROWS = (HALF && INV) ? L / 2 : L;
+    static constexpr bool XIN = IN_ROWS == L;     // exchange inside the input staging (no line buffers)
+    static constexpr int NIN = 2, NOUT = OUT_ROWS == L ? 1 : 2;  // staging buffers
     static constexpr int NBI = IN_ROWS > 256 ? IN_ROWS / 256 : 1, BI = IN_ROWS / NBI;
     static constexpr int NBO = OUT_ROWS > 256 ? OUT_ROWS / 256 : 1, BO = OUT_ROWS / NBO;
     static constexpr int IN_GROUP = IN_ROWS * 64, OUT_GROUP = OUT_ROWS * 64;
@@ -59,7 +63,7 @@ template <int L, bool INV> struct Yq {
     static constexpr int LDP = pitch_row(L);
     // byte offsets from the 1024-aligned base
     static constexpr int IN0 = 0, OUT0 = NIN * IN_BYTES, LINES = OUT0 + NOUT * OUT_BYTES;
-    static constexpr int TWO = LINES + (INV ? 0 : B * LDP * 8);  // the inverse has no line buffers
+    static constexpr int TWO = LINES + (XIN ? 0 : B * LDP * 8);
     __host__ __device__ static constexpr int bars(int ntw) { return (TWO + ntw * 8 + 15) & ~15; }
     __host__ __device__ static constexpr int bytes(int ntw) { return bars(ntw) + 8 * 8 + 16 + 1024; }  // + alignment slack
     static_assert(G >= 1 && G * 8 == B, "whole 64-byte column groups");
@@ -74,14 +78,14 @@ struct YqMaps {
 
 __device__ __forceinline__ bool warp_ok(bool ok) { return __all_sync(0xffffffffu, ok); }
 
-template <int L, bool INV>
+template <int L, bool INV, bool HALF>
 __global__ void __launch_bounds__(YQ_THREADS, 1)
     k_yq(const ColArgs a, const __grid_constant__ YqMaps maps, const int nxt, const int nplanes, const int ntiles,
          int *status)
 {
     using C = float2;
     using PL = WP<L>;
-    using Q = Yq<L, INV>;
+    using Q = Yq<L, INV, HALF>;
     constexpr int LAST = PL::NST - 1;
     using T0 = St<L, 0>;
     using TL = St<L, LAST>;
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
             if (j < 0) break;
             unsigned char *stg = base + Q::IN0 + s * Q::IN_BYTES + (b >> 3) * Q::IN_GROUP;
             C v[TL::U][TL::R];
-            if constexpr (!INV) {
+            if constexpr (!Q::XIN) {
                 C v0[1][32];
                 // rows >= L/2 are the zero padding
 #pragma unroll
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
 #pragma unroll
                 for (int r = 0; r < 32; ++r)
                     v0[0][r] = *reinterpret_cast<const C *>(stg + sw + T0::in_pos(t, 0, r) * 64);
-                twiddle_dft<L, 0, true>(v0, TW, t);
+                twiddle_dft<L, 0, INV>(v0, TW, t);
                 __syncwarp();  // the column's lanes have read its rows
 #pragma unroll
                 for (int r = 0; r < 32; ++r) *slot(T0::out_pos(t, 0, r)) = v0[0][r];
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
 #pragma unroll
                     for (int r = 0; r < TL::R; ++r) v[u][r] = *slot(TL::in_pos(t, u, r));
                 mbar_arrive(empty0 + 8 * s);
-                twiddle_dft<L, LAST, true>(v, TW, t);
+                twiddle_dft<L, LAST, INV>(v, TW, t);
             }
 
             const int so = q % Q::NOUT;
@@ -234,8 +238,8 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
                 if (!ok) break;
             }
             unsigned char *ostg = base + Q::OUT0 + so * Q::OUT_BYTES + (b >> 3) * Q::OUT_GROUP;
-            // inverse: out_pos = r M + bf with bf < M = L / R, so r < R/2 is the kept half
-            constexpr int RW = INV ? TL::R / 2 : TL::R;
+            // unbounded inverse: out_pos = r M + bf with bf < M = L / R, so r < R/2 is the kept half
+            constexpr int RW = Q::OUT_ROWS < L ? TL::R / 2 : TL::R;
 #pragma unroll
             for (int u = 0; u < TL::U; ++u)
 #pragma unroll
@@ -257,9 +261,9 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
     if (!ok && lane == 0) atomicOr(status, 1);
 }
 
-template <int L, bool INV> cudaError_t launch_yq_t(const ColArgs &a, int nplanes, int *status, cudaStream_t st)
+template <int L, bool INV, bool HALF> cudaError_t launch_yq_t(const ColArgs &a, int nplanes, int *status, cudaStream_t st)
 {
-    using Q = Yq<L, INV>;
+    using Q = Yq<L, INV, HALF>;
     YqMaps maps;
     memset(&maps, 0, sizeof(maps));
     for (int c = 0; c < a.ncomp; ++c) {
@@ -273,34 +277,51 @@ template <int L, bool INV> cudaError_t launch_yq_t(const ColArgs &a, int nplanes
     if (ntiles <= 0) return cudaSuccess;
     const int grid = ntiles < tma::sm_count() ? ntiles : tma::sm_count();
     const size_t sm = Q::bytes(a.plan.ntw);
-    cudaError_t e = cudaFuncSetAttribute(k_yq<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_yq<L, INV, HALF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(status + 1, 0, sizeof(int), st)) != cudaSuccess) return e;  // tile counter
-    k_yq<L, INV><<<grid, YQ_THREADS, sm, st>>>(a, maps, nxt, nplanes, ntiles, status);
+    k_yq<L, INV, HALF><<<grid, YQ_THREADS, sm, st>>>(a, maps, nxt, nplanes, ntiles, status);
     return cudaGetLastError();
 }
 
-template <int L> size_t yq_bytes(int inverse, int ntw)
+template <int L> size_t yq_bytes(int inverse, int half, int ntw)
 {
-    return inverse ? Yq<L, true>::bytes(ntw) : Yq<L, false>::bytes(ntw);
+    if (half) return inverse ? Yq<L, true, true>::bytes(ntw) : Yq<L, false, true>::bytes(ntw);
+    return inverse ? Yq<L, true, false>::bytes(ntw) : Yq<L, false, false>::bytes(ntw);
+}
+
+template <int L> cudaError_t launch_yq_len(int inverse, int half, const ColArgs &a, int nplanes, int *status, cudaStream_t st)
+{
+    if (half) return inverse ? launch_yq_t<L, true, true>(a, nplanes, status, st) : launch_yq_t<L, false, true>(a, nplanes, status, st);
+    return inverse ? launch_yq_t<L, true, false>(a, nplanes, status, st) : launch_yq_t<L, false, false>(a, nplanes, status, st);
+}
+
+// unbounded (the zero-padded half pruned) or periodic
+int yq_half(int inverse, int L, int n_in, int n_out)
+{
+    if (inverse ? (n_in == L && 2 * n_out == L) : (2 * n_in == L && n_out == L)) return 1;
+    if (n_in == L && n_out == L) return 0;
+    return -1;
 }
 
 }  // namespace
 
 bool yq_supported(int prec, int inverse, int L, int n_in, int n_out)
 {
-    const bool half = inverse ? (n_in == L && 2 * n_out == L) : (2 * n_in == L && n_out == L);
-    return prec == PREC_FP32 && (L == 256 || L == 512 || L == 1024) && half && tma::encode_fn() != nullptr;
+    return prec == PREC_FP32 && (L == 256 || L == 512 || L == 1024) && yq_half(inverse, L, n_in, n_out) >= 0 &&
+           tma::encode_fn() != nullptr;
 }
 
 int yq_lines(int L) { return L >= 32 ? YQ_COMPUTE / (L / 32) : 0; }
 
-size_t smem_lines_yq(int inverse, int L, int ntw_entries)
+size_t smem_lines_yq(int inverse, int L, int n_in, int n_out, int ntw_entries)
 {
+    const int half = yq_half(inverse, L, n_in, n_out);
+    if (half < 0) return 0;
     switch (L) {
-    case 256: return yq_bytes<256>(inverse, ntw_entries);
-    case 512: return yq_bytes<512>(inverse, ntw_entries);
-    case 1024: return yq_bytes<1024>(inverse, ntw_entries);
+    case 256: return yq_bytes<256>(inverse, half, ntw_entries);
+    case 512: return yq_bytes<512>(inverse, half, ntw_entries);
+    case 1024: return yq_bytes<1024>(inverse, half, ntw_entries);
     default: return 0;
     }
 }
@@ -310,11 +331,11 @@ cudaError_t launch_yq(int inverse, const ColArgs &a, int nplanes, int *status, c
     if (!status || a.B != yq_lines(a.L) || a.ncomp < 1 || a.ncomp > 3 ||
         !yq_supported(PREC_FP32, inverse, a.L, a.n_in, a.n_out))
         return cudaErrorInvalidConfiguration;
+    const int half = yq_half(inverse, a.L, a.n_in, a.n_out);
     switch (a.L) {
-    case 256: return inverse ? launch_yq_t<256, true>(a, nplanes, status, st) : launch_yq_t<256, false>(a, nplanes, status, st);
-    case 512: return inverse ? launch_yq_t<512, true>(a, nplanes, status, st) : launch_yq_t<512, false>(a, nplanes, status, st);
-    case 1024:
-        return inverse ? launch_yq_t<1024, true>(a, nplanes, status, st) : launch_yq_t<1024, false>(a, nplanes, status, st);
+    case 256: return launch_yq_len<256>(inverse, half, a, nplanes, status, st);
+    case 512: return launch_yq_len<512>(inverse, half, a, nplanes, status, st);
+    case 1024: return launch_yq_len<1024>(inverse, half, a, nplanes, status, st);
     default: return cudaErrorInvalidValue;
     }
 }

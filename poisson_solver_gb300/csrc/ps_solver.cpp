@@ -646,8 +646,8 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
 // specialised FP32 kernels (powers of two 64..2048), 'w' wide FP32 kernels
 // (256..2048; for z the shared-memory fused kernel), 't' the fused z kernel
 // with tensor-memory staging (z only), 'q' a warp per line or column group
-// (x: L = 256..1024; y and z: unbounded axes of 256..1024 points, fed by
-// tiled bulk copies).
+// (x and y: L = 256..1024; z: unbounded axes of 256..1024 points; y and z
+// fed by tiled bulk copies).
 // Defaults, measured at 512^3 (FP32 curl): the 'q' kernels where they apply
 // (x: a warp per line; y, z: bulk copies), else x forward p2 with 2 lines a
 // CTA (2.3 against 3.4 ms for wide), x inverse p2 with 4, y wide with 8 and
@@ -704,7 +704,11 @@ size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Pl
         return smem_z(prec, pl.dev, B, nbuf);
     }
     const bool x = pass == 0 || pass == 4;
-    if (fam == 'q') return x ? wide::smem_lines_xq(L, ntw) : wide::smem_lines_yq(pass == 3, L, ntw);
+    if (fam == 'q') {
+        if (x) return wide::smem_lines_xq(L, ntw);
+        const ColArgs &c = pass == 1 ? pa.y : pa.yi;
+        return wide::smem_lines_yq(pass == 3, L, c.n_in, c.n_out, ntw);
+    }
     if (fam == 'w') return wide::smem_lines(L, B, 1, ntw, !x);
     if (fam == 'p') return p2::smem_lines(prec, L, B, 1, ntw);
     return x ? smem_x(prec, pl.dev, B) : smem_col(prec, pl.dev, B);

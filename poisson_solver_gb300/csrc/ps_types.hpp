@@ -190,13 +190,14 @@ int zq_lines(int L);
 size_t smem_lines_zq(int L, int ntw_entries);
 cudaError_t launch_zq(const ZArgs &a, int ny, int *status, cudaStream_t st);
 // y passes, a warp per column group, tiled bulk copies (ps_kernels_yq.cu):
-// unbounded y (forward n_in = L / 2, inverse n_out = L / 2), L = 256..1024, a
+// unbounded y (forward n_in = L / 2, inverse n_out = L / 2) or periodic y
+// (n_in = n_out = L), L = 256..1024, a
 // persistent CTA per SM holding yq_lines(L) columns, tiles handed out by a
 // counter at status[1] (reset by the launch). A wait that times out sets bit
 // 0 of status[0].
 bool yq_supported(int prec, int inverse, int L, int n_in, int n_out);
 int yq_lines(int L);
-size_t smem_lines_yq(int inverse, int L, int ntw_entries);
+size_t smem_lines_yq(int inverse, int L, int n_in, int n_out, int ntw_entries);
 cudaError_t launch_yq(int inverse, const ColArgs &a, int nplanes, int *status, cudaStream_t st);
 // x passes, a warp per line group (ps_kernels_xq.cu): L = 256..1024, not
 // mirrored; xq_lines(L) lines a CTA. n = n_in (forward) or n_out (inverse).
