@@ -13,13 +13,15 @@
 //   * the store warp waits until every compute thread has written a tile's
 //     outputs into the output staging, starts the tiled stores and releases
 //     the staging once the copies have read it.
-// Inputs are double-buffered. The forward pass exchanges between its stages
-// through padded line buffers and single-buffers its (full-size) output; the
-// inverse pass exchanges inside its own input staging, whose column of L
-// rows is free once the column's first stage has read it (positions p held
-// at row p ^ ((p >> 5) & 7), two-way bank conflicts), which leaves room to
-// double-buffer the full-size input that the loads must keep ahead of. Either
-// way the shared memory of one CTA per SM is full. The CTAs are persistent, one per SM, and
+// Inputs are double-buffered. The unbounded forward pass exchanges between
+// its stages through padded line buffers and single-buffers its (full-size)
+// output. Where the input holds all L rows (the unbounded inverse, both
+// periodic passes) the pass exchanges inside its own input staging, whose
+// column of L rows is free once the column's first stage has read them
+// (positions p held at row p ^ ((p >> 5) & 7), two-way bank conflicts),
+// which leaves room to double-buffer the full-size input that the loads must
+// keep ahead of. Either way the shared memory of one CTA per SM is full.
+// The CTAs are persistent, one per SM, and
 // take tiles from a global counter in order: the CTAs then work on
 // neighbouring tiles at any time (the same y rows of adjacent column groups),
 // where a fixed round-robin assignment drifts apart over hundreds of tiles
