@@ -44,6 +44,38 @@ template <bool INV, typename C> __device__ __forceinline__ C rot(C a)
 {
     return INV ? C{-a.y, a.x} : C{a.y, -a.x};
 }
+// a + rot(b) and a - rot(b), the rotation folded into the additions
+template <bool INV, typename C> __device__ __forceinline__ C addrot(C a, C b)
+{
+    return INV ? C{a.x - b.y, a.y + b.x} : C{a.x + b.y, a.y - b.x};
+}
+template <bool INV, typename C> __device__ __forceinline__ C subrot(C a, C b)
+{
+    return INV ? C{a.x + b.y, a.y - b.x} : C{a.x - b.y, a.y + b.x};
+}
+
+// FP32 complex addition and subtraction as one packed instruction each
+// (add/sub.rn.f32x2, sm_100 and later): both lanes round to nearest like
+// two scalar operations, so results are unchanged; the butterflies of the
+// FFT stages issue half the instructions.
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
 // multiply by w = (c, -s) forward or (c, s) inverse, i.e. e^{-+ i theta}
 template <bool INV, typename C, typename S> __device__ __forceinline__ C crot(C a, S c, S s)
 {
@@ -62,11 +94,22 @@ template <bool INV, typename C> __device__ __forceinline__ void dft2(C &a, C &b)
 
 template <bool INV, typename C> __device__ __forceinline__ void dft4(C &x0, C &x1, C &x2, C &x3)
 {
-    C t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = rot<INV>(csub(x1, x3));
+    const C t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), d = csub(x1, x3);
     x0 = cadd(t0, t2);
     x2 = csub(t0, t2);
-    x1 = cadd(t1, t3);
-    x3 = csub(t1, t3);
+    x1 = addrot<INV>(t1, d);
+    x3 = subrot<INV>(t1, d);
+}
+
+// dft4 of (x0, x1, rot(x2), x3): x2 holds the third input before its
+// rotation, which is folded into the first additions
+template <bool INV, typename C> __device__ __forceinline__ void dft4_rot2(C &x0, C &x1, C &x2, C &x3)
+{
+    const C t0 = addrot<INV>(x0, x2), t1 = subrot<INV>(x0, x2), t2 = cadd(x1, x3), d = csub(x1, x3);
+    x0 = cadd(t0, t2);
+    x2 = csub(t0, t2);
+    x1 = addrot<INV>(t1, d);
+    x3 = subrot<INV>(t1, d);
 }
 
 template <bool INV, typename C> __device__ __forceinline__ void dft8(C *x)
@@ -75,14 +118,14 @@ template <bool INV, typename C> __device__ __forceinline__ void dft8(C *x)
     const S h = (S)0.70710678118654752440;
     dft4<INV>(x[0], x[2], x[4], x[6]);
     dft4<INV>(x[1], x[3], x[5], x[7]);
-    // twiddles w8^k on the odd half
+    // twiddles w8^k on the odd half: w8^1, w8^2 = rot (folded into the
+    // additions), w8^3 = rot w8^1 (folded into the constants)
     x[3] = crot<INV>(x[3], h, h);
-    x[5] = rot<INV>(x[5]);
-    x[7] = rot<INV>(crot<INV>(x[7], h, h));
+    x[7] = crot<INV>(x[7], -h, h);
     C y[8];
     y[0] = cadd(x[0], x[1]); y[4] = csub(x[0], x[1]);
     y[1] = cadd(x[2], x[3]); y[5] = csub(x[2], x[3]);
-    y[2] = cadd(x[4], x[5]); y[6] = csub(x[4], x[5]);
+    y[2] = addrot<INV>(x[4], x[5]); y[6] = subrot<INV>(x[4], x[5]);
     y[3] = cadd(x[6], x[7]); y[7] = csub(x[6], x[7]);
 #pragma unroll
     for (int i = 0; i < 8; ++i) x[i] = y[i];
@@ -106,11 +149,11 @@ template <bool INV, typename C> __device__ __forceinline__ void dft16_half(C *x)
 {
 #pragma unroll
     for (int n1 = 0; n1 < 4; ++n1) {
-        const C a = x[n1], b = x[n1 + 4], rb = rot<INV>(b);
+        const C a = x[n1], b = x[n1 + 4];
         x[n1] = cadd(a, b);
         x[n1 + 8] = csub(a, b);
-        x[n1 + 4] = cadd(a, rb);
-        x[n1 + 12] = csub(a, rb);
+        x[n1 + 4] = addrot<INV>(a, b);
+        x[n1 + 12] = subrot<INV>(a, b);
     }
     dft16_layer2<INV>(x);
 }
@@ -120,22 +163,24 @@ template <bool INV, typename C> __device__ __forceinline__ void dft16_layer2(C *
     using S = decltype(x[0].x);
     const S c1 = (S)0.92387953251128675613, s1 = (S)0.38268343236508977173;
     const S h = (S)0.70710678118654752440;
-    // x[n1 + 4 k1] now holds A[n1][k1]; multiply by w16^{n1 k1}
+    // x[n1 + 4 k1] now holds A[n1][k1]; multiply by w16^{n1 k1}. w^4 = rot is
+    // folded into the k1 = 2 DFT, rot w^2 = w^6 and -w^1 = w^9 into the
+    // constants.
     x[5] = crot<INV>(x[5], c1, s1);                // w^1
     x[9] = crot<INV>(x[9], h, h);                  // w^2
     x[13] = crot<INV>(x[13], s1, c1);              // w^3
     x[6] = crot<INV>(x[6], h, h);                  // w^2
-    x[10] = rot<INV>(x[10]);                       // w^4
-    x[14] = rot<INV>(crot<INV>(x[14], h, h));      // w^6
+    x[14] = crot<INV>(x[14], -h, h);               // w^6
     x[7] = crot<INV>(x[7], s1, c1);                // w^3
-    x[11] = rot<INV>(crot<INV>(x[11], h, h));      // w^6
-    x[15] = cscale(crot<INV>(x[15], c1, s1), (S)-1);  // w^9 = -w^1
+    x[11] = crot<INV>(x[11], -h, h);               // w^6
+    x[15] = crot<INV>(x[15], -c1, -s1);            // w^9
     // X[k1 + 4 k2] = DFT4 over n1 of A[n1][k1]
     C y[16];
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) {
         C a0 = x[4 * k1], a1 = x[4 * k1 + 1], a2 = x[4 * k1 + 2], a3 = x[4 * k1 + 3];
-        dft4<INV>(a0, a1, a2, a3);
+        if (k1 == 2) dft4_rot2<INV>(a0, a1, a2, a3);  // a2 = A[2][2] w^4
+        else dft4<INV>(a0, a1, a2, a3);
         y[k1] = a0; y[k1 + 4] = a1; y[k1 + 8] = a2; y[k1 + 12] = a3;
     }
 #pragma unroll
@@ -149,9 +194,8 @@ template <bool INV, typename C> __device__ __forceinline__ void dft3(C *x)
     C t1 = cadd(x[1], x[2]), t2 = cscale(csub(x[1], x[2]), s3);
     C a = C{x[0].x - (S)0.5 * t1.x, x[0].y - (S)0.5 * t1.y};
     x[0] = cadd(x[0], t1);
-    C r = rot<INV>(t2);
-    x[1] = cadd(a, r);
-    x[2] = csub(a, r);
+    x[1] = addrot<INV>(a, t2);
+    x[2] = subrot<INV>(a, t2);
 }
 
 // Odd prime R with cosines c[k-1] = cos(2 pi k/R), sines s[k-1] = sin(2 pi k/R):
@@ -180,9 +224,8 @@ __device__ __forceinline__ void dft_odd(C *x, const S *c, const S *s)
             a = C{a.x + cc * p[n - 1].x, a.y + cc * p[n - 1].y};
             b = C{b.x + ss * q[n - 1].x, b.y + ss * q[n - 1].y};
         }
-        C r = rot<INV>(b);
-        x[k] = cadd(a, r);
-        x[R - k] = csub(a, r);
+        x[k] = addrot<INV>(a, b);
+        x[R - k] = subrot<INV>(a, b);
     }
     x[0] = y0;
 }
@@ -218,16 +261,22 @@ template <bool INV, typename C> __device__ __forceinline__ void dft32(C *x)
     const S c[8] = {(S)1.0, (S)0.98078528040323044913, (S)0.92387953251128675613, (S)0.83146961230254523708,
                     (S)0.70710678118654752440, (S)0.55557023301960222474, (S)0.38268343236508977173,
                     (S)0.19509032201612826785};
+    // w32^k: k < 8 from the table; w32^8 = rot, folded into the additions;
+    // w32^k = rot w32^(k-8) for k > 8, folded into the constants
 #pragma unroll
     for (int k = 1; k < 16; ++k) {
         if (k < 8) o[k] = crot<INV>(o[k], c[k], c[8 - k]);
-        else if (k == 8) o[k] = rot<INV>(o[k]);
-        else o[k] = rot<INV>(crot<INV>(o[k], c[k - 8], c[16 - k]));
+        else if (k > 8) o[k] = crot<INV>(o[k], -c[16 - k], c[k - 8]);
     }
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        x[k] = cadd(e[k], o[k]);
-        x[k + 16] = csub(e[k], o[k]);
+        if (k == 8) {
+            x[k] = addrot<INV>(e[k], o[k]);
+            x[k + 16] = subrot<INV>(e[k], o[k]);
+        } else {
+            x[k] = cadd(e[k], o[k]);
+            x[k + 16] = csub(e[k], o[k]);
+        }
     }
 }
 
@@ -247,16 +296,22 @@ template <bool INV, typename C> __device__ __forceinline__ void dft32_half(C *x)
     const S c[8] = {(S)1.0, (S)0.98078528040323044913, (S)0.92387953251128675613, (S)0.83146961230254523708,
                     (S)0.70710678118654752440, (S)0.55557023301960222474, (S)0.38268343236508977173,
                     (S)0.19509032201612826785};
+    // w32^k: k < 8 from the table; w32^8 = rot, folded into the additions;
+    // w32^k = rot w32^(k-8) for k > 8, folded into the constants
 #pragma unroll
     for (int k = 1; k < 16; ++k) {
         if (k < 8) o[k] = crot<INV>(o[k], c[k], c[8 - k]);
-        else if (k == 8) o[k] = rot<INV>(o[k]);
-        else o[k] = rot<INV>(crot<INV>(o[k], c[k - 8], c[16 - k]));
+        else if (k > 8) o[k] = crot<INV>(o[k], -c[16 - k], c[k - 8]);
     }
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        x[k] = cadd(e[k], o[k]);
-        x[k + 16] = csub(e[k], o[k]);
+        if (k == 8) {
+            x[k] = addrot<INV>(e[k], o[k]);
+            x[k + 16] = subrot<INV>(e[k], o[k]);
+        } else {
+            x[k] = cadd(e[k], o[k]);
+            x[k + 16] = csub(e[k], o[k]);
+        }
     }
 }
 
