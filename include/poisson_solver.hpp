@@ -14,7 +14,6 @@
  *   - One GPU holds the whole grid: `partition` has one entry (icell = 0).
  *     Client code that indexes partition[rank] with rank 0 works as before.
  *   - No MPI is needed or used. Clients that call MPI themselves keep doing so.
- *   - setup2d/solve2d report "not part of this build".
  */
 #ifndef GB300_POISSON_SOLVER_HPP
 #define GB300_POISSON_SOLVER_HPP
@@ -58,6 +57,16 @@ private:
         return true;
     }
 
+    void fill_partition()
+    {
+        const int n = ps_partition_count(h_);
+        for (int i = 0; i < n; ++i) {
+            class_partition p;
+            ps_partition(h_, i, p.ncell, p.icell, p.dx);
+            partition.push_back(p);
+        }
+    }
+
 public:
     std::vector<class_partition> partition;
 
@@ -71,19 +80,16 @@ public:
 
     void setup2d(int ncell[2], int bc[2], double dx[2], int reg_order = 0)
     {
-        report(ps_setup2d(h_, ncell, bc, dx, reg_order), "setup2d");
+        partition.clear();
+        if (!report(ps_setup2d(h_, ncell, bc, dx, reg_order), "setup2d")) return;
+        fill_partition();
     }
 
     void setup3d(int ncell[3], int bc[3], double dx[3], int reg_order = 0)
     {
         partition.clear();
         if (!report(ps_setup3d(h_, ncell, bc, dx, reg_order), "setup3d")) return;
-        const int n = ps_partition_count(h_);
-        for (int i = 0; i < n; ++i) {
-            class_partition p;
-            ps_partition(h_, i, p.ncell, p.icell, p.dx);
-            partition.push_back(p);
-        }
+        fill_partition();
     }
 
     void set_return_grad(bool toggle) { report(ps_set_option(h_, PS_OPT_GRAD, toggle ? 1 : 0), "set_return_grad"); }

@@ -130,8 +130,14 @@ int ps_solve3d_device_noalloc(ps_solver *h, const double *bx, const double *by, 
 int ps_partition_count(const ps_solver *h);
 int ps_partition(const ps_solver *h, int index, int ncell[3], int icell[3], double dx[3]);
 
-/* setup2d / solve2d (poisson_solver.hpp:110, 118): the 2D solver is not
- * part of this build; both return PS_ERR_UNSUPPORTED. */
+/* setup2d / solve2d (poisson_solver.hpp:110, 118; setup2d.cpp:8,
+ * greens2d.cpp:9, solve2d.cpp:8). Boundary conditions per axis 0 (unbounded)
+ * or 1 (periodic), all four combinations. Fields are [Ny][Nx], x fastest,
+ * pushed and pulled with ps_push / ps_pull (X, Y and the out-of-plane Z as
+ * the reference: grad of X -> X, Y; div of X, Y -> X; curl of Z -> X, Y =
+ * (dZ/dy, -dZ/dx) of the solution). A handle set up by setup2d solves with
+ * ps_solve2d (ps_solve3d returns PS_ERR_STATE, and the reverse);
+ * ps_solve3d_device runs whichever solve the handle is set up for. */
 int ps_setup2d(ps_solver *h, const int ncell[2], const int bc[2], const double dx[2], int reg_order);
 int ps_solve2d(ps_solver *h);
 

@@ -58,6 +58,9 @@ def _lib(kind: str) -> ctypes.CDLL:
         f = lib.oracle_solve3d_timed
         f.restype = ctypes.c_int
         f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 4 + [_dp] * 10
+    f = getattr(lib, pre + "solve2d")
+    f.restype = ctypes.c_int
+    f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 3 + [_dp] * 9
     f = getattr(lib, pre + "greens3d")
     f.restype = ctypes.c_int
     f.argtypes = [_ip, _ip, _dp, ctypes.c_int, _dp, _dp, _dp, _ip]
@@ -148,6 +151,31 @@ def solve3d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False,
     if st:
         raise ValueError(f"oracle solve3d status {st}")
     # components the solve did not produce stay NaN-filled: report them as None
+    A = [a if not np.isnan(a).all() else None for a in A]
+    RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
+    return A, RB
+
+
+def solve2d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False, want_rhs=False,
+            kind: str = "port"):
+    """Run setup2d/push/solve2d/pull. B: sequence of 3 arrays [Ny][Nx] or None
+    (X, Y and the out-of-plane Z). Returns (A, RB) as solve3d."""
+    nx, ny = ncell
+    shape = (ny, nx)
+    Bc = [_f64(b) for b in B]
+    for b in Bc:
+        if b is not None and b.shape != shape:
+            raise ValueError(f"field shape {b.shape} != {shape}")
+    nan = float("nan")
+    A = [np.full(shape, nan) for _ in range(3)]
+    RB = [np.full(shape, nan) for _ in range(3)] if want_rhs else [None] * 3
+    nc = (ctypes.c_int * 2)(*ncell)
+    b = (ctypes.c_int * 2)(*bc)
+    d = (ctypes.c_double * 2)(*dx)
+    st = _fn(kind, "solve2d")(nc, b, d, int(reg), int(grad), int(div), int(curl),
+                              *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
+    if st:
+        raise ValueError(f"oracle solve2d status {st}")
     A = [a if not np.isnan(a).all() else None for a in A]
     RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
     return A, RB

@@ -259,7 +259,11 @@ static void transform_axis(cplx *a, const int p[3], int axis, int shift, int inv
     free(pen); free(w);
 }
 
-static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const double dx[3], int reg)
+/* two_d: the 2D kernel (greens2d.cpp:9-443) on a grid of one periodic
+ * z-plane (ncell[2] = 1, bc[2] = 1, dx[2] <= dx[0], dx[1] so that the filter
+ * width h = max(dx, dy) as greens2d.cpp:55 takes it); all four (x, y)
+ * boundary combinations are allowed. */
+static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const double dx[3], int reg, int two_d)
 {
     memset(K, 0, sizeof(*K));
     for (int d = 0; d < 3; ++d) {
@@ -270,6 +274,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
     int b0 = bc[0], b1 = bc[1], b2 = bc[2];
     int ok = (b0 == 0 && b1 == 0 && b2 == 0) || (b0 == 1 && b1 == 1 && b2 == 0) ||
              (b0 == 0 && b1 == 0 && b2 == 1) || (b0 == 1 && b1 == 1 && b2 == 1);
+    if (two_d) ok = b2 == 1 && ncell[2] == 1 && (b0 == 0 || b0 == 1) && (b1 == 0 || b1 == 1);
     if (!ok) return 2;
     for (int d = 0; d < 3; ++d) K->p[d] = (bc[d] == 0 ? 2 : 1) * ncell[d];
     K->reg = reg;
@@ -397,6 +402,32 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
                                         K->ik[2][k] * K->ik[2][k]);
                 }
         free(G2);
+    } else if (b0 != b1) {
+        /* 2D mixed (greens2d.cpp:316-440): along the unbounded axis u the line
+         * of zero wavenumber on the periodic axis is the transform of the 1D
+         * kernel -(sigma/pi)(rho Si(rho) + cos rho) du, sigma = du/pi, sampled
+         * at -(P_u/2) du + m du and half-swapped; every other mode is 1/|k|^2.
+         * For the x-unbounded case the reference stores the samples at an index
+         * it never sets (greens2d.cpp:400); the samples go to their own index. */
+        const int u = b0 == 0 ? 0 : 1;
+        int n = p[u];
+        cplx *pen = malloc(sizeof(cplx) * (size_t)n), *w = malloc(sizeof(cplx) * (size_t)n);
+        double sigma = dx[u] / PI, C1 = sigma / PI;
+        double umin = -(0.5 * (double)n) * dx[u];
+        for (int m = 0; m < n; ++m) {
+            double s = umin + (double)m * dx[u];
+            double rho = fabs(s) / sigma;
+            pen[m] = CMPLX(-C1 * (oracle_sine_int(rho) * rho + cos(rho)) * dx[u], 0.0);
+        }
+        fft_shift(pen, n);
+        glassman(pen, w, n, 0);
+        for (int j = 0; j < p[1]; ++j)
+            for (int i = 0; i < p[0]; ++i) {
+                size_t q = (size_t)j * p[0] + i;
+                if (u == 1 ? i == 0 : j == 0) G[q] = pen[u == 1 ? j : i];
+                else G[q] = -1.0 / (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j]);
+            }
+        free(pen); free(w);
     } else {
         /* Periodic (greens3d.cpp:478-521): 1/|k|^2 with the zero mode removed. */
         for (int k = 0; k < p[2]; ++k)
@@ -415,7 +446,7 @@ int oracle_greens3d(const int ncell[3], const int bc[3], const double dx[3], int
                     double *g_re, double *g_im, double *zeta, int pext[3])
 {
     kernel_t K;
-    int st = kernel_build(&K, ncell, bc, dx, reg);
+    int st = kernel_build(&K, ncell, bc, dx, reg, 0);
     if (st) { kernel_free(&K); return st; }
     size_t np = (size_t)K.p[0] * K.p[1] * K.p[2];
     for (int d = 0; d < 3; ++d) pext[d] = K.p[d];
@@ -447,11 +478,15 @@ int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int 
                                 rbx, rby, rbz, NULL);
 }
 
-int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3], int reg,
-                         int grad, int div, int curl, int reproject,
-                         const double *bx, const double *by, const double *bz,
-                         double *ax, double *ay, double *az,
-                         double *rbx, double *rby, double *rbz, double seconds[3])
+/* setup3d/push/solve3d/pull, or with two_d setup2d/push/solve2d/pull on a
+ * grid of one periodic z-plane (see kernel_build): the z transforms are then
+ * of length one and ikZ = 0, so the 3D data flow is the 2D one
+ * (solve2d.cpp:8-475); only the output selection differs. */
+static int solve_core(const int ncell[3], const int bc[3], const double dx[3], int reg,
+                      int grad, int div, int curl, int reproject, int two_d,
+                      const double *bx, const double *by, const double *bz,
+                      double *ax, double *ay, double *az,
+                      double *rbx, double *rby, double *rbz, double seconds[3])
 {
     double t0 = now_s();
     const double *B[3] = {bx, by, bz};
@@ -460,22 +495,40 @@ int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3]
     int r[3] = {bx != NULL, by != NULL, bz != NULL};
     int l[3] = {0, 0, 0};
 
-    /* Output selection (solve3d.cpp:43-107). */
-    if (grad) {
-        if (!r[0]) return 3;
-        l[0] = l[1] = l[2] = 1;
-    } else if (div) {
-        if (!(r[0] && r[1] && r[2])) return 3;
-        l[0] = 1;
-    } else if (curl) {
-        if (!(r[0] && r[1] && r[2])) return 3;
-        l[0] = l[1] = l[2] = 1;
+    if (!two_d) {
+        /* Output selection (solve3d.cpp:43-107). */
+        if (grad) {
+            if (!r[0]) return 3;
+            l[0] = l[1] = l[2] = 1;
+        } else if (div) {
+            if (!(r[0] && r[1] && r[2])) return 3;
+            l[0] = 1;
+        } else if (curl) {
+            if (!(r[0] && r[1] && r[2])) return 3;
+            l[0] = l[1] = l[2] = 1;
+        } else {
+            for (int c = 0; c < 3; ++c) l[c] = r[c];
+        }
     } else {
-        for (int c = 0; c < 3; ++c) l[c] = r[c];
+        /* 2D (solve2d.cpp:43-103): grad of X -> (X, Y); div of (X, Y) -> X;
+         * curl of Z -> (X, Y) = (d/dy, -d/dx); no reprojection. */
+        reproject = 0;
+        if (grad) {
+            if (!r[0]) return 3;
+            l[0] = l[1] = 1;
+        } else if (div) {
+            if (!(r[0] && r[1])) return 3;
+            l[0] = 1;
+        } else if (curl) {
+            if (!r[2]) return 3;
+            l[0] = l[1] = 1;
+        } else {
+            for (int c = 0; c < 3; ++c) l[c] = r[c];
+        }
     }
 
     kernel_t K;
-    int st = kernel_build(&K, ncell, bc, dx, reg);
+    int st = kernel_build(&K, ncell, bc, dx, reg, two_d);
     if (st) { kernel_free(&K); return st; }
     double t1 = now_s();
 
@@ -535,15 +588,30 @@ int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3]
                 for (int k = nz; k < nfft; ++k) pr[c][k] = CMPLX(0.0, 0.0);
                 glassman(pr[c], w, nfft, 0);
             }
-            /* grad reads component d, or component x where d was not pushed */
-            const cplx *gY = r[1] ? pr[1] : pr[0], *gZ = r[2] ? pr[2] : pr[0];
+            /* grad reads component d, or component x where d was not pushed
+             * (2D: always x, solve2d.cpp:298-299) */
+            const cplx *gY = (r[1] && !two_d) ? pr[1] : pr[0], *gZ = r[2] ? pr[2] : pr[0];
             for (int k = 0; k < nfft; ++k) {
                 size_t q = ((size_t)k * py + j) * px + i;
                 if (reg > 0)
                     for (int c = 0; c < 3; ++c)
                         if (r[c]) pr[c][k] *= K.zeta[q];
                 cplx G = K.G[q];
-                if (grad) {
+                if (two_d) {
+                    /* solve2d.cpp:292-325 */
+                    if (grad) {
+                        pl[0][k] = ikX[i] * G * pr[0][k];
+                        pl[1][k] = ikY[j] * G * pr[0][k];
+                    } else if (div) {
+                        pl[0][k] = G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k]);
+                    } else if (curl) {
+                        pl[0][k] = ikY[j] * G * pr[2][k];
+                        pl[1][k] = -ikX[i] * G * pr[2][k];
+                    } else {
+                        for (int c = 0; c < 3; ++c)
+                            if (l[c]) pl[c][k] = G * pr[c][k];
+                    }
+                } else if (grad) {
                     pl[0][k] = ikX[i] * G * pr[0][k];
                     pl[1][k] = ikY[j] * G * gY[k];
                     pl[2][k] = ikZ[k] * G * gZ[k];
@@ -626,4 +694,26 @@ int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3]
         seconds[2] = now_s() - t2;   /* pull */
     }
     return 0;
+}
+
+int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3], int reg,
+                         int grad, int div, int curl, int reproject,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz, double seconds[3])
+{
+    return solve_core(ncell, bc, dx, reg, grad, div, curl, reproject, 0, bx, by, bz, ax, ay, az, rbx, rby, rbz,
+                      seconds);
+}
+
+int oracle_solve2d(const int ncell[2], const int bc[2], const double dx[2], int reg,
+                   int grad, int div, int curl,
+                   const double *bx, const double *by, const double *bz,
+                   double *ax, double *ay, double *az,
+                   double *rbx, double *rby, double *rbz)
+{
+    const int nc3[3] = {ncell[0], ncell[1], 1};
+    const int bc3[3] = {bc[0], bc[1], 1};
+    const double dx3[3] = {dx[0], dx[1], fmin(dx[0], dx[1])};
+    return solve_core(nc3, bc3, dx3, reg, grad, div, curl, 0, 1, bx, by, bz, ax, ay, az, rbx, rby, rbz, NULL);
 }

@@ -50,6 +50,15 @@ int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3]
                          double *ax, double *ay, double *az,
                          double *rbx, double *rby, double *rbz, double seconds[3]);
 
+/* Full setup2d / push / solve2d / pull (solve2d.cpp:8-475). Real fields are
+ * [Ny][Nx], x fastest; X, Y, Z as in the reference (grad of X -> X, Y; div
+ * of X, Y -> X; curl of Z -> X, Y). Returns 0, 2 or 3 as oracle_solve3d. */
+int oracle_solve2d(const int ncell[2], const int bc[2], const double dx[2], int reg,
+                   int grad, int div, int curl,
+                   const double *bx, const double *by, const double *bz,
+                   double *ax, double *ay, double *az,
+                   double *rbx, double *rby, double *rbz);
+
 #ifdef __cplusplus
 }
 #endif

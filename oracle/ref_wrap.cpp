@@ -53,6 +53,29 @@ int ref_solve3d(const int ncell[3], const int bc[3], const double dx[3], int reg
     return 0;
 }
 
+/* One setup2d/push/solve2d/pull sequence (setup2d.cpp:8, push.cpp:9,
+ * solve2d.cpp:8, pull.cpp:8); fields [Ny][Nx]. */
+int ref_solve2d(const int ncell[2], const int bc[2], const double dx[2], int reg,
+                int grad, int div, int curl,
+                const double *bx, const double *by, const double *bz,
+                double *ax, double *ay, double *az,
+                double *rbx, double *rby, double *rbz)
+{
+    int nc[2] = {ncell[0], ncell[1]};
+    int b[2] = {bc[0], bc[1]};
+    double d[2] = {dx[0], dx[1]};
+    poisson_solver ps;
+    ps.setup2d(nc, b, d, reg);
+    if (ps.G2D == NULL) return 2;
+    ps.set_return_grad(grad != 0);
+    ps.set_return_div(div != 0);
+    ps.set_return_curl(curl != 0);
+    ps.push(const_cast<double *>(bx), const_cast<double *>(by), const_cast<double *>(bz));
+    ps.solve2d();
+    ps.pull(ax, ay, az, rbx, rby, rbz);
+    return 0;
+}
+
 double ref_sine_int(double x) { return sine_int(x); }
 double ref_bessel_int_J0(double x) { return bessel_int_J0(x); }
 

@@ -7,6 +7,6 @@ that ABI; it mirrors the reference solver class (PoissonSolver) and builds the
 native library in-tree (build.py).
 """
 from ._lib import PSError, load  # noqa: F401
-from .solver import Partition, PoissonBatch, PoissonSolver, solve  # noqa: F401
+from .solver import Partition, PoissonBatch, PoissonSolver, solve, solve2d  # noqa: F401
 
-__all__ = ["PoissonSolver", "PoissonBatch", "Partition", "PSError", "load", "solve"]
+__all__ = ["PoissonSolver", "PoissonBatch", "Partition", "PSError", "load", "solve", "solve2d"]

@@ -96,7 +96,7 @@ int ps_push_device(ps_solver *h, const double *bx, const double *by, const doubl
 
 int ps_solve3d(ps_solver *h)
 {
-    return guarded(h, [&](ps::Solver &s) { s.solve_internal(); });
+    return guarded(h, [&](ps::Solver &s) { s.solve_internal(3); });
 }
 
 int ps_pull(ps_solver *h, double *ax, double *ay, double *az, double *bx, double *by, double *bz)
@@ -142,16 +142,15 @@ int ps_partition(const ps_solver *h, int index, int ncell[3], int icell[3], doub
     return PS_OK;
 }
 
-int ps_setup2d(ps_solver *h, const int *, const int *, const double *, int)
+int ps_setup2d(ps_solver *h, const int ncell[2], const int bc[2], const double dx[2], int reg_order)
 {
-    if (h) h->s.last_error = "the 2D solver is not part of this build";
-    return PS_ERR_UNSUPPORTED;
+    if (!ncell || !bc || !dx) return PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) { s.setup2d(ncell, bc, dx, reg_order); });
 }
 
 int ps_solve2d(ps_solver *h)
 {
-    if (h) h->s.last_error = "the 2D solver is not part of this build";
-    return PS_ERR_UNSUPPORTED;
+    return guarded(h, [&](ps::Solver &s) { s.solve_internal(2); });
 }
 
 int ps_set_stream(ps_solver *h, void *stream)
@@ -190,7 +189,7 @@ int ps_get_info(const ps_solver *h, int what, double *value)
     case PS_INFO_PADDED_X: *value = s.P[0]; break;
     case PS_INFO_PADDED_Y: *value = s.P[1]; break;
     case PS_INFO_PADDED_Z: *value = s.P[2]; break;
-    case PS_INFO_LAUNCHES_PER_SOLVE: *value = 5; break;
+    case PS_INFO_LAUNCHES_PER_SOLVE: *value = s.dims == 2 ? 3 : 5; break;
     case PS_INFO_DEVICE_BYTES: *value = (double)s.device_bytes(); break;
     case PS_INFO_KERNEL_OCTANT: *value = (double)s.Mx * s.oy * s.oz; break;
     default: return PS_ERR_ARGUMENT;

@@ -235,6 +235,9 @@ __global__ void k_kernel_fill(const KernelFillArgs a)
             case 0: g = a.spec[((long long)kz * a.P[1] + ky) * a.Mx + kx].x; break;
             case 1: g = (kx == 0 && ky == 0) ? a.line[kz] : 1.0 / k2; break;
             case 2: g = (kz == 0) ? a.plane[(long long)ky * a.Mx + kx].x : 1.0 / k2; break;
+            // 2D mixed (greens2d.cpp:316-440): the zero-wavenumber line of the periodic axis
+            case 4: g = (kx == 0) ? a.line[ky] : 1.0 / k2; break;  // x periodic, y unbounded
+            case 5: g = (ky == 0) ? a.line[kx] : 1.0 / k2; break;  // x unbounded, y periodic
             default: g = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : 1.0 / k2; break;
             }
         }

@@ -181,6 +181,7 @@ template <typename F> int lines_per_cta(int tpl, F smem)
 int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
 {
     if (!s.is_setup) throw Error(PS_ERR_STATE, "setup3d has not been called");
+    if (s.dims != 3) throw Error(PS_ERR_STATE, "the no-allocation solve is 3D only");
     int in_mask = 0;
     for (int c = 0; c < 3; ++c)
         if (Bin[c]) in_mask |= 1 << c;

@@ -289,6 +289,7 @@ void Solver::setup3d(const int ncell[3], const int bcs[3], const double dxs[3], 
         if (p > 8192) throw Error(PS_ERR_UNSUPPORTED, "padded transform length above 8192");
     }
     is_setup = false;
+    dims = 3;
     for (int d = 0; d < 3; ++d) {
         n[d] = ncell[d];
         bc[d] = bcs[d];
@@ -296,11 +297,46 @@ void Solver::setup3d(const int ncell[3], const int bcs[3], const double dxs[3], 
         P[d] = (bcs[d] == 0 ? 2 : 1) * ncell[d];
     }
     reg = reg_order;
+    finish_setup();
+}
+
+// setup2d (setup2d.cpp:8-71, greens2d.cpp:9-443): every (x, y) boundary
+// combination. The problem is held as one periodic z-plane: n[2] = P[2] = 1
+// (kz = 0 only) and dx[2] = min(dx, dy), so the filter width h = max(dx, dy)
+// as greens2d.cpp:55 takes it.
+void Solver::setup2d(const int ncell[2], const int bcs[2], const double dxs[2], int reg_order)
+{
+    for (int d = 0; d < 2; ++d) {
+        if (ncell[d] < 1) throw Error(PS_ERR_ARGUMENT, "ncell must be positive");
+        if (!(dxs[d] > 0.0) || !std::isfinite(dxs[d])) throw Error(PS_ERR_ARGUMENT, "dx must be positive and finite");
+        if (bcs[d] != 0 && bcs[d] != 1) throw Error(PS_ERR_BOUNDARY, "boundary condition must be 0 (unbounded) or 1 (periodic)");
+        if ((bcs[d] == 0 ? 2LL : 1LL) * ncell[d] > 8192) throw Error(PS_ERR_UNSUPPORTED, "padded transform length above 8192");
+    }
+    if (reg_order < 0) throw Error(PS_ERR_ARGUMENT, "reg_order must be >= 0");
+    is_setup = false;
+    dims = 2;
+    for (int d = 0; d < 2; ++d) {
+        n[d] = ncell[d];
+        bc[d] = bcs[d];
+        dx[d] = dxs[d];
+        P[d] = (bcs[d] == 0 ? 2 : 1) * ncell[d];
+    }
+    n[2] = 1;
+    bc[2] = 1;
+    dx[2] = std::min(dxs[0], dxs[1]);
+    P[2] = 1;
+    reg = reg_order;
+    finish_setup();
+}
+
+void Solver::finish_setup()
+{
     Mx = P[0] / 2 + 1;
     ldx = (Mx + 1) & ~1;  // even: rows of the spectra are whole 16-byte units
     oy = P[1] / 2 + 1;
     oz = P[2] / 2 + 1;
-    kzp = (oz + 3) & ~3;
+    // z pitch of the fast-axis kernel copy: the fused pass runs along z (3D) or y (2D)
+    kzp = ((dims == 2 ? oy : oz) + 3) & ~3;
     pushed = produced = rhs_ready = 0;
     kern32.release();
     kernzf32.release();
@@ -370,7 +406,10 @@ void Solver::build_kernel()
     fa.reg = reg;
     fa.norm = (double)P[0] * (double)P[1] * (double)P[2];
     const int b0 = bc[0], b1 = bc[1], b2 = bc[2];
-    fa.kind = (b0 == 0 && b1 == 0 && b2 == 0) ? 0 : (b0 == 1 && b1 == 1 && b2 == 0) ? 1 : (b2 == 1 && b0 == 0) ? 2 : 3;
+    if (dims == 3)
+        fa.kind = (b0 == 0 && b1 == 0 && b2 == 0) ? 0 : (b0 == 1 && b1 == 1 && b2 == 0) ? 1 : (b2 == 1 && b0 == 0) ? 2 : 3;
+    else  // 2D on one kz = 0 plane: unbounded = the 2D kernel plane, periodic, or one mixed line
+        fa.kind = (b0 == 0 && b1 == 0) ? 2 : (b0 == 1 && b1 == 1) ? 3 : (b0 == 1) ? 4 : 5;
 
     DevBuf oct, spec, line;
     const int ox = P[0] / 2 + 1;
@@ -442,9 +481,12 @@ void Solver::build_kernel()
         } else {
             fa.plane = (const double2 *)spec.p;
         }
-    } else if (fa.kind == 1) {
-        line.ensure((size_t)oz * sizeof(double));
-        PS_CK(launch_line_ppf((double *)line.p, P[2], dx[2], stream));
+    } else if (fa.kind == 1 || fa.kind == 4 || fa.kind == 5) {
+        // the 1D kernel along the unbounded axis: z (3D periodic-periodic-
+        // unbounded), y (2D x-periodic) or x (2D y-periodic)
+        const int u = fa.kind == 1 ? 2 : fa.kind == 4 ? 1 : 0;
+        line.ensure((size_t)(P[u] / 2 + 1) * sizeof(double));
+        PS_CK(launch_line_ppf((double *)line.p, P[u], dx[u], stream));
         fa.line = (const double *)line.p;
     }
     PS_CK(launch_kernel_fill(fa, stream));
@@ -459,10 +501,14 @@ void Solver::ensure_kernel(int prec)
         kern32.ensure(nk * sizeof(float));
         PS_CK(launch_to_fp32((const double *)kern64.p, (float *)kern32.p, nk, stream));
     }
-    // the z-fastest copy for the bulk-copy z kernel, on the z extents it runs
-    if (!kernzf32.p && bc[2] == 0 && (P[2] == 256 || P[2] == 512 || P[2] == 1024)) {
-        kernzf32.ensure((size_t)Mx * oy * kzp * sizeof(float));
-        PS_CK(launch_kernel_zfast((const double *)kern64.p, (float *)kernzf32.p, Mx, oy, oz, kzp, stream));
+    // the fast-axis copy for the bulk-copy fused kernel, on the extents it
+    // runs: z in 3D; y in 2D, where the kernel [oy][Mx] is read as [oy][1][Mx]
+    const int fa_axis = dims == 2 ? 1 : 2;
+    const int Lf = P[fa_axis];
+    if (!kernzf32.p && bc[fa_axis] == 0 && (Lf == 256 || Lf == 512 || Lf == 1024)) {
+        const int rows = dims == 2 ? 1 : oy, planes = dims == 2 ? oy : oz;
+        kernzf32.ensure((size_t)Mx * rows * kzp * sizeof(float));
+        PS_CK(launch_kernel_zfast((const double *)kern64.p, (float *)kernzf32.p, Mx, rows, planes, kzp, stream));
     }
 }
 
@@ -493,6 +539,22 @@ void Solver::ensure_zeta(int prec)
 // ---------------------------------------------------------------------------
 int Solver::output_mask(int in_mask) const
 {
+    if (dims == 2) {
+        // solve2d.cpp:43-103: grad of X -> X, Y; div of X, Y -> X; curl of Z -> X, Y
+        if (opt_grad) {
+            if (!(in_mask & 1)) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for grad option");
+            return 3;
+        }
+        if (opt_div) {
+            if ((in_mask & 3) != 3) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for div option");
+            return 1;
+        }
+        if (opt_curl) {
+            if (!(in_mask & 4)) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for curl option");
+            return 3;
+        }
+        return in_mask;
+    }
     if (opt_grad) {
         if (!(in_mask & 1)) throw Error(PS_ERR_COMPONENTS, "rhs fields have not been pushed correctly for grad option");
         return 7;
@@ -609,6 +671,46 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     za.kxc = 2.0 * M_PI / ((double)P[0] * dx[0]);
     za.kyc = 2.0 * M_PI / ((double)P[1] * dx[1]);
     za.kzc = 2.0 * M_PI / ((double)P[2] * dx[2]);
+    if (dims == 2) {
+        // The fused pass runs along y over one row of x columns: its transform
+        // axis ("z") is y, its row axis has one entry (ky = 0 there), and the
+        // kernel [oy][Mx] is its [oz][1][Mx] octant. The 2D outputs
+        // (solve2d.cpp:292-325) from the 3D operations with k = (kx, 0, ky):
+        // grad X -> (X, -, Y); div (X, -, Y); curl of Z = (ky, -kx) K Z is the
+        // gradient with kx negated, written (Y, -, X).
+        za.L = P[1];
+        za.n_in = n[1];
+        za.n_out = n[1];
+        za.axis_stride = ldx;
+        za.row_stride = ldx;
+        za.oct_y = 1;
+        za.Py = 1;
+        za.Pz = P[1];
+        za.kyc = 0.0;
+        za.kzc = 2.0 * M_PI / ((double)P[1] * dx[1]);
+        za.reproject = 0;
+        void *wX = (write_mask & 1) ? work[0].p : nullptr, *wY = (write_mask & 2) ? work[1].p : nullptr;
+        if (op == OP_GRAD || op == OP_CURL) {
+            const bool curl = op == OP_CURL;
+            za.op = OP_GRAD;
+            za.nin = 1;
+            za.in[0] = work[curl ? 2 : 0].p;
+            za.in[1] = za.in[2] = nullptr;
+            za.nout = 3;
+            za.out[0] = curl ? wY : wX;
+            za.out[1] = nullptr;
+            za.out[2] = curl ? wX : wY;
+            if (curl) za.kxc = -za.kxc;
+        } else if (op == OP_DIV) {
+            za.nin = 3;
+            za.in[0] = work[0].p;
+            za.in[1] = work[0].p;  // weighted by ky = 0
+            za.in[2] = work[1].p;
+            za.nout = 1;
+            za.out[0] = wX;
+            za.out[1] = za.out[2] = nullptr;
+        }
+    }
 
     // y inverse (cropped to Ny) and x inverse (cropped to Nx) of the written outputs
     ColArgs &yi = pa.yi;
@@ -658,9 +760,11 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
 
 static int axis_of(int pass) { return pass == 0 || pass == 4 ? 0 : pass == 2 ? 2 : 1; }
 
+int Solver::pass_len(int pass) const { return dims == 2 && pass == 2 ? P[1] : P[axis_of(pass)]; }
+
 bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
 {
-    const int prec = precision, L = P[axis_of(pass)], op = pa.z.op;
+    const int prec = precision, L = pass_len(pass), op = pa.z.op;
     switch (fam) {
     case 'r': return true;
     case 'p': return p2::supported(prec, L) && (pass != 2 || p2::supports_op(op));
@@ -761,7 +865,7 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
         const int want = atoi(v);
         if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) pref = want;
     }
-    const Plan &pl = plan(P[axis], precision, family_emax(pass, fam));
+    const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam));
     if (fam == 'q')  // fixed by the length
         pref = pass == 2 ? wide::zq_lines(pl.dev.L) : axis == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L);
     int B = pref;
@@ -775,7 +879,7 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
 void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
 {
     const int prec = precision, axis = axis_of(pass);
-    const Plan &pl = plan(P[axis], prec, family_emax(pass, c.fam));
+    const Plan &pl = plan(pass_len(pass), prec, family_emax(pass, c.fam));
     switch (pass) {
     case 0: {
         XFwdArgs &a = pa.x;
@@ -803,11 +907,12 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
         ZArgs &a = pa.z;
         a.plan = pl.dev;
         a.B = c.B;
-        if (c.fam == 'q') PS_CK(wide::launch_zq(a, P[1], static_cast<int *>(status.p), stream));
-        else if (c.fam == 't') PS_CK(wide::launch_zt(a, P[1], stream));
-        else if (c.fam == 'w') PS_CK(wide::launch_z(a, P[1], stream));
-        else if (c.fam == 'p') PS_CK(p2::launch_z(a, P[1], family_emax(2, 'p'), stream));
-        else PS_CK(launch_z(prec, a, P[1], stream));
+        const int ny = dims == 2 ? 1 : P[1];  // rows of columns (2D: one row of x columns)
+        if (c.fam == 'q') PS_CK(wide::launch_zq(a, ny, static_cast<int *>(status.p), stream));
+        else if (c.fam == 't') PS_CK(wide::launch_zt(a, ny, stream));
+        else if (c.fam == 'w') PS_CK(wide::launch_z(a, ny, stream));
+        else if (c.fam == 'p') PS_CK(p2::launch_z(a, ny, family_emax(2, 'p'), stream));
+        else PS_CK(launch_z(prec, a, ny, stream));
         break;
     }
     default: {
@@ -886,7 +991,7 @@ std::string Solver::tune_key(int pass, const PassArgs &pa)
         device_tag = d.str();
     }
     std::ostringstream k;
-    k << device_tag << ":" << (precision == PREC_FP64 ? "fp64" : "fp32") << ":N" << n[0] << 'x'
+    k << device_tag << ":" << (precision == PREC_FP64 ? "fp64" : "fp32") << ":" << dims << "d:N" << n[0] << 'x'
       << n[1] << 'x' << n[2] << ":P" << P[0] << 'x' << P[1] << 'x' << P[2] << ":op" << pa.z.op << ":in" << pa.x.ncomp
       << ":out" << pa.xi.ncomp << ":z" << pa.z.nin << pa.z.nout << ":pass" << pass;
     return k.str();
@@ -908,7 +1013,7 @@ PassChoice Solver::choice(int pass, const PassArgs &pa)
         tune_load_locked();
         auto it = tune_table.find(tune_key(pass, pa));
         if (it != tune_table.end() && family_ok(pass, it->second.fam, pa)) {
-            const Plan &pl = plan(P[axis_of(pass)], precision, family_emax(pass, it->second.fam));
+            const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, it->second.fam));
             if (pass_fits(pass, it->second.fam, it->second.B, pa, pl)) return it->second;
         }
     }
@@ -937,7 +1042,8 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     // x forward, y forward, z (forward, spectral operation, inverse), then
     // y inverse and x inverse of the written outputs
     for (int pass = 0; pass < NPASS; ++pass) {
-        if (pass < 3 || write_mask) launch_pass(pass, choice(pass, pa), pa);
+        // 2D: the fused pass transforms y itself
+        if ((pass < 3 || write_mask) && !(dims == 2 && (pass == 1 || pass == 3))) launch_pass(pass, choice(pass, pa), pa);
         mark(pass + 1);
     }
     return write_mask;
@@ -976,11 +1082,12 @@ void Solver::autotune(int in_mask)
     try {
         for (int pass = 0; pass < NPASS; ++pass) {
             if (pass >= 3 && !write_mask) continue;
+            if (dims == 2 && (pass == 1 || pass == 3)) continue;  // the fused pass transforms y
             PassChoice best{0, 0};
             float best_ms = 0.f;
             for (char fam : {'q', 't', 'w', 'p', 'r'}) {
                 if (!family_ok(pass, fam, pa)) continue;
-                const Plan &pl = plan(P[axis_of(pass)], precision, family_emax(pass, fam));
+                const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam));
                 for (int B = 1; B <= 64; B *= 2) {
                     if (!pass_fits(pass, fam, B, pa, pl)) continue;
                     const PassChoice c{fam, B};
@@ -1051,9 +1158,11 @@ void Solver::push(const double *const B[3], cudaMemcpyKind kind)
     rhs_ready = 0;
 }
 
-void Solver::solve_internal()
+void Solver::solve_internal(int want_dims)
 {
     check_setup();
+    if (want_dims != dims)
+        throw Error(PS_ERR_STATE, dims == 2 ? "handle set up by setup2d: call solve2d" : "handle set up by setup3d: call solve3d");
     if (!pushed) throw Error(PS_ERR_STATE, "solve3d called before push");
     const int out_mask = output_mask(pushed);
     const double *Bin[3];

@@ -62,6 +62,10 @@ struct Solver {
     cudaStream_t stream = nullptr;
 
     bool is_setup = false;
+    // 2: set up by setup2d. The 2D problem is held as one periodic z-plane
+    // (n[2] = P[2] = 1); its solve is the x pass, one fused pass along y
+    // (forward, spectral operation, inverse) and the x inverse.
+    int dims = 3;
     int n[3] = {0, 0, 0}, bc[3] = {0, 0, 0}, P[3] = {0, 0, 0};
     double dx[3] = {0, 0, 0};
     int reg = 0;
@@ -99,6 +103,8 @@ struct Solver {
     ~Solver();
 
     void setup3d(const int ncell[3], const int bcs[3], const double dxs[3], int reg_order);
+    void setup2d(const int ncell[2], const int bcs[2], const double dxs[2], int reg_order);
+    void finish_setup();  // buffers and the kernel once n, bc, dx, P, reg are set
     void set_option(int option, int value);
     int get_option(int option) const;
 
@@ -113,7 +119,7 @@ struct Solver {
     int output_mask(int in_mask) const;
 
     void push(const double *const B[3], cudaMemcpyKind kind);
-    void solve_internal();
+    void solve_internal(int want_dims = 3);
     void pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind);
     // After the stream has drained: throws PS_ERR_TIMEOUT (and clears the
     // word) if a kernel reported a timed-out wait.
@@ -133,6 +139,9 @@ struct Solver {
     const Plan &plan(int L, int prec, int emax = 0);  // emax 0: e_max(prec)
     void ensure_kernel(int prec);
     void ensure_zeta(int prec);
+
+    // length of the transform a pass runs (the fused pass runs along y in 2D)
+    int pass_len(int pass) const;
 
 private:
     bool family_ok(int pass, char fam, const PassArgs &pa) const;

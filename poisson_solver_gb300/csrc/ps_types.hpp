@@ -222,8 +222,9 @@ struct KernelFillArgs {
     double *zeta_out;      // out (optional): zeta / norm
     const double2 *spec;   // kind 0: spectrum [oz][Py][Mx] (real part used)
     const double2 *plane;  // kind 2 (kz = 0 plane): spectrum [oy][Mx]
-    const double *line;    // kind 1 (kx = ky = 0 line): 1D kernel spectrum, length Pz
-    int kind;              // 0 unbounded, 1 ppf, 2 ffp, 3 periodic
+    const double *line;    // kinds 1, 4, 5: 1D kernel spectrum along the unbounded axis (z, y, x)
+    int kind;              // 0 unbounded, 1 ppf, 2 ffp (and 2D unbounded), 3 periodic,
+                           // 4 2D x-periodic y-unbounded, 5 2D x-unbounded y-periodic
     int Mx, oy, oz;
     int P[3];
     double dx[3];

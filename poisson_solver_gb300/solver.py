@@ -1,11 +1,11 @@
 """Python mirror of the reference solver class (c++/source/poisson_solver.hpp:39-124).
 
 Same member names and argument meaning as the reference C++ class --
-setup3d, set_return_grad/div/curl, set_reprojection, push, solve3d, pull and
-the ``partition`` list -- over the C ABI of libps_gb300.so. Where the
-reference prints an error and returns, this raises PSError with the same
-message. Fields are float64 arrays shaped (Nz, Ny, Nx) (x fastest), the
-layout the reference's push/pull use.
+setup3d/setup2d, set_return_grad/div/curl, set_reprojection, push,
+solve3d/solve2d, pull and the ``partition`` list -- over the C ABI of
+libps_gb300.so. Where the reference prints an error and returns, this raises
+PSError with the same message. Fields are float64 arrays shaped (Nz, Ny, Nx)
+(2D: (Ny, Nx)), x fastest, the layout the reference's push/pull use.
 """
 from __future__ import annotations
 
@@ -44,7 +44,7 @@ def _host_ptr(a, shape, name, writable=False):
 
 
 class PoissonSolver:
-    """GB300 Green's-function FFT Poisson solver: lap(A) = -B in 3D."""
+    """GB300 Green's-function FFT Poisson solver: lap(A) = -B in 3D or 2D."""
 
     def __init__(self):
         self._lib = L.load()
@@ -84,6 +84,9 @@ class PoissonSolver:
         d = (ctypes.c_double * 3)(*[float(v) for v in dx])
         self._call("ps_setup3d", nc, b, d, int(reg_order))
         self._shape = (int(ncell[2]), int(ncell[1]), int(ncell[0]))
+        self._fill_partition()
+
+    def _fill_partition(self):
         self.partition = []
         for i in range(self._lib.ps_partition_count(self._h)):
             n3 = (ctypes.c_int * 3)()
@@ -93,10 +96,13 @@ class PoissonSolver:
             self.partition.append(Partition(tuple(n3), tuple(i3), tuple(d3)))
 
     def setup2d(self, ncell, bc, dx, reg_order: int = 0):
-        nc = (ctypes.c_int * 2)(*ncell)
-        b = (ctypes.c_int * 2)(*bc)
-        d = (ctypes.c_double * 2)(*dx)
+        """2D solver (setup2d.cpp:8): fields are [Ny][Nx] arrays."""
+        nc = (ctypes.c_int * 2)(*[int(v) for v in ncell])
+        b = (ctypes.c_int * 2)(*[int(v) for v in bc])
+        d = (ctypes.c_double * 2)(*[float(v) for v in dx])
         self._call("ps_setup2d", nc, b, d, int(reg_order))
+        self._shape = (int(ncell[1]), int(ncell[0]))
+        self._fill_partition()
 
     def solve2d(self):
         self._call("ps_solve2d")
@@ -287,6 +293,29 @@ class PoissonBatch:
         if st != L.PS_OK:
             raise L.PSError(st, self._lib.ps_status_string(st).decode())
         return v.value
+
+
+def solve2d(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,
+            precision="fp64", want_rhs=False):
+    """One-shot host 2D solve; B: 3 arrays [Ny][Nx] or None (X, Y, Z).
+    Returns (A, RB) lists of 3 arrays or None."""
+    shape = (ncell[1], ncell[0])
+    with PoissonSolver() as ps:
+        ps.setup2d(ncell, bc, dx, reg_order)
+        ps.set_return_grad(grad)
+        ps.set_return_div(div)
+        ps.set_return_curl(curl)
+        ps.set_precision(precision)
+        Bc = [None if b is None else np.ascontiguousarray(b, dtype=np.float64) for b in B]
+        ps.push(*Bc)
+        ps.solve2d()
+        nan = float("nan")
+        A = [np.full(shape, nan) for _ in range(3)]
+        RB = [np.full(shape, nan) for _ in range(3)] if want_rhs else [None] * 3
+        ps.pull(*A, *RB)
+    A = [a if not np.isnan(a).all() else None for a in A]
+    RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
+    return A, RB
 
 
 def solve(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,

@@ -36,15 +36,27 @@ CASES = [
 ]
 
 
+# 2D (setup2d/solve2d): name, ncell, bc, dx, reg, options, pushed components,
+# zero mean. The x-unbounded y-periodic combination has no fixture: the
+# reference leaves its 1D line kernel unset there (greens2d.cpp:400).
+CASES2D = [
+    ("2d_unb_grad_reg4", (12, 10), (0, 0), (0.1, 0.12), 4, dict(grad=True), "x", False),
+    ("2d_unb_none_xyz_odd", (9, 13), (0, 0), (0.2, 0.15), 0, dict(), "xyz", False),
+    ("2d_per_curl_reg2", (12, 10), (1, 1), (0.1, 0.12), 2, dict(curl=True), "z", True),
+    ("2d_xper_div", (10, 14), (1, 0), (0.15, 0.1), 0, dict(div=True), "xy", False),
+]
+
+
 def make_inputs(name, ncell, comps, zero_mean):
     rng = np.random.default_rng(sum(map(ord, name)))
-    shape = (ncell[2], ncell[1], ncell[0])
+    shape = tuple(reversed(ncell))
+    axes = tuple(range(1, len(shape)))
     B = []
     for c in "xyz":
         if c in comps:
             b = rng.standard_normal(shape)
             if zero_mean:
-                b -= b.mean(axis=(1, 2), keepdims=True)
+                b -= b.mean(axis=axes if len(shape) == 3 else None, keepdims=True)
             B.append(b)
         else:
             B.append(None)
@@ -54,9 +66,10 @@ def make_inputs(name, ncell, comps, zero_mean):
 def main():
     if not oracle.available("reference"):
         oracle.build()
-    for name, ncell, bc, dx, reg, opts, comps, zm in CASES:
+    for name, ncell, bc, dx, reg, opts, comps, zm in CASES + CASES2D:
         B = make_inputs(name, ncell, comps, zm)
-        A, RB = oracle.solve3d(ncell, bc, dx, B, reg, want_rhs=True, kind="reference", **opts)
+        solve = oracle.solve3d if len(ncell) == 3 else oracle.solve2d
+        A, RB = solve(ncell, bc, dx, B, reg, want_rhs=True, kind="reference", **opts)
         out = dict(ncell=np.array(ncell), bc=np.array(bc), dx=np.array(dx), reg=np.array(reg),
                    options=np.array([int(opts.get(k, False)) for k in ("grad", "div", "curl", "reproject")]))
         for i, c in enumerate("xyz"):

@@ -45,7 +45,7 @@ def test_status_strings_and_null_handles(native):
     assert b"timed out" in lib.ps_status_string(_lib.PS_ERR_TIMEOUT)
     assert lib.ps_solve3d(None) == _lib.PS_ERR_ARGUMENT
     assert lib.ps_destroy(None) == _lib.PS_OK
-    assert lib.ps_setup2d(None, None, None, None, 0) == _lib.PS_ERR_UNSUPPORTED
+    assert lib.ps_setup2d(None, None, None, None, 0) == _lib.PS_ERR_ARGUMENT
     assert lib.ps_partition_count(None) == 0
 
 
@@ -83,9 +83,10 @@ def test_dropin_header_compiles_and_links(native, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-@pytest.mark.parametrize("prog", ["unbounded3d", "periodic3d", "mixed_ppf3d", "mixed_ffp3d"])
+@pytest.mark.parametrize("prog", ["unbounded3d", "periodic3d", "mixed_ppf3d", "mixed_ffp3d",
+                                  "unbounded2d", "periodic2d", "mixed2d"])
 def test_reference_validation_programs_build_unchanged(native, tmp_path, prog):
-    """The reference's own 3D test programs compile and link, unmodified, against the drop-in."""
+    """The reference's own 3D and 2D test programs compile and link, unmodified, against the drop-in."""
     src = os.path.join(REF_TESTS, prog, "sources", "main.cpp")
     if not os.path.exists(src):
         pytest.skip("reference test sources not present")

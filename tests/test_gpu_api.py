@@ -30,9 +30,16 @@ def test_error_statuses(native):
         ps.setup3d((0, 8, 8), (0, 0, 0), (0.1,) * 3)
     assert e.value.status == _lib.PS_ERR_ARGUMENT
     with pytest.raises(PSError) as e:
-        ps.setup2d((8, 8), (0, 0), (0.1, 0.1))
-    assert e.value.status == _lib.PS_ERR_UNSUPPORTED
+        ps.setup2d((8, 8), (0, 2), (0.1, 0.1))
+    assert e.value.status == _lib.PS_ERR_BOUNDARY
+    ps.setup2d((8, 8), (0, 0), (0.1, 0.1))
+    with pytest.raises(PSError) as e:
+        ps.solve3d()  # a 2D handle solves with solve2d
+    assert e.value.status == _lib.PS_ERR_STATE
     ps.setup3d((8, 8, 8), (0, 0, 0), (0.1,) * 3)
+    with pytest.raises(PSError) as e:
+        ps.solve2d()  # and a 3D handle with solve3d
+    assert e.value.status == _lib.PS_ERR_STATE
     with pytest.raises(PSError) as e:
         ps.solve3d()
     assert e.value.status == _lib.PS_ERR_STATE

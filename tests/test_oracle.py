@@ -106,7 +106,8 @@ def test_solve_matches_reference(oracle, case):
 @pytest.mark.parametrize("name", golden_cases())
 def test_port_matches_golden(oracle, name):
     g = load_golden(name)
-    A, RB = oracle.solve3d(g["ncell"], g["bc"], g["dx"], g["B"], g["reg"], want_rhs=True, **g["opts"])
+    solve = oracle.solve3d if len(g["ncell"]) == 3 else oracle.solve2d
+    A, RB = solve(g["ncell"], g["bc"], g["dx"], g["B"], g["reg"], want_rhs=True, **g["opts"])
     # bitwise on the machine that wrote the fixtures; libm may differ by an ulp elsewhere
     assert rel_l2(A, g["A"]) < 1e-13
     assert rel_l2(RB, g["RB"]) < 1e-13
@@ -129,3 +130,69 @@ def test_rejections_match_reference(oracle):
         oracle.solve3d(nc, (0, 0, 0), dx, [None, b, None], grad=True)
     with pytest.raises(ValueError, match="status 2"):
         oracle.solve3d(nc, (0, 1, 0), dx, [b, None, None])
+
+
+# ---------------------------------------------------------------------------
+# 2D (setup2d / solve2d)
+SOLVES2D = [
+    ((12, 10), (0, 0), (0.1, 0.12), 0, dict(), "xyz"),
+    ((12, 10), (0, 0), (0.1, 0.12), 4, dict(grad=True), "x"),
+    ((9, 14), (1, 1), (0.2, 0.1), 2, dict(curl=True), "z"),
+    ((9, 14), (1, 0), (0.2, 0.1), 0, dict(div=True), "xy"),
+    ((10, 11), (1, 0), (0.1, 0.1), 6, dict(curl=True), "z"),
+]
+
+
+def _fields2d(nc, comps, seed, zero_mean):
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in "xyz":
+        if c in comps:
+            b = rng.standard_normal((nc[1], nc[0]))
+            out.append(b - b.mean() if zero_mean else b)
+        else:
+            out.append(None)
+    return out
+
+
+@pytest.mark.parametrize("case", SOLVES2D, ids=[f"{c[1]}-{list(c[4])}-reg{c[3]}" for c in SOLVES2D])
+def test_solve2d_matches_reference(oracle, case):
+    _need_ref(oracle)
+    nc, bc, dx, reg, opts, comps = case
+    B = _fields2d(nc, comps, sum(nc) + reg, bc == (1, 1))
+    A1, R1 = oracle.solve2d(nc, bc, dx, B, reg, want_rhs=True, kind="port", **opts)
+    A2, R2 = oracle.solve2d(nc, bc, dx, B, reg, want_rhs=True, kind="reference", **opts)
+    assert rel_l2(A1, A2) == 0.0
+    assert rel_l2(R1, R2) == 0.0
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(grad=True), dict(curl=True)])
+def test_solve2d_x_unbounded_is_the_transposed_y_unbounded(oracle, opts):
+    """The x-unbounded, y-periodic domain has no reference output (its line
+    kernel is stored at an unset index, greens2d.cpp:400): check it against
+    the y-unbounded, x-periodic domain of the transposed problem."""
+    nc, dx = (12, 10), (2.0 / 12, 1.5 / 10)
+    comps = "z" if opts.get("curl") else "x"
+    B = _fields2d(nc, comps, 5, False)
+    A, _ = oracle.solve2d(nc, (0, 1), dx, B, 2, **opts)
+    At, _ = oracle.solve2d((nc[1], nc[0]), (1, 0), (dx[1], dx[0]),
+                           [None if b is None else b.T.copy() for b in B], 2, **opts)
+    if opts.get("grad"):
+        pairs = [(A[0], At[1]), (A[1], At[0])]       # d/dx <-> d/dy
+    elif opts.get("curl"):
+        pairs = [(A[0], -At[1]), (A[1], -At[0])]     # (d/dy, -d/dx) <-> -(d/dx, -d/dy) swapped
+    else:
+        pairs = [(A[0], At[0])]
+    for a, b in pairs:
+        assert rel_l2([a.T], [b]) < 1e-14
+
+
+def test_solve2d_rejections(oracle):
+    nc, dx = (6, 6), (0.1, 0.1)
+    b = np.ones((6, 6))
+    with pytest.raises(ValueError, match="status 3"):
+        oracle.solve2d(nc, (0, 0), dx, [b, None, None], curl=True)
+    with pytest.raises(ValueError, match="status 3"):
+        oracle.solve2d(nc, (0, 0), dx, [b, None, None], div=True)
+    with pytest.raises(ValueError, match="status 3"):
+        oracle.solve2d(nc, (0, 0), dx, [None, b, None], grad=True)
