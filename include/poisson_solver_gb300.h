@@ -141,6 +141,27 @@ int ps_partition(const ps_solver *h, int index, int ncell[3], int icell[3], doub
 int ps_setup2d(ps_solver *h, const int ncell[2], const int bc[2], const double dx[2], int reg_order);
 int ps_solve2d(ps_solver *h);
 
+/* Fortran-style fields (poisson_solver_push.f:8, poisson_solver_pull.f:8):
+ * one HOST array holding ncomp = 1..3 components interleaved, component
+ * fastest, then x, y, z, with allocated extents ext[3] (ghost layers
+ * included); the field's cell (i, j, k) is element
+ * ((k + offset[2]) ext[1] + (j + offset[1])) ext[0] + (i + offset[0]),
+ * times ncomp, plus the component. push_interleaved pushes X (ncomp 1),
+ * X, Y (2) or X, Y, Z (3). pull_interleaved writes the first ncomp_a solution
+ * components to a and the first ncomp_b returned right-hand-side components
+ * to b (either may be NULL); components the solve did not produce are
+ * written as zero, and elements outside the field box are left untouched. */
+int ps_push_interleaved(ps_solver *h, const double *b, int ncomp, const int ext[3], const int offset[3]);
+int ps_pull_interleaved(ps_solver *h, double *a, int ncomp_a, double *b, int ncomp_b, const int ext[3],
+                        const int offset[3]);
+
+/* Gaussian smoothing of the pushed fields in place (poisson_solver_smooth3d.f):
+ * each is zero-padded on unbounded axes, transformed, multiplied by
+ * exp(-width^2 |k|^2 / 2) with the solver's wavenumbers, transformed back and
+ * cropped; a later solve3d or pull of the right-hand side sees the smoothed
+ * fields. 3D handles only. */
+int ps_smooth3d(ps_solver *h, double width);
+
 /* Stream the handle launches on (a cudaStream_t; NULL = legacy default). */
 int ps_set_stream(ps_solver *h, void *stream);
 /* Wait for the handle's stream. */

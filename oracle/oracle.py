@@ -58,6 +58,10 @@ def _lib(kind: str) -> ctypes.CDLL:
         f = lib.oracle_solve3d_timed
         f.restype = ctypes.c_int
         f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 4 + [_dp] * 10
+    if kind == "port":
+        f = lib.oracle_smooth3d
+        f.restype = ctypes.c_int
+        f.argtypes = [_ip, _ip, _dp, ctypes.c_double] + [_dp] * 6
     f = getattr(lib, pre + "solve2d")
     f.restype = ctypes.c_int
     f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 3 + [_dp] * 9
@@ -179,6 +183,20 @@ def solve2d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False, w
     A = [a if not np.isnan(a).all() else None for a in A]
     RB = [r if (r is not None and not np.isnan(r).all()) else None for r in RB]
     return A, RB
+
+
+def smooth3d(ncell, bc, dx, B, width: float):
+    """Port of smooth3d: the fields B (3 arrays [Nz][Ny][Nx] or None), smoothed."""
+    shape = (ncell[2], ncell[1], ncell[0])
+    Bc = [_f64(b) for b in B]
+    out = [None if b is None else np.empty(shape) for b in Bc]
+    nc = (ctypes.c_int * 3)(*ncell)
+    b = (ctypes.c_int * 3)(*bc)
+    d = (ctypes.c_double * 3)(*dx)
+    st = _lib("port").oracle_smooth3d(nc, b, d, float(width), *[_ptr(x) for x in Bc], *[_ptr(x) for x in out])
+    if st:
+        raise ValueError(f"oracle smooth3d status {st}")
+    return out
 
 
 def solve3d_timed(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False, reproject=False):

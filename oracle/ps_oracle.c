@@ -717,3 +717,59 @@ int oracle_solve2d(const int ncell[2], const int bc[2], const double dx[2], int 
     const double dx3[3] = {dx[0], dx[1], fmin(dx[0], dx[1])};
     return solve_core(nc3, bc3, dx3, reg, grad, div, curl, 0, 1, bx, by, bz, ax, ay, az, rbx, rby, rbz, NULL);
 }
+
+/* ------------------------------------------------------------------------ */
+/* smooth3d (fortran/source/poisson_solver/poisson_solver_smooth3d.f): each
+ * field zero-padded on unbounded axes, transformed along x, y, z, multiplied
+ * by exp(-s^2 |k|^2 / 2) with the ik wavenumbers of greens3d.cpp:73-118,
+ * transformed back, normalised by the padded size and cropped. */
+int oracle_smooth3d(const int ncell[3], const int bc[3], const double dx[3], double s,
+                    const double *bx, const double *by, const double *bz,
+                    double *ox, double *oy, double *oz)
+{
+    const double *B[3] = {bx, by, bz};
+    double *O[3] = {ox, oy, oz};
+    int p[3];
+    for (int d = 0; d < 3; ++d) {
+        if (bc[d] != 0 && bc[d] != 1) return 2;
+        p[d] = (bc[d] == 0 ? 2 : 1) * ncell[d];
+    }
+    double *k2[3];
+    for (int d = 0; d < 3; ++d) {
+        k2[d] = malloc(sizeof(double) * (size_t)p[d]);
+        double dk = 1.0 / ((double)p[d] * dx[d]);
+        for (int m = 0; m < p[d]; ++m) {
+            int mm = (2 * m < p[d]) ? m : m - p[d];
+            double k = 2.0 * PI * (double)mm * dk;
+            k2[d][m] = k * k;
+        }
+    }
+    size_t np = (size_t)p[0] * p[1] * p[2];
+    cplx *a = malloc(sizeof(cplx) * np);
+    for (int c = 0; c < 3; ++c) {
+        if (!B[c] || !O[c]) continue;
+        for (size_t q = 0; q < np; ++q) a[q] = CMPLX(0.0, 0.0);
+        for (int k = 0; k < ncell[2]; ++k)
+            for (int j = 0; j < ncell[1]; ++j)
+                for (int i = 0; i < ncell[0]; ++i)
+                    a[((size_t)k * p[1] + j) * p[0] + i] = CMPLX(B[c][((size_t)k * ncell[1] + j) * ncell[0] + i], 0.0);
+        transform_axis(a, p, 0, 0, 0);
+        transform_axis(a, p, 1, 0, 0);
+        transform_axis(a, p, 2, 0, 0);
+        for (int k = 0; k < p[2]; ++k)
+            for (int j = 0; j < p[1]; ++j)
+                for (int i = 0; i < p[0]; ++i)
+                    a[((size_t)k * p[1] + j) * p[0] + i] *= exp(-0.5 * s * s * (k2[0][i] + k2[1][j] + k2[2][k]));
+        transform_axis(a, p, 2, 0, 1);
+        transform_axis(a, p, 1, 0, 1);
+        transform_axis(a, p, 0, 0, 1);
+        for (int k = 0; k < ncell[2]; ++k)
+            for (int j = 0; j < ncell[1]; ++j)
+                for (int i = 0; i < ncell[0]; ++i)
+                    O[c][((size_t)k * ncell[1] + j) * ncell[0] + i] =
+                        creal(a[((size_t)k * p[1] + j) * p[0] + i]) / (double)np;
+    }
+    free(a);
+    for (int d = 0; d < 3; ++d) free(k2[d]);
+    return 0;
+}

@@ -59,6 +59,12 @@ int oracle_solve2d(const int ncell[2], const int bc[2], const double dx[2], int 
                    double *ax, double *ay, double *az,
                    double *rbx, double *rby, double *rbz);
 
+/* Gaussian smoothing of up to three fields [Nz][Ny][Nx] by
+ * exp(-s^2 |k|^2 / 2) on the (zero-padded) solver grid. */
+int oracle_smooth3d(const int ncell[3], const int bc[3], const double dx[3], double s,
+                    const double *bx, const double *by, const double *bz,
+                    double *ox, double *oy, double *oz);
+
 #ifdef __cplusplus
 }
 #endif

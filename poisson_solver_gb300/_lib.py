@@ -61,6 +61,9 @@ SIGNATURES = {
     "ps_set_option": (_i, [_vp, _i, _i]),
     "ps_get_option": (_i, [_vp, _i, _ip]),
     "ps_push": (_i, [_vp, _dp, _dp, _dp]),
+    "ps_push_interleaved": (_i, [_vp, _dp, _i, _ip, _ip]),
+    "ps_pull_interleaved": (_i, [_vp, _dp, _i, _dp, _i, _ip, _ip]),
+    "ps_smooth3d": (_i, [_vp, ctypes.c_double]),
     "ps_solve3d": (_i, [_vp]),
     "ps_pull": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "ps_push_device": (_i, [_vp, _dp, _dp, _dp]),

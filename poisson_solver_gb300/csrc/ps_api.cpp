@@ -153,6 +153,26 @@ int ps_solve2d(ps_solver *h)
     return guarded(h, [&](ps::Solver &s) { s.solve_internal(2); });
 }
 
+int ps_push_interleaved(ps_solver *h, const double *b, int ncomp, const int ext[3], const int offset[3])
+{
+    if (!ext || !offset) return PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) { s.push_interleaved(b, ncomp, ext, offset, cudaMemcpyHostToDevice); });
+}
+
+int ps_pull_interleaved(ps_solver *h, double *a, int ncomp_a, double *b, int ncomp_b, const int ext[3],
+                        const int offset[3])
+{
+    if (!ext || !offset) return PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) {
+        s.pull_interleaved(a, ncomp_a, b, ncomp_b, ext, offset, cudaMemcpyDeviceToHost);
+    });
+}
+
+int ps_smooth3d(ps_solver *h, double width)
+{
+    return guarded(h, [&](ps::Solver &s) { s.smooth3d(width); });
+}
+
 int ps_set_stream(ps_solver *h, void *stream)
 {
     return guarded(h, [&](ps::Solver &s) { s.stream = (cudaStream_t)stream; });

@@ -241,9 +241,12 @@ __global__ void k_kernel_fill(const KernelFillArgs a)
             default: g = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : 1.0 / k2; break;
             }
         }
-        // zeta = e^{-a} sum_{n < r/2} a^n / n!, a = sigma^2 |k|^2 / 2 (greens3d.cpp:123-159)
+        // zeta = e^{-a} sum_{n < r/2} a^n / n!, a = sigma^2 |k|^2 / 2 (greens3d.cpp:123-159);
+        // the smooth3d filter e^{-s^2 |k|^2 / 2} (poisson_solver_smooth3d.f:205-212)
         double zeta = 1.0;
-        if (a.reg > 0) {
+        if (a.smooth) {
+            zeta = exp(-0.5 * a.smooth_sigma * a.smooth_sigma * k2);
+        } else if (a.reg > 0) {
             const double arg = 0.5 * sigma * sigma * k2;
             double c = 1.0, p = 1.0, sum = 1.0;
             for (int m = 1; m <= r / 2 - 1; ++m) {

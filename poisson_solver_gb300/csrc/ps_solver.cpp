@@ -342,6 +342,10 @@ void Solver::finish_setup()
     kernzf32.release();
     zeta64.release();
     zeta32.release();
+    smooth64.release();
+    smooth32.release();
+    smooth_s = -1.0;
+    stage.release();
     for (int c = 0; c < 3; ++c) {
         work[c].release();
         fb[c].release();
@@ -581,6 +585,7 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     if (filter_only) {
         op = OP_FILTER;
         out_mask = in_mask;
+        if (filter_source == 1 && !smooth64.p) throw Error(PS_ERR_STATE, "smoothing filter not built");
     } else {
         out_mask = output_mask(in_mask);
         op = opt_grad ? OP_GRAD : opt_div ? OP_DIV : opt_curl ? OP_CURL : OP_NONE;
@@ -592,7 +597,11 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     const int prec = precision;
     const size_t csz = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
     ensure_kernel(prec);
-    if (op == OP_FILTER) ensure_zeta(prec);
+    if (op == OP_FILTER && filter_source == 0) ensure_zeta(prec);
+    if (op == OP_FILTER && filter_source == 1 && prec == PREC_FP32 && !smooth32.p) {
+        smooth32.ensure((size_t)Mx * oy * oz * sizeof(float));
+        PS_CK(launch_to_fp32((const double *)smooth64.p, (float *)smooth32.p, (size_t)Mx * oy * oz, stream));
+    }
     for (int c = 0; c < 3; ++c)
         if ((in_mask | out_mask) >> c & 1) work[c].ensure(work_elems() * csz);
     pa = PassArgs{};
@@ -659,9 +668,12 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     za.axis_stride = (long long)P[1] * ldx;
     za.row_stride = ldx;
     za.op = op;
-    za.reproject = op == OP_FILTER && opt_reproject && in_mask == 7;
+    za.reproject = op == OP_FILTER && filter_source == 0 && opt_reproject && in_mask == 7;
     za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
-    za.zeta = op == OP_FILTER ? (prec == PREC_FP64 ? zeta64.p : zeta32.p) : nullptr;
+    za.zeta = nullptr;
+    if (op == OP_FILTER)
+        za.zeta = filter_source == 1 ? (prec == PREC_FP64 ? smooth64.p : smooth32.p)
+                                     : (prec == PREC_FP64 ? zeta64.p : zeta32.p);
     za.oct_y = oy;
     za.kern_zf = prec == PREC_FP32 ? static_cast<const float *>(kernzf32.p) : nullptr;
     za.kzp = kzp;
@@ -1179,6 +1191,30 @@ void Solver::solve_internal(int want_dims)
     rhs_ready = 0;
 }
 
+void Solver::returned_rhs(const double *out[3])
+{
+    // the reference returns B after its forward/inverse round trip, i.e.
+    // B itself unless the regulariser or the reprojection changed it
+    const size_t bytes = field_elems() * sizeof(double);
+    const bool filtered = reg > 0 || (opt_reproject && pushed == 7 && dims == 3);
+    if (filtered && !rhs_ready) {
+        const double *Bin[3];
+        double *Rout[3];
+        for (int c = 0; c < 3; ++c) {
+            Bin[c] = (pushed >> c & 1) ? (const double *)fb[c].p : nullptr;
+            Rout[c] = nullptr;
+            if (pushed >> c & 1) {
+                fr[c].ensure(bytes);
+                Rout[c] = (double *)fr[c].p;
+            }
+        }
+        solve(Bin, Rout, true);
+        rhs_ready = 1;
+    }
+    for (int c = 0; c < 3; ++c)
+        out[c] = (pushed >> c & 1) ? (const double *)(filtered ? fr[c].p : fb[c].p) : nullptr;
+}
+
 void Solver::pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind)
 {
     check_setup();
@@ -1189,28 +1225,133 @@ void Solver::pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind)
     for (int c = 0; c < 3; ++c)
         if (RB[c] && (pushed >> c & 1)) want_rhs = true;
     if (want_rhs) {
-        // the reference returns B after its forward/inverse round trip, i.e.
-        // B itself unless the regulariser or the reprojection changed it
-        const bool filtered = reg > 0 || (opt_reproject && pushed == 7);
-        if (filtered && !rhs_ready) {
-            const double *Bin[3];
-            double *Rout[3];
-            for (int c = 0; c < 3; ++c) {
-                Bin[c] = (pushed >> c & 1) ? (const double *)fb[c].p : nullptr;
-                Rout[c] = nullptr;
-                if (pushed >> c & 1) {
-                    fr[c].ensure(bytes);
-                    Rout[c] = (double *)fr[c].p;
-                }
-            }
-            solve(Bin, Rout, true);
-            rhs_ready = 1;
-        }
+        const double *src[3];
+        returned_rhs(src);
         for (int c = 0; c < 3; ++c)
-            if (RB[c] && (pushed >> c & 1))
-                PS_CK(cudaMemcpyAsync(RB[c], filtered ? fr[c].p : fb[c].p, bytes, kind, stream));
+            if (RB[c] && src[c]) PS_CK(cudaMemcpyAsync(RB[c], src[c], bytes, kind, stream));
     }
     synchronize();
+}
+
+// Fortran-style arrays (poisson_solver_push.f:8-140, poisson_solver_pull.f:8-485):
+// element (c, i, j, k) of the field at ((k + o2) e1 + (j + o1)) e0 + (i + o0))
+// ncomp + c. The field box moves as one pitched 3D copy to or from a packed
+// device buffer, which the (de)interleave kernels split or build.
+static cudaMemcpy3DParms box_copy(const int n[3], int ncomp)
+{
+    cudaMemcpy3DParms p{};
+    p.extent = make_cudaExtent((size_t)n[0] * ncomp * sizeof(double), (size_t)n[1], (size_t)n[2]);
+    return p;
+}
+
+static void check_box(const int n[3], int ncomp, const int ext[3], const int off[3])
+{
+    if (ncomp < 1 || ncomp > 3) throw Error(PS_ERR_ARGUMENT, "an interleaved array holds 1 to 3 components");
+    for (int d = 0; d < 3; ++d)
+        if (off[d] < 0 || ext[d] < off[d] + n[d])
+            throw Error(PS_ERR_ARGUMENT, "array extents must hold the field at its offset");
+}
+
+void Solver::push_interleaved(const double *b, int ncomp, const int ext[3], const int off[3], cudaMemcpyKind kind)
+{
+    check_setup();
+    if (!b) throw Error(PS_ERR_ARGUMENT, "null array");
+    check_box(n, ncomp, ext, off);
+    const size_t elems = field_elems();
+    stage.ensure(elems * ncomp * sizeof(double));
+    cudaMemcpy3DParms p = box_copy(n, ncomp);
+    p.srcPtr = make_cudaPitchedPtr(const_cast<double *>(b), (size_t)ext[0] * ncomp * sizeof(double),
+                                   (size_t)ext[0] * ncomp, (size_t)ext[1]);
+    p.srcPos = make_cudaPos((size_t)off[0] * ncomp * sizeof(double), (size_t)off[1], (size_t)off[2]);
+    p.dstPtr = make_cudaPitchedPtr(stage.p, (size_t)n[0] * ncomp * sizeof(double), (size_t)n[0] * ncomp, (size_t)n[1]);
+    p.kind = kind;
+    PS_CK(cudaMemcpy3DAsync(&p, stream));
+    double *dst[3] = {nullptr, nullptr, nullptr};
+    for (int c = 0; c < ncomp; ++c) {
+        fb[c].ensure(elems * sizeof(double));
+        dst[c] = (double *)fb[c].p;
+    }
+    PS_CK(launch_deinterleave((const double *)stage.p, ncomp, (long long)elems, dst, stream));
+    PS_CK(cudaStreamSynchronize(stream));
+    pushed = (1 << ncomp) - 1;  // X; X, Y; or X, Y, Z as the array's first extent says
+    rhs_ready = 0;
+}
+
+void Solver::pull_interleaved(double *a, int ncomp_a, double *b, int ncomp_b, const int ext[3], const int off[3],
+                              cudaMemcpyKind kind)
+{
+    check_setup();
+    const size_t elems = field_elems();
+    for (int which = 0; which < 2; ++which) {
+        double *arr = which == 0 ? a : b;
+        const int ncomp = which == 0 ? ncomp_a : ncomp_b;
+        if (!arr) continue;
+        check_box(n, ncomp, ext, off);
+        // solution components the solve produced, or the returned right-hand
+        // side; components not there are written as zero (pull.f:340-365)
+        const double *src[3] = {nullptr, nullptr, nullptr};
+        if (which == 0) {
+            for (int c = 0; c < 3; ++c) src[c] = (produced >> c & 1) ? (const double *)fa[c].p : nullptr;
+        } else {
+            returned_rhs(src);
+        }
+        stage.ensure(elems * ncomp * sizeof(double));
+        PS_CK(launch_interleave(src, ncomp, (long long)elems, (double *)stage.p, stream));
+        cudaMemcpy3DParms p = box_copy(n, ncomp);
+        p.srcPtr = make_cudaPitchedPtr(stage.p, (size_t)n[0] * ncomp * sizeof(double), (size_t)n[0] * ncomp, (size_t)n[1]);
+        p.dstPtr = make_cudaPitchedPtr(arr, (size_t)ext[0] * ncomp * sizeof(double), (size_t)ext[0] * ncomp, (size_t)ext[1]);
+        p.dstPos = make_cudaPos((size_t)off[0] * ncomp * sizeof(double), (size_t)off[1], (size_t)off[2]);
+        p.kind = kind;
+        PS_CK(cudaMemcpy3DAsync(&p, stream));
+        PS_CK(cudaStreamSynchronize(stream));  // the stage is reused by the next array
+    }
+    synchronize();
+}
+
+// smooth3d (poisson_solver_smooth3d.f): the pushed fields, zero-padded on
+// unbounded axes, transformed, multiplied by exp(-s^2 |k|^2 / 2) with the
+// solver's wavenumbers, transformed back and cropped, in place. It runs the
+// filter pass of the pipeline with the Gaussian octant.
+void Solver::smooth3d(double s)
+{
+    check_setup();
+    if (dims != 3) throw Error(PS_ERR_STATE, "smooth3d is for 3D handles");
+    if (!(s >= 0.0) || !std::isfinite(s)) throw Error(PS_ERR_ARGUMENT, "smoothing width must be finite and >= 0");
+    if (!pushed) throw Error(PS_ERR_STATE, "smooth3d called before push");
+    const size_t nk = (size_t)Mx * oy * oz;
+    if (smooth_s != s) {
+        smooth64.ensure(nk * sizeof(double));
+        smooth32.release();
+        KernelFillArgs fa{};
+        fa.zeta_out = (double *)smooth64.p;
+        fa.Mx = Mx;
+        fa.oy = oy;
+        fa.oz = oz;
+        for (int d = 0; d < 3; ++d) {
+            fa.P[d] = P[d];
+            fa.dx[d] = dx[d];
+        }
+        fa.norm = (double)P[0] * (double)P[1] * (double)P[2];
+        fa.smooth = 1;
+        fa.smooth_sigma = s;
+        PS_CK(launch_kernel_fill(fa, stream));
+        smooth_s = s;
+    }
+    const double *Bin[3];
+    double *Aout[3];
+    for (int c = 0; c < 3; ++c) {
+        Bin[c] = (pushed >> c & 1) ? (const double *)fb[c].p : nullptr;
+        Aout[c] = (pushed >> c & 1) ? (double *)fb[c].p : nullptr;
+    }
+    filter_source = 1;
+    try {
+        solve(Bin, Aout, true);
+    } catch (...) {
+        filter_source = 0;
+        throw;
+    }
+    filter_source = 0;
+    rhs_ready = 0;
 }
 
 void Solver::synchronize()

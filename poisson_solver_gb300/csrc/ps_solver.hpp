@@ -79,6 +79,10 @@ struct Solver {
     DevBuf kern64, kern32;  // octant K = G zeta / (Px Py Pz)
     DevBuf kernzf32;        // FP32 K with z fastest, [oy][Mx][kzp] (unbounded z of 256..1024 points)
     DevBuf zeta64, zeta32;  // octant zeta / (Px Py Pz), built on first use
+    DevBuf smooth64, smooth32;  // octant exp(-s^2 |k|^2 / 2) / (Px Py Pz) of smooth3d(s)
+    double smooth_s = -1.0;     // s the smooth octants hold (-1: none)
+    int filter_source = 0;      // the filter pass multiplies by zeta (0) or the smooth octant (1)
+    DevBuf stage;               // packed interleaved fields for push/pull_interleaved
     DevBuf work[3];         // per-component spectra [Nz][Py][Mx], pass precision
     DevBuf fb[3], fa[3], fr[3];  // handle-owned fields: pushed B, solution A, returned B
     DevBuf status;               // int[4]: [0] bit 0 set by a kernel whose bounded wait timed out,
@@ -121,6 +125,17 @@ struct Solver {
     void push(const double *const B[3], cudaMemcpyKind kind);
     void solve_internal(int want_dims = 3);
     void pull(double *const A[3], double *const RB[3], cudaMemcpyKind kind);
+    // The returned right-hand side of the pushed fields (device pointers,
+    // null where not pushed): B itself unless the regulariser or the
+    // reprojection changed it, else the filtered copy (built on demand).
+    void returned_rhs(const double *out[3]);
+    // Fortran-style push/pull of one array with interleaved components
+    // (component fastest, then x, y, z; extents ext, field box at offset).
+    void push_interleaved(const double *b, int ncomp, const int ext[3], const int offset[3], cudaMemcpyKind kind);
+    void pull_interleaved(double *a, int ncomp_a, double *b, int ncomp_b, const int ext[3], const int offset[3],
+                          cudaMemcpyKind kind);
+    // Gaussian smoothing of the pushed fields, exp(-s^2 |k|^2 / 2), in place.
+    void smooth3d(double s);
     // After the stream has drained: throws PS_ERR_TIMEOUT (and clears the
     // word) if a kernel reported a timed-out wait.
     void check_status();

@@ -230,8 +230,14 @@ struct KernelFillArgs {
     double dx[3];
     int reg;
     double norm;
+    int smooth;           // zeta_out = exp(-smooth_sigma^2 |k|^2 / 2) / norm (the smooth3d
+    double smooth_sigma;  // filter) in place of the regularisation filter
 };
 cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st);
+// Fields with interleaved components (ps_fields.cu): packed [nz][ny][nx][ncomp]
+// <-> ncomp separate [nz][ny][nx] arrays (absent = zero on the way out).
+cudaError_t launch_deinterleave(const double *packed, int ncomp, long long n, double *const out[3], cudaStream_t st);
+cudaError_t launch_interleave(const double *const in[3], int ncomp, long long n, double *packed, cudaStream_t st);
 cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t st);
 // FP32 copy of the octant [oz][oy][Mx] with z fastest: out[(y Mx + x) kzp + z],
 // zero for oz <= z < kzp (each column a whole number of 16-byte units).

@@ -142,6 +142,35 @@ class PoissonSolver:
                                                          ("Ax", "Ay", "Az", "Bx", "By", "Bz"))]
         self._call("ps_pull", *ptrs)
 
+    # -- Fortran-style interleaved arrays (poisson_solver_push.f / pull.f) ----
+    def push_interleaved(self, b, offset=(0, 0, 0)):
+        """b: float64 array shaped (ext_z, ext_y, ext_x, ncomp), ncomp 1..3
+        (X; X, Y; X, Y, Z); the field box starts at offset (x, y, z)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        ext = (ctypes.c_int * 3)(b.shape[2], b.shape[1], b.shape[0])
+        off = (ctypes.c_int * 3)(*[int(v) for v in offset])
+        self._call("ps_push_interleaved", b.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), int(b.shape[3]), ext, off)
+
+    def pull_interleaved(self, a=None, b=None, offset=(0, 0, 0)):
+        """Write the solution into a and the returned right-hand side into b,
+        arrays shaped (ext_z, ext_y, ext_x, ncomp) (either may be None)."""
+        ref = a if a is not None else b
+        if ref is None:
+            return
+        for arr in (a, b):
+            if arr is not None and (arr.dtype != np.float64 or not arr.flags.c_contiguous or arr.ndim != 4
+                                    or arr.shape[:3] != ref.shape[:3]):
+                raise TypeError("interleaved arrays must be C-contiguous float64 (ext_z, ext_y, ext_x, ncomp) alike")
+        ext = (ctypes.c_int * 3)(ref.shape[2], ref.shape[1], ref.shape[0])
+        off = (ctypes.c_int * 3)(*[int(v) for v in offset])
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._call("ps_pull_interleaved", None if a is None else a.ctypes.data_as(dp), 0 if a is None else a.shape[3],
+                   None if b is None else b.ctypes.data_as(dp), 0 if b is None else b.shape[3], ext, off)
+
+    def smooth3d(self, width: float):
+        """Gaussian smoothing of the pushed fields, exp(-width^2 |k|^2 / 2), in place."""
+        self._call("ps_smooth3d", float(width))
+
     # -- device pointers (raw CUDA addresses, e.g. torch tensor.data_ptr()) --
     def push_device(self, bx, by=0, bz=0):
         self._call("ps_push_device", bx or None, by or None, bz or None)
