@@ -111,6 +111,8 @@ public:
 
     /* Extensions beyond the reference interface. */
     void set_precision(int precision) { report(ps_set_option(h_, PS_OPT_PRECISION, precision), "set_precision"); }
+    void set_kernel(int family, double width = 0.0) { report(ps_set_kernel(h_, family, width), "set_kernel"); }
+    void smooth3d(double width) { report(ps_smooth3d(h_, width), "smooth3d"); }
     int last_status() const { return status_; }
     ps_solver *handle() { return h_; }
 };

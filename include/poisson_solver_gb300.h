@@ -59,6 +59,17 @@ enum {
     PS_PREC_FP32 = 1   /* FP64 kernel build, FP32 transforms, FP64 field I/O */
 };
 
+/* Kernel families for ps_set_kernel. */
+enum {
+    PS_KERNEL_SPECTRAL = 0, /* the reference's kernels (greens3d.cpp, greens2d.cpp):
+                               spectrally truncated free-space parts, times the
+                               regularisation filter zeta of reg_order */
+    PS_KERNEL_GAUSSIAN = 1  /* extension: Gaussian-regularised kernels whose
+                               spectrum is zeta_m(s |k|) / |k|^2 exactly, sampled in
+                               real space on unbounded axes (erf in 3D, E1 in 2D,
+                               erf in 1D, plus Laguerre terms for m > 1) */
+};
+
 /* Constructor / destructor: poisson_solver::poisson_solver / ~poisson_solver
  * (poisson_solver.hpp:107-108). ps_create binds the handle to the current
  * CUDA device. */
@@ -161,6 +172,14 @@ int ps_pull_interleaved(ps_solver *h, double *a, int ncomp_a, double *b, int nco
  * cropped; a later solve3d or pull of the right-hand side sees the smoothed
  * fields. 3D handles only. */
 int ps_smooth3d(ps_solver *h, double width);
+
+/* Extension with no reference counterpart: select the kernel family.
+ * PS_KERNEL_GAUSSIAN uses order 2m = max(2, reg_order rounded up to even) and
+ * width s = width (0: twice the largest cell size, the width of the
+ * reference's filter); its returned right-hand side is filtered by
+ * zeta_m(s |k|). Applies to the next setup; on a set-up handle the kernel is
+ * rebuilt at once, as a new setup (pushed fields are dropped). */
+int ps_set_kernel(ps_solver *h, int family, double width);
 
 /* Stream the handle launches on (a cudaStream_t; NULL = legacy default). */
 int ps_set_stream(ps_solver *h, void *stream);

@@ -62,6 +62,15 @@ def _lib(kind: str) -> ctypes.CDLL:
         f = lib.oracle_smooth3d
         f.restype = ctypes.c_int
         f.argtypes = [_ip, _ip, _dp, ctypes.c_double] + [_dp] * 6
+        f = lib.oracle_gauss_green
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        f = lib.oracle_solve3d_gauss
+        f.restype = ctypes.c_int
+        f.argtypes = [_ip, _ip, _dp, ctypes.c_int, ctypes.c_double] + [ctypes.c_int] * 4 + [_dp] * 9
+        f = lib.oracle_solve2d_gauss
+        f.restype = ctypes.c_int
+        f.argtypes = [_ip, _ip, _dp, ctypes.c_int, ctypes.c_double] + [ctypes.c_int] * 3 + [_dp] * 9
     f = getattr(lib, pre + "solve2d")
     f.restype = ctypes.c_int
     f.argtypes = [_ip, _ip, _dp, ctypes.c_int] + [ctypes.c_int] * 3 + [_dp] * 9
@@ -132,10 +141,17 @@ def greens3d(ncell, bc, dx, reg: int = 0, kind: str = "port"):
     return g, (zeta.reshape(shape) if zeta is not None else None)
 
 
+def gauss_green(dim: int, m: int, s: float, r: float) -> float:
+    """The Gaussian family's free-space kernel (dimension dim, order 2m, width s) at r."""
+    return _lib("port").oracle_gauss_green(int(dim), int(m), float(s), float(r))
+
+
 def solve3d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False,
-            reproject=False, want_rhs=False, kind: str = "port"):
+            reproject=False, want_rhs=False, kind: str = "port", gauss_width: float | None = None):
     """Run setup3d/push/solve3d/pull. B: sequence of 3 arrays [Nz][Ny][Nx] or None.
 
+    gauss_width (port only): solve with the Gaussian-regularised kernel family
+    of that width (0: twice the largest cell size).
     Returns (A, RB): lists of 3 arrays or None (component not produced).
     """
     nx, ny, nz = ncell
@@ -150,8 +166,13 @@ def solve3d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False,
     nc = (ctypes.c_int * 3)(*ncell)
     b = (ctypes.c_int * 3)(*bc)
     d = (ctypes.c_double * 3)(*dx)
-    st = _fn(kind, "solve3d")(nc, b, d, int(reg), int(grad), int(div), int(curl), int(reproject),
-                              *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
+    if gauss_width is None:
+        st = _fn(kind, "solve3d")(nc, b, d, int(reg), int(grad), int(div), int(curl), int(reproject),
+                                  *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
+    else:
+        st = _lib("port").oracle_solve3d_gauss(nc, b, d, int(reg), float(gauss_width), int(grad), int(div),
+                                               int(curl), int(reproject), *[_ptr(x) for x in Bc],
+                                               *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
     if st:
         raise ValueError(f"oracle solve3d status {st}")
     # components the solve did not produce stay NaN-filled: report them as None
@@ -161,7 +182,7 @@ def solve3d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False,
 
 
 def solve2d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False, want_rhs=False,
-            kind: str = "port"):
+            kind: str = "port", gauss_width: float | None = None):
     """Run setup2d/push/solve2d/pull. B: sequence of 3 arrays [Ny][Nx] or None
     (X, Y and the out-of-plane Z). Returns (A, RB) as solve3d."""
     nx, ny = ncell
@@ -176,8 +197,13 @@ def solve2d(ncell, bc, dx, B, reg: int = 0, grad=False, div=False, curl=False, w
     nc = (ctypes.c_int * 2)(*ncell)
     b = (ctypes.c_int * 2)(*bc)
     d = (ctypes.c_double * 2)(*dx)
-    st = _fn(kind, "solve2d")(nc, b, d, int(reg), int(grad), int(div), int(curl),
-                              *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
+    if gauss_width is None:
+        st = _fn(kind, "solve2d")(nc, b, d, int(reg), int(grad), int(div), int(curl),
+                                  *[_ptr(x) for x in Bc], *[_ptr(x) for x in A], *[_ptr(x) for x in RB])
+    else:
+        st = _lib("port").oracle_solve2d_gauss(nc, b, d, int(reg), float(gauss_width), int(grad), int(div),
+                                               int(curl), *[_ptr(x) for x in Bc], *[_ptr(x) for x in A],
+                                               *[_ptr(x) for x in RB])
     if st:
         raise ValueError(f"oracle solve2d status {st}")
     A = [a if not np.isnan(a).all() else None for a in A]

@@ -221,6 +221,8 @@ double oracle_bessel_int_J0(double x)
 /* Spectral kernel (greens3d.cpp:9-547). */
 typedef struct {
     int n[3], bc[3], p[3], reg;
+    int gm;        /* Gaussian family of order 2 gm (0: the reference's kernels) */
+    double gs;     /* its width */
     double dx[3];
     cplx *ik[3];   /* spectral derivative vectors, lengths p[d] */
     double *zeta;  /* [p2][p1][p0] or NULL */
@@ -259,11 +261,70 @@ static void transform_axis(cplx *a, const int p[3], int axis, int shift, int inv
     free(pen); free(w);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Gaussian-regularised family (an extension; the reference has no such
+ * kernels): spectrum zeta_m(s|k|)/|k|^2, zeta_m(k) = e^{-a} sum_{n<m} a^n/n!,
+ * a = s^2 k^2 / 2. In d dimensions G = G_0 + sum_{n=1}^{m-1} G_n with G_0 the
+ * potential of a unit Gaussian of width s (zero added constant: G_0 tends to
+ * the free-space kernel) and
+ *   G_n(r) = s^{2-d} / (2 (2 pi)^{d/2}) e^{-u} L^{(d/2-1)}_{n-1}(u) / n,
+ * u = r^2/(2 s^2). The functions below evaluate it by other means than the
+ * GPU build does (explicit Laguerre sums, a backward continued fraction), so
+ * the two check each other; tests/test_oracle.py pins them to quadratures of
+ * the spectrum. */
+
+/* L^{(alpha)}_n(u) = sum_{i<=n} (-1)^i binom(n+alpha, n-i) u^i / i! */
+static double laguerre(int n, double alpha, double u)
+{
+    double sum = 0.0;
+    for (int i = 0; i <= n; ++i) {
+        double b = 1.0, f = 1.0;
+        for (int t = 1; t <= n - i; ++t) b *= (alpha + (double)i + (double)t) / (double)t;
+        for (int t = 1; t <= i; ++t) f *= u / (double)t;
+        sum += ((i & 1) ? -1.0 : 1.0) * b * f;
+    }
+    return sum;
+}
+
+/* ln r + E1(u)/2, u = r^2/(2 s^2): the series of E1 below u = 1 with ln r
+ * cancelled analytically; above, E1(u) = e^{-u}/(u+ 1/(1+ 1/(u+ 2/(1+ 2/(u+ ...)))))
+ * evaluated backward from a fixed depth. */
+static double log_e1_half(double r, double s)
+{
+    double u = 0.5 * (r / s) * (r / s);
+    if (u <= 1.0) {
+        double term = 1.0, sum = 0.0;
+        for (int k = 1; k < 100; ++k) {
+            term *= -u / (double)k;
+            sum += term / (double)k;
+        }
+        return 0.5 * (log(2.0 * s * s) - EULER_GAMMA - sum);
+    }
+    double t = u;
+    for (int n = 2000; n >= 1; --n) t = u + (double)n / (1.0 + (double)n / t);
+    return log(r) + 0.5 * exp(-u) / t;
+}
+
+double oracle_gauss_green(int dim, int m, double s, double r)
+{
+    double u = 0.5 * (r / s) * (r / s), tail = 0.0, g0;
+    for (int n = 1; n <= m - 1; ++n) tail += laguerre(n - 1, 0.5 * (double)dim - 1.0, u) / (double)n;
+    double kappa = pow(s, 2.0 - (double)dim) / (2.0 * pow(2.0 * PI, 0.5 * (double)dim));
+    if (dim == 3) g0 = r > 0.0 ? erf(r / (sqrt(2.0) * s)) / (4.0 * PI * r) : 1.0 / (pow(2.0 * PI, 1.5) * s);
+    else if (dim == 2) g0 = -log_e1_half(r, s) / (2.0 * PI);
+    else g0 = -0.5 * fabs(r) * erf(fabs(r) / (sqrt(2.0) * s)) - s / sqrt(2.0 * PI) * exp(-u);
+    return g0 + kappa * exp(-u) * tail;
+}
+
 /* two_d: the 2D kernel (greens2d.cpp:9-443) on a grid of one periodic
  * z-plane (ncell[2] = 1, bc[2] = 1, dx[2] <= dx[0], dx[1] so that the filter
  * width h = max(dx, dy) as greens2d.cpp:55 takes it); all four (x, y)
  * boundary combinations are allowed. */
-static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const double dx[3], int reg, int two_d)
+/* gauss_width >= 0 builds the Gaussian family instead (width 0: 2h); its
+ * zeta is the family's filter and its G already carries the regularisation,
+ * so the solve applies zeta to the returned right-hand side only. */
+static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const double dx[3], int reg, int two_d,
+                        double gauss_width)
 {
     memset(K, 0, sizeof(*K));
     for (int d = 0; d < 3; ++d) {
@@ -296,10 +357,16 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
      * a = sigma^2 |k|^2 / 2, sigma = 2h, m = reg rounded up to even. The
      * reference allocates m/2 - 1 coefficients and writes m/2 of them; this
      * keeps all m/2. */
-    if (reg > 0) {
+    if (reg > 0 || gauss_width >= 0.0) {
         int r = reg % 2 != 0 ? reg + 1 : reg;
         double sigma = 2.0 * h;
         int nc = r / 2;
+        if (gauss_width >= 0.0) {
+            if (nc < 1) nc = 1;
+            if (gauss_width > 0.0) sigma = gauss_width;
+            K->gm = nc;
+            K->gs = sigma;
+        }
         double *c = malloc(sizeof(double) * (size_t)nc);
         c[0] = 1.0;
         for (int n = 1; n <= nc - 1; ++n) c[n] = c[n - 1] * 1.0 / (double)n;
@@ -336,7 +403,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
                     double r = sqrt(x * x + y * y + z * z);
                     double rho = r / sigma;
                     double g;
-                    if (r > 0.25 * dx[0]) g = c_1_2pi2 * oracle_sine_int(rho) / r * dx[0] * dx[1] * dx[2];
+                    if (K->gm) g = oracle_gauss_green(3, K->gm, K->gs, r) * dx[0] * dx[1] * dx[2];
+                    else if (r > 0.25 * dx[0]) g = c_1_2pi2 * oracle_sine_int(rho) / r * dx[0] * dx[1] * dx[2];
                     else g = c_1_2pi2 / sigma * dx[0] * dx[1] * dx[2];
                     G[((size_t)k * p[1] + j) * p[0] + i] = CMPLX(g, 0.0);
                 }
@@ -356,7 +424,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         for (int k = 0; k < n; ++k) {
             double z = zmin + (double)k * dx[2];
             double rho = fabs(z) / sigma;
-            pen[k] = CMPLX(-C1 * (oracle_sine_int(rho) * rho + cos(rho)) * dx[2], 0.0);
+            pen[k] = CMPLX(K->gm ? oracle_gauss_green(1, K->gm, K->gs, z) * dx[2]
+                                 : -C1 * (oracle_sine_int(rho) * rho + cos(rho)) * dx[2], 0.0);
         }
         fft_shift(pen, n);
         glassman(pen, w, n, 0);
@@ -365,8 +434,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
                 for (int i = 0; i < p[0]; ++i) {
                     size_t q = ((size_t)k * p[1] + j) * p[0] + i;
                     if (i == 0 && j == 0) G[q] = pen[k];
-                    else G[q] = -1.0 / (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j] +
-                                        K->ik[2][k] * K->ik[2][k]);
+                    else G[q] = -(K->gm ? K->zeta[q] : 1.0) /
+                                 (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j] + K->ik[2][k] * K->ik[2][k]);
                 }
         free(pen); free(w);
     } else if (b0 == 0 && b1 == 0 && b2 == 1) {
@@ -388,7 +457,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
                 double x = xmin0 + (double)i * dx[0];
                 double r = sqrt(x * x + y * y);
                 double rho = r / sigma;
-                G2[(size_t)j * p[0] + i] = CMPLX(-c_1_2pi * (oracle_bessel_int_J0(rho) + C2) * dx[0] * dx[1], 0.0);
+                G2[(size_t)j * p[0] + i] = CMPLX(K->gm ? oracle_gauss_green(2, K->gm, K->gs, r) * dx[0] * dx[1]
+                                                       : -c_1_2pi * (oracle_bessel_int_J0(rho) + C2) * dx[0] * dx[1], 0.0);
             }
         }
         transform_axis(G2, p2, 0, 1, 0);
@@ -398,8 +468,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
                 for (int i = 0; i < p[0]; ++i) {
                     size_t q = ((size_t)k * p[1] + j) * p[0] + i;
                     if (k == 0) G[q] = G2[(size_t)j * p[0] + i];
-                    else G[q] = -1.0 / (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j] +
-                                        K->ik[2][k] * K->ik[2][k]);
+                    else G[q] = -(K->gm ? K->zeta[q] : 1.0) /
+                                 (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j] + K->ik[2][k] * K->ik[2][k]);
                 }
         free(G2);
     } else if (b0 != b1) {
@@ -417,7 +487,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         for (int m = 0; m < n; ++m) {
             double s = umin + (double)m * dx[u];
             double rho = fabs(s) / sigma;
-            pen[m] = CMPLX(-C1 * (oracle_sine_int(rho) * rho + cos(rho)) * dx[u], 0.0);
+            pen[m] = CMPLX(K->gm ? oracle_gauss_green(1, K->gm, K->gs, s) * dx[u]
+                                 : -C1 * (oracle_sine_int(rho) * rho + cos(rho)) * dx[u], 0.0);
         }
         fft_shift(pen, n);
         glassman(pen, w, n, 0);
@@ -425,7 +496,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
             for (int i = 0; i < p[0]; ++i) {
                 size_t q = (size_t)j * p[0] + i;
                 if (u == 1 ? i == 0 : j == 0) G[q] = pen[u == 1 ? j : i];
-                else G[q] = -1.0 / (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j]);
+                else G[q] = -(K->gm ? K->zeta[q] : 1.0) / (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j]);
             }
         free(pen); free(w);
     } else {
@@ -435,8 +506,8 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
                 for (int i = 0; i < p[0]; ++i) {
                     size_t q = ((size_t)k * p[1] + j) * p[0] + i;
                     if (i == 0 && j == 0 && k == 0) G[q] = CMPLX(0.0, 0.0);
-                    else G[q] = -1.0 / (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j] +
-                                        K->ik[2][k] * K->ik[2][k]);
+                    else G[q] = -(K->gm ? K->zeta[q] : 1.0) /
+                                 (K->ik[0][i] * K->ik[0][i] + K->ik[1][j] * K->ik[1][j] + K->ik[2][k] * K->ik[2][k]);
                 }
     }
     return 0;
@@ -446,7 +517,7 @@ int oracle_greens3d(const int ncell[3], const int bc[3], const double dx[3], int
                     double *g_re, double *g_im, double *zeta, int pext[3])
 {
     kernel_t K;
-    int st = kernel_build(&K, ncell, bc, dx, reg, 0);
+    int st = kernel_build(&K, ncell, bc, dx, reg, 0, -1.0);
     if (st) { kernel_free(&K); return st; }
     size_t np = (size_t)K.p[0] * K.p[1] * K.p[2];
     for (int d = 0; d < 3; ++d) pext[d] = K.p[d];
@@ -482,7 +553,7 @@ int oracle_solve3d(const int ncell[3], const int bc[3], const double dx[3], int 
  * grid of one periodic z-plane (see kernel_build): the z transforms are then
  * of length one and ikZ = 0, so the 3D data flow is the 2D one
  * (solve2d.cpp:8-475); only the output selection differs. */
-static int solve_core(const int ncell[3], const int bc[3], const double dx[3], int reg,
+static int solve_core(const int ncell[3], const int bc[3], const double dx[3], int reg, double gauss_width,
                       int grad, int div, int curl, int reproject, int two_d,
                       const double *bx, const double *by, const double *bz,
                       double *ax, double *ay, double *az,
@@ -528,7 +599,7 @@ static int solve_core(const int ncell[3], const int bc[3], const double dx[3], i
     }
 
     kernel_t K;
-    int st = kernel_build(&K, ncell, bc, dx, reg, two_d);
+    int st = kernel_build(&K, ncell, bc, dx, reg, two_d, gauss_width);
     if (st) { kernel_free(&K); return st; }
     double t1 = now_s();
 
@@ -593,7 +664,7 @@ static int solve_core(const int ncell[3], const int bc[3], const double dx[3], i
             const cplx *gY = (r[1] && !two_d) ? pr[1] : pr[0], *gZ = r[2] ? pr[2] : pr[0];
             for (int k = 0; k < nfft; ++k) {
                 size_t q = ((size_t)k * py + j) * px + i;
-                if (reg > 0)
+                if (K.zeta && !K.gm)
                     for (int c = 0; c < 3; ++c)
                         if (r[c]) pr[c][k] *= K.zeta[q];
                 cplx G = K.G[q];
@@ -625,8 +696,14 @@ static int solve_core(const int ncell[3], const int bc[3], const double dx[3], i
                     for (int c = 0; c < 3; ++c)
                         if (l[c]) pl[c][k] = G * pr[c][k];
                 }
-                if (reproject && r[0] && r[1] && r[2]) {
-                    cplx div_psi = G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k] + ikZ[k] * pr[2][k]);
+                /* the Gaussian family filters the returned right-hand side after
+                 * the kernel has acted on the unfiltered one */
+                const int rp = reproject && r[0] && r[1] && r[2];
+                cplx div_psi = rp ? G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k] + ikZ[k] * pr[2][k]) : 0.0;
+                if (K.gm)
+                    for (int c = 0; c < 3; ++c)
+                        if (r[c]) pr[c][k] *= K.zeta[q];
+                if (rp) {
                     pr[0][k] += ikX[i] * div_psi;
                     pr[1][k] += ikY[j] * div_psi;
                     pr[2][k] += ikZ[k] * div_psi;
@@ -702,8 +779,19 @@ int oracle_solve3d_timed(const int ncell[3], const int bc[3], const double dx[3]
                          double *ax, double *ay, double *az,
                          double *rbx, double *rby, double *rbz, double seconds[3])
 {
-    return solve_core(ncell, bc, dx, reg, grad, div, curl, reproject, 0, bx, by, bz, ax, ay, az, rbx, rby, rbz,
+    return solve_core(ncell, bc, dx, reg, -1.0, grad, div, curl, reproject, 0, bx, by, bz, ax, ay, az, rbx, rby, rbz,
                       seconds);
+}
+
+int oracle_solve3d_gauss(const int ncell[3], const int bc[3], const double dx[3], int reg, double width,
+                         int grad, int div, int curl, int reproject,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz)
+{
+    if (!(width >= 0.0)) return 1;
+    return solve_core(ncell, bc, dx, reg, width, grad, div, curl, reproject, 0, bx, by, bz, ax, ay, az, rbx, rby,
+                      rbz, NULL);
 }
 
 int oracle_solve2d(const int ncell[2], const int bc[2], const double dx[2], int reg,
@@ -715,7 +803,20 @@ int oracle_solve2d(const int ncell[2], const int bc[2], const double dx[2], int 
     const int nc3[3] = {ncell[0], ncell[1], 1};
     const int bc3[3] = {bc[0], bc[1], 1};
     const double dx3[3] = {dx[0], dx[1], fmin(dx[0], dx[1])};
-    return solve_core(nc3, bc3, dx3, reg, grad, div, curl, 0, 1, bx, by, bz, ax, ay, az, rbx, rby, rbz, NULL);
+    return solve_core(nc3, bc3, dx3, reg, -1.0, grad, div, curl, 0, 1, bx, by, bz, ax, ay, az, rbx, rby, rbz, NULL);
+}
+
+int oracle_solve2d_gauss(const int ncell[2], const int bc[2], const double dx[2], int reg, double width,
+                         int grad, int div, int curl,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz)
+{
+    const int nc3[3] = {ncell[0], ncell[1], 1};
+    const int bc3[3] = {bc[0], bc[1], 1};
+    const double dx3[3] = {dx[0], dx[1], fmin(dx[0], dx[1])};
+    if (!(width >= 0.0)) return 1;
+    return solve_core(nc3, bc3, dx3, reg, width, grad, div, curl, 0, 1, bx, by, bz, ax, ay, az, rbx, rby, rbz, NULL);
 }
 
 /* ------------------------------------------------------------------------ */

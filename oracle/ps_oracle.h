@@ -65,6 +65,26 @@ int oracle_smooth3d(const int ncell[3], const int bc[3], const double dx[3], dou
                     const double *bx, const double *by, const double *bz,
                     double *ox, double *oy, double *oz);
 
+/* Gaussian-regularised kernel family (an extension with no reference
+ * counterpart): the d-dimensional (dim = 1, 2, 3) free-space kernel of order
+ * 2m and width s at distance r, whose spectrum is zeta_m(s|k|)/|k|^2. */
+double oracle_gauss_green(int dim, int m, double s, double r);
+
+/* oracle_solve3d / oracle_solve2d with the Gaussian family of order
+ * max(2, reg rounded up to even) and width `width` (0: twice the largest cell
+ * size); the returned right-hand side is filtered by zeta_m. Returns 1 for a
+ * negative width, else as oracle_solve3d. */
+int oracle_solve3d_gauss(const int ncell[3], const int bc[3], const double dx[3], int reg, double width,
+                         int grad, int div, int curl, int reproject,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz);
+int oracle_solve2d_gauss(const int ncell[2], const int bc[2], const double dx[2], int reg, double width,
+                         int grad, int div, int curl,
+                         const double *bx, const double *by, const double *bz,
+                         double *ax, double *ay, double *az,
+                         double *rbx, double *rby, double *rbz);
+
 #ifdef __cplusplus
 }
 #endif

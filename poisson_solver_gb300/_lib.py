@@ -31,6 +31,9 @@ PS_OPT_PASS_TIMING = 5
 PS_PREC_FP64 = 0
 PS_PREC_FP32 = 1
 
+PS_KERNEL_SPECTRAL = 0
+PS_KERNEL_GAUSSIAN = 1
+
 PS_INFO_PADDED_X = 0
 PS_INFO_PADDED_Y = 1
 PS_INFO_PADDED_Z = 2
@@ -64,6 +67,7 @@ SIGNATURES = {
     "ps_push_interleaved": (_i, [_vp, _dp, _i, _ip, _ip]),
     "ps_pull_interleaved": (_i, [_vp, _dp, _i, _dp, _i, _ip, _ip]),
     "ps_smooth3d": (_i, [_vp, ctypes.c_double]),
+    "ps_set_kernel": (_i, [_vp, _i, ctypes.c_double]),
     "ps_solve3d": (_i, [_vp]),
     "ps_pull": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "ps_push_device": (_i, [_vp, _dp, _dp, _dp]),

@@ -173,6 +173,11 @@ int ps_smooth3d(ps_solver *h, double width)
     return guarded(h, [&](ps::Solver &s) { s.smooth3d(width); });
 }
 
+int ps_set_kernel(ps_solver *h, int family, double width)
+{
+    return guarded(h, [&](ps::Solver &s) { s.set_kernel(family, width); });
+}
+
 int ps_set_stream(ps_solver *h, void *stream)
 {
     return guarded(h, [&](ps::Solver &s) { s.stream = (cudaStream_t)stream; });

@@ -143,12 +143,95 @@ __device__ double bessel_int_j0(double x)
     return sqrt(2.0 / (PI * x)) / x * fac + EULER_GAMMA + log(0.5 * x);
 }
 
+// ---------------------------------------------------------------------------
+// Gaussian-regularised family of order 2m and width s (an extension with no
+// counterpart in the reference). Its spectrum is zeta_m(s|k|)/|k|^2 with the
+// reference's filter zeta_m(k) = e^{-a} sum_{n<m} a^n/n!, a = s^2 k^2/2, so
+// in d dimensions G = G_0 + sum_{n=1}^{m-1} G_n, where G_0 is the potential of
+// a unit Gaussian of width s and, with u = r^2/(2 s^2),
+//   G_n(r) = s^{2-d} / (2 (2 pi)^{d/2}) e^{-u} L^{(d/2-1)}_{n-1}(u) / n
+// (generalised Laguerre polynomials). G_0 is erf(r/(sqrt2 s))/(4 pi r) in 3D,
+// -(ln r + E1(u)/2)/(2 pi) in 2D and -|z| erf(|z|/(sqrt2 s))/2 -
+// s e^{-u}/sqrt(2 pi) in 1D, each tending to the free-space kernel at
+// infinity with no added constant.
+
+// sum_{n=1}^{m-1} L^{(alpha)}_{n-1}(u) / n by the three-term recurrence
+// (k+1) L_{k+1} = (2k+1+alpha-u) L_k - (k+alpha) L_{k-1}.
+__device__ double laguerre_tail(int m, double alpha, double u)
+{
+    double s = 0.0, lp = 0.0, l = 1.0;
+    for (int n = 1; n <= m - 1; ++n) {
+        s += l / (double)n;
+        const double k = (double)(n - 1);
+        const double nx = ((2.0 * k + 1.0 + alpha - u) * l - (k + alpha) * lp) / (k + 1.0);
+        lp = l;
+        l = nx;
+    }
+    return s;
+}
+
+// sum_{k>=1} (-u)^k / (k k!), the power series of -gamma - ln u - E1(u).
+__device__ double e1_series(double u)
+{
+    double term = 1.0, sum = 0.0;
+    for (int k = 1; k < 80; ++k) {
+        term *= -u / (double)k;
+        const double d = term / (double)k;
+        sum += d;
+        if (fabs(d) <= 1e-17 * fabs(sum)) break;
+    }
+    return sum;
+}
+
+// ln r + E1(r^2/(2 s^2))/2. For u <= 1 by the series, written so that ln r
+// cancels analytically (the value at r = 0 is (ln(2 s^2) - gamma)/2); above,
+// E1 by the continued fraction e^{-u}/(u+1- 1/(u+3- 4/(u+5- ...))) evaluated
+// with the modified Lentz method.
+__device__ double log_e1_half(double r, double s)
+{
+    const double u = 0.5 * (r / s) * (r / s);
+    if (u <= 1.0) return 0.5 * (log(2.0 * s * s) - EULER_GAMMA - e1_series(u));
+    double b = u + 1.0, c = 1.0e300, d = 1.0 / b, h = d;
+    for (int i = 1; i < 300; ++i) {
+        const double an = -(double)i * (double)i;
+        b += 2.0;
+        d = 1.0 / (an * d + b);
+        c = b + an / c;
+        const double del = c * d;
+        h *= del;
+        if (fabs(del - 1.0) < 1e-16) break;
+    }
+    return log(r) + 0.5 * h * exp(-u);
+}
+
+__device__ double gauss_green3(double r, int m, double s)
+{
+    const double u = 0.5 * (r / s) * (r / s);
+    const double inv_2pi_32 = 1.0 / ((2.0 * PI) * sqrt(2.0 * PI));
+    const double g0 = r > 0.0 ? erf(r / (sqrt(2.0) * s)) / (4.0 * PI * r) : inv_2pi_32 / s;
+    return g0 + 0.5 * inv_2pi_32 / s * exp(-u) * laguerre_tail(m, 0.5, u);
+}
+
+__device__ double gauss_green2(double r, int m, double s)
+{
+    const double u = 0.5 * (r / s) * (r / s);
+    return -log_e1_half(r, s) / (2.0 * PI) + exp(-u) * laguerre_tail(m, 0.0, u) / (4.0 * PI);
+}
+
+__device__ double gauss_green1(double z, int m, double s)
+{
+    const double a = fabs(z), u = 0.5 * (a / s) * (a / s);
+    const double c = s / sqrt(2.0 * PI);
+    return -0.5 * a * erf(a / (sqrt(2.0) * s)) - c * exp(-u) + 0.5 * c * exp(-u) * laguerre_tail(m, -0.5, u);
+}
+
 // 3D unbounded kernel, spectrally truncated: G(r) = Si(r/sigma)/(2 pi^2 r) dV,
 // sigma = h/pi, h = max dx; 1/(2 pi^2 sigma) dV at the origin
 // (greens3d.cpp:193-225). Octant index i' is the half-swapped grid index, so
 // the sample sits at x = -(P/2) dx + (i' + P/2) dx as the reference forms it.
+// With gf.gm >= 1 the samples are the Gaussian family's gauss_green3 dV.
 __global__ void k_sample_unbounded3d(double *oct, int ox, int oy, int oz, int P0, int P1, int P2,
-                                     double dx0, double dx1, double dx2)
+                                     double dx0, double dx1, double dx2, GaussFamily gf)
 {
     const long long n = (long long)ox * oy * oz;
     const double h = fmax(fmax(dx0, dx1), dx2);
@@ -163,15 +246,18 @@ __global__ void k_sample_unbounded3d(double *oct, int ox, int oy, int oz, int P0
         const double z = xmin2 + (double)(k + P2 / 2) * dx2;
         const double r = sqrt(x * x + y * y + z * z);
         double g;
-        if (r > 0.25 * dx0) g = c * sine_int(r / sigma) / r * dx0 * dx1 * dx2;
+        if (gf.gm > 0) g = gauss_green3(r, gf.gm, gf.gs) * dx0 * dx1 * dx2;
+        else if (r > 0.25 * dx0) g = c * sine_int(r / sigma) / r * dx0 * dx1 * dx2;
         else g = c / sigma * dx0 * dx1 * dx2;
         oct[q] = g;
     }
 }
 
 // 2D unbounded kernel -(1/2 pi)(Ji0(r/sigma) + ln(2 sigma) - gamma) dx dy,
-// sigma = max(dx, dy)/pi (greens2d.cpp:157-202).
-__global__ void k_sample_unbounded2d(double *oct, int ox, int oy, int P0, int P1, double dx0, double dx1)
+// sigma = max(dx, dy)/pi (greens2d.cpp:157-202); with gf.gm >= 1 the
+// Gaussian family's gauss_green2 dx dy.
+__global__ void k_sample_unbounded2d(double *oct, int ox, int oy, int P0, int P1, double dx0, double dx1,
+                                     GaussFamily gf)
 {
     const long long n = (long long)ox * oy;
     const double sigma = fmax(dx0, dx1) / PI;
@@ -183,7 +269,7 @@ __global__ void k_sample_unbounded2d(double *oct, int ox, int oy, int P0, int P1
         const double x = xmin0 + (double)(i + P0 / 2) * dx0;
         const double y = xmin1 + (double)(j + P1 / 2) * dx1;
         const double r = sqrt(x * x + y * y);
-        oct[q] = -c * (bessel_int_j0(r / sigma) + C2) * dx0 * dx1;
+        oct[q] = gf.gm > 0 ? gauss_green2(r, gf.gm, gf.gs) * dx0 * dx1 : -c * (bessel_int_j0(r / sigma) + C2) * dx0 * dx1;
     }
 }
 
@@ -192,7 +278,8 @@ __global__ void k_sample_unbounded2d(double *oct, int ox, int oy, int P0, int P1
 // sigma = dz/pi (greens3d.cpp:361-373), sampled at z = -(Pz/2) dz + k dz and
 // half-swapped. The samples are even, so the transform is the real cosine sum
 // G1[k] = g0 + (-1)^k g_{P/2} + 2 sum_{0<m<P/2} g_m cos(2 pi k m / P).
-__global__ void k_line_ppf(double *line, int P, double dz)
+// With gf.gm >= 1 the samples are the Gaussian family's gauss_green1 dz.
+__global__ void k_line_ppf(double *line, int P, double dz, GaussFamily gf)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > P / 2) return;
@@ -200,6 +287,7 @@ __global__ void k_line_ppf(double *line, int P, double dz)
     const double zmin = -(0.5 * (double)P) * dz;
     auto g = [&](int m) {
         const double z = zmin + (double)(m + P / 2) * dz;
+        if (gf.gm > 0) return gauss_green1(z, gf.gm, gf.gs) * dz;
         const double rho = fabs(z) / sigma;
         return -C1 * (sine_int(rho) * rho + cos(rho)) * dz;
     };
@@ -229,16 +317,28 @@ __global__ void k_kernel_fill(const KernelFillArgs a)
         const int kx = (int)(q % a.Mx), ky = (int)((q / a.Mx) % a.oy), kz = (int)(q / ((long long)a.Mx * a.oy));
         const double fx = wn(kx, a.P[0], a.dx[0]), fy = wn(ky, a.P[1], a.dx[1]), fz = wn(kz, a.P[2], a.dx[2]);
         const double k2 = fx * fx + fy * fy + fz * fz;
+        // zeta_m(s |k|) of the Gaussian family: the spectral part of its kernel and its RHS filter
+        double zg = 1.0;
+        if (a.gauss.gm > 0) {
+            const double arg = 0.5 * a.gauss.gs * a.gauss.gs * k2;
+            double t = 1.0, sum = 1.0;
+            for (int m = 1; m <= a.gauss.gm - 1; ++m) {
+                t *= arg / (double)m;
+                sum += t;
+            }
+            zg = sum * exp(-arg);
+        }
+        const double inv = zg / k2;
         double g = 0.0;
         if (a.kern) {
             switch (a.kind) {
             case 0: g = a.spec[((long long)kz * a.P[1] + ky) * a.Mx + kx].x; break;
-            case 1: g = (kx == 0 && ky == 0) ? a.line[kz] : 1.0 / k2; break;
-            case 2: g = (kz == 0) ? a.plane[(long long)ky * a.Mx + kx].x : 1.0 / k2; break;
+            case 1: g = (kx == 0 && ky == 0) ? a.line[kz] : inv; break;
+            case 2: g = (kz == 0) ? a.plane[(long long)ky * a.Mx + kx].x : inv; break;
             // 2D mixed (greens2d.cpp:316-440): the zero-wavenumber line of the periodic axis
-            case 4: g = (kx == 0) ? a.line[ky] : 1.0 / k2; break;  // x periodic, y unbounded
-            case 5: g = (ky == 0) ? a.line[kx] : 1.0 / k2; break;  // x unbounded, y periodic
-            default: g = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : 1.0 / k2; break;
+            case 4: g = (kx == 0) ? a.line[ky] : inv; break;  // x periodic, y unbounded
+            case 5: g = (ky == 0) ? a.line[kx] : inv; break;  // x unbounded, y periodic
+            default: g = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : inv; break;
             }
         }
         // zeta = e^{-a} sum_{n < r/2} a^n / n!, a = sigma^2 |k|^2 / 2 (greens3d.cpp:123-159);
@@ -246,6 +346,11 @@ __global__ void k_kernel_fill(const KernelFillArgs a)
         double zeta = 1.0;
         if (a.smooth) {
             zeta = exp(-0.5 * a.smooth_sigma * a.smooth_sigma * k2);
+        } else if (a.gauss.gm > 0) {
+            // the family's kernel carries its regularisation; zeta filters the returned RHS
+            if (a.kern) a.kern[q] = g / a.norm;
+            if (a.zeta_out) a.zeta_out[q] = zg / a.norm;
+            continue;
         } else if (a.reg > 0) {
             const double arg = 0.5 * sigma * sigma * k2;
             double c = 1.0, p = 1.0, sum = 1.0;
@@ -277,26 +382,26 @@ unsigned grid_for(long long n, int threads)
 }  // namespace
 
 cudaError_t launch_sample_unbounded3d(double *oct, const int oext[3], const int P[3], const double dx[3],
-                                      cudaStream_t st)
+                                      GaussFamily gf, cudaStream_t st)
 {
     const long long n = (long long)oext[0] * oext[1] * oext[2];
     k_sample_unbounded3d<<<grid_for(n, 256), 256, 0, st>>>(oct, oext[0], oext[1], oext[2], P[0], P[1], P[2], dx[0],
-                                                             dx[1], dx[2]);
+                                                             dx[1], dx[2], gf);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sample_unbounded2d(double *oct, const int oext[2], const int P[2], const double dx[2],
-                                      cudaStream_t st)
+                                      GaussFamily gf, cudaStream_t st)
 {
     const long long n = (long long)oext[0] * oext[1];
-    k_sample_unbounded2d<<<grid_for(n, 256), 256, 0, st>>>(oct, oext[0], oext[1], P[0], P[1], dx[0], dx[1]);
+    k_sample_unbounded2d<<<grid_for(n, 256), 256, 0, st>>>(oct, oext[0], oext[1], P[0], P[1], dx[0], dx[1], gf);
     return cudaGetLastError();
 }
 
-cudaError_t launch_line_ppf(double *line, int P, double dz, cudaStream_t st)
+cudaError_t launch_line_ppf(double *line, int P, double dz, GaussFamily gf, cudaStream_t st)
 {
     const int n = P / 2 + 1;
-    k_line_ppf<<<(n + 127) / 128, 128, 0, st>>>(line, P, dz);
+    k_line_ppf<<<(n + 127) / 128, 128, 0, st>>>(line, P, dz, gf);
     return cudaGetLastError();
 }
 

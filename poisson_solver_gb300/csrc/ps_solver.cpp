@@ -378,6 +378,28 @@ void Solver::set_option(int option, int value)
     }
 }
 
+void Solver::set_kernel(int family, double width)
+{
+    if (family != PS_KERNEL_SPECTRAL && family != PS_KERNEL_GAUSSIAN) throw Error(PS_ERR_ARGUMENT, "unknown kernel family");
+    if (!(width >= 0.0) || !std::isfinite(width)) throw Error(PS_ERR_ARGUMENT, "kernel width must be finite and >= 0");
+    kernel_family = family;
+    gauss_width = width;
+    if (is_setup) {
+        is_setup = false;
+        finish_setup();
+    }
+}
+
+GaussFamily Solver::gauss_family() const
+{
+    GaussFamily g{0, 0.0};
+    if (kernel_family != PS_KERNEL_GAUSSIAN) return g;
+    const int r = (reg % 2 != 0) ? reg + 1 : reg;
+    g.gm = std::max(1, r / 2);
+    g.gs = gauss_width > 0.0 ? gauss_width : 2.0 * std::max(std::max(dx[0], dx[1]), dx[2]);
+    return g;
+}
+
 int Solver::get_option(int option) const
 {
     switch (option) {
@@ -409,6 +431,7 @@ void Solver::build_kernel()
     }
     fa.reg = reg;
     fa.norm = (double)P[0] * (double)P[1] * (double)P[2];
+    fa.gauss = gauss_family();
     const int b0 = bc[0], b1 = bc[1], b2 = bc[2];
     if (dims == 3)
         fa.kind = (b0 == 0 && b1 == 0 && b2 == 0) ? 0 : (b0 == 1 && b1 == 1 && b2 == 0) ? 1 : (b2 == 1 && b0 == 0) ? 2 : 3;
@@ -426,11 +449,11 @@ void Solver::build_kernel()
         oct.ensure((size_t)ox * oy * ozs * sizeof(double));
         if (three) {
             const int oext[3] = {ox, oy, oz};
-            PS_CK(launch_sample_unbounded3d((double *)oct.p, oext, P, dx, stream));
+            PS_CK(launch_sample_unbounded3d((double *)oct.p, oext, P, dx, fa.gauss, stream));
         } else {
             const int oext[2] = {ox, oy}, P2[2] = {P[0], P[1]};
             const double dx2[2] = {dx[0], dx[1]};
-            PS_CK(launch_sample_unbounded2d((double *)oct.p, oext, P2, dx2, stream));
+            PS_CK(launch_sample_unbounded2d((double *)oct.p, oext, P2, dx2, fa.gauss, stream));
         }
         spec.ensure((size_t)pz * P[1] * Mx * sizeof(double2));
         XFwdArgs xa{};
@@ -490,7 +513,7 @@ void Solver::build_kernel()
         // unbounded), y (2D x-periodic) or x (2D y-periodic)
         const int u = fa.kind == 1 ? 2 : fa.kind == 4 ? 1 : 0;
         line.ensure((size_t)(P[u] / 2 + 1) * sizeof(double));
-        PS_CK(launch_line_ppf((double *)line.p, P[u], dx[u], stream));
+        PS_CK(launch_line_ppf((double *)line.p, P[u], dx[u], fa.gauss, stream));
         fa.line = (const double *)line.p;
     }
     PS_CK(launch_kernel_fill(fa, stream));
@@ -532,6 +555,7 @@ void Solver::ensure_zeta(int prec)
         }
         fa.reg = reg;
         fa.norm = (double)P[0] * (double)P[1] * (double)P[2];
+        fa.gauss = gauss_family();
         PS_CK(launch_kernel_fill(fa, stream));
     }
     if (prec == PREC_FP32 && !zeta32.p) {
@@ -1194,9 +1218,10 @@ void Solver::solve_internal(int want_dims)
 void Solver::returned_rhs(const double *out[3])
 {
     // the reference returns B after its forward/inverse round trip, i.e.
-    // B itself unless the regulariser or the reprojection changed it
+    // B itself unless the regulariser or the reprojection changed it (the
+    // Gaussian family always filters)
     const size_t bytes = field_elems() * sizeof(double);
-    const bool filtered = reg > 0 || (opt_reproject && pushed == 7 && dims == 3);
+    const bool filtered = reg > 0 || kernel_family == PS_KERNEL_GAUSSIAN || (opt_reproject && pushed == 7 && dims == 3);
     if (filtered && !rhs_ready) {
         const double *Bin[3];
         double *Rout[3];

@@ -69,6 +69,11 @@ struct Solver {
     int n[3] = {0, 0, 0}, bc[3] = {0, 0, 0}, P[3] = {0, 0, 0};
     double dx[3] = {0, 0, 0};
     int reg = 0;
+    // Kernel family: PS_KERNEL_SPECTRAL (the reference's) or PS_KERNEL_GAUSSIAN
+    // of order max(2, reg rounded up to even) and width gauss_width (0: twice
+    // the largest cell size, the width of the reference's filter).
+    int kernel_family = 0;
+    double gauss_width = 0.0;
     int Mx = 0, oy = 0, oz = 0;  // half-spectrum length and kernel octant extents
     int ldx = 0;                 // row pitch of the spectra work[c] (Mx rounded up to even)
     int kzp = 0;                 // z pitch of kernzf32 (oz rounded up to a multiple of 4)
@@ -111,6 +116,12 @@ struct Solver {
     void finish_setup();  // buffers and the kernel once n, bc, dx, P, reg are set
     void set_option(int option, int value);
     int get_option(int option) const;
+    // Select the kernel family; on a set-up handle the kernel is rebuilt
+    // (as a new setup: pushed fields are dropped).
+    void set_kernel(int family, double width);
+    // The family's order m (zeta_m) and width for the current setup; m = 0
+    // for the spectral family.
+    GaussFamily gauss_family() const;
 
     // Device-pointer pipeline. B: input components (NULL = absent); A: outputs.
     // Returns the mask of components written to A.

@@ -209,12 +209,20 @@ cudaError_t launch_xiq(const XInvArgs &a, cudaStream_t st);
 }  // namespace wide
 
 // Kernel-build helpers (ps_greens.cu), all FP64.
+// Kernel family of the build: gm = 0 is the reference's spectrally truncated
+// kernel (Si, Ji0) with the zeta filter; gm >= 1 is the Gaussian-regularised
+// family of order 2 gm and width gs, whose spectrum is zeta_gm(gs |k|) / |k|^2.
+struct GaussFamily {
+    int gm;
+    double gs;
+};
 cudaError_t launch_sample_unbounded3d(double *oct, const int oext[3], const int P[3], const double dx[3],
-                                      cudaStream_t st);
+                                      GaussFamily gf, cudaStream_t st);
 cudaError_t launch_sample_unbounded2d(double *oct, const int oext[2], const int P[2], const double dx[2],
-                                      cudaStream_t st);
-// Spectrum G1[k], k <= P/2, of the 1D kernel of the periodic-periodic-unbounded domain.
-cudaError_t launch_line_ppf(double *line, int P, double dz, cudaStream_t st);
+                                      GaussFamily gf, cudaStream_t st);
+// Spectrum G1[k], k <= P/2, of the 1D kernel along an unbounded axis whose
+// cross-section is periodic.
+cudaError_t launch_line_ppf(double *line, int P, double dz, GaussFamily gf, cudaStream_t st);
 // Octant of K = G zeta / norm from the kernel spectrum (kind 0), or from
 // 1/|k|^2 with the plane/line overrides of the mixed domains.
 struct KernelFillArgs {
@@ -232,6 +240,8 @@ struct KernelFillArgs {
     double norm;
     int smooth;           // zeta_out = exp(-smooth_sigma^2 |k|^2 / 2) / norm (the smooth3d
     double smooth_sigma;  // filter) in place of the regularisation filter
+    GaussFamily gauss;    // gm >= 1: the Gaussian-regularised family (kern = its spectrum,
+                          // zeta_out = zeta_gm(gs |k|) / norm)
 };
 cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st);
 // Fields with interleaved components (ps_fields.cu): packed [nz][ny][nx][ncomp]

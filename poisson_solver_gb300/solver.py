@@ -128,6 +128,14 @@ class PoissonSolver:
     def set_stream(self, stream_handle: int):
         self._call("ps_set_stream", ctypes.c_void_p(int(stream_handle)))
 
+    def set_kernel(self, family: str, width: float = 0.0):
+        """'spectral' (the reference's kernels, default) or 'gaussian': the
+        Gaussian-regularised kernels of order max(2, reg_order) and width
+        `width` (0: twice the largest cell size). On a set-up handle the
+        kernel is rebuilt as a new setup."""
+        v = {"spectral": L.PS_KERNEL_SPECTRAL, "gaussian": L.PS_KERNEL_GAUSSIAN}[family]
+        self._call("ps_set_kernel", v, float(width))
+
     # -- host push / solve / pull ----------------------------------------
     def push(self, bx, by=None, bz=None):
         s = self._shape
@@ -325,11 +333,12 @@ class PoissonBatch:
 
 
 def solve2d(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,
-            precision="fp64", want_rhs=False):
+            precision="fp64", want_rhs=False, kernel="spectral", width=0.0):
     """One-shot host 2D solve; B: 3 arrays [Ny][Nx] or None (X, Y, Z).
     Returns (A, RB) lists of 3 arrays or None."""
     shape = (ncell[1], ncell[0])
     with PoissonSolver() as ps:
+        ps.set_kernel(kernel, width)
         ps.setup2d(ncell, bc, dx, reg_order)
         ps.set_return_grad(grad)
         ps.set_return_div(div)
@@ -348,10 +357,11 @@ def solve2d(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,
 
 
 def solve(ncell, bc, dx, B, reg_order=0, grad=False, div=False, curl=False,
-          reproject=False, precision="fp64", want_rhs=False):
+          reproject=False, precision="fp64", want_rhs=False, kernel="spectral", width=0.0):
     """One-shot host solve; returns (A, RB) lists of 3 arrays or None."""
     shape = (ncell[2], ncell[1], ncell[0])
     with PoissonSolver() as ps:
+        ps.set_kernel(kernel, width)
         ps.setup3d(ncell, bc, dx, reg_order)
         ps.set_return_grad(grad)
         ps.set_return_div(div)
