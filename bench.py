@@ -10,7 +10,11 @@ Gaussian-cored vortex rings. One step = one solve of that problem.
              transform solve of the same inputs is reported beside it with the
              relative L2 difference between the two
   e2e        the same metric through the public C-ABI push/solve3d/pull with
-             pinned HOST buffers, both copies inside the timed region
+             pinned HOST buffers, both copies of every step inside the timed
+             region: three handles, each on its own stream and host thread,
+             take the steps in turn, so one step's copies overlap another's
+             solve and the two copy directions overlap (serial_value: one
+             handle, no overlap)
   roofline   the dominant kernel's algorithmic bytes per launch over its
              CUDA-event duration, against the measured HBM copy bandwidth
   cpu_baseline / --impl reference
@@ -286,6 +290,61 @@ def max_over_ranks(pg, value):
     return float(t.item())
 
 
+def e2e_handles(psg, setup, Bn, steps, pg, nh=3):
+    """Throughput of `steps` host-buffer solves (blocking ps_push, ps_solve3d,
+    ps_pull) taken in turn by nh handles, each on its own CUDA stream and host
+    thread. Handle j starts once handle j-1 has pushed its first inputs, so
+    the copies in the two directions and the solves overlap instead of
+    queueing in lock-step. Bn: pinned numpy inputs, shared by the handles.
+    Returns (seconds, outputs of each handle)."""
+    import threading
+
+    import torch
+    handles, outs = [], []
+    for _ in range(nh):
+        h = psg.PoissonSolver()
+        s = torch.cuda.Stream()
+        h.set_stream(s.cuda_stream)
+        setup(h)
+        handles.append((h, s))
+        outs.append([torch.empty(b.shape, dtype=torch.float64).pin_memory().numpy() for b in Bn])
+    for (h, _), A in zip(handles, outs):  # first use: buffers, kernel copies
+        h.push(*Bn)
+        h.solve3d()
+        h.pull(*A)
+    errors = []
+    pushed = [threading.Event() for _ in range(nh)]
+
+    def worker(j):
+        h, A = handles[j][0], outs[j]
+        try:
+            if j > 0:
+                pushed[j - 1].wait()
+            for i in range(j, steps, nh):
+                h.push(*Bn)
+                pushed[j].set()
+                h.solve3d()
+                h.pull(*A)
+        except Exception as e:  # re-raised on the calling thread
+            errors.append(e)
+        finally:
+            pushed[j].set()
+
+    barrier(pg)
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=worker, args=(j,)) for j in range(nh)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    elapsed = time.perf_counter() - t0
+    if errors:
+        raise errors[0]
+    for h, _ in handles:
+        h.close()
+    return elapsed, outs
+
+
 def replica_throughput(points_per_rank, steps, elapsed_s_max, world):
     """Whole-job Mpts/s: every rank solves its own replica in the slowest rank's time."""
     return world * points_per_rank * steps / elapsed_s_max / 1e6
@@ -531,16 +590,26 @@ def run_ours(args, w):
         ps.push(*Bn)
         ps.solve3d()
         ps.pull(*An)
-    Ke = max(2, min(K, 5))
+    Ke = max(2, min(K, 10))
     barrier(pg)
     t0 = time.perf_counter()
     for _ in range(Ke):
         ps.push(*Bn)
         ps.solve3d()
         ps.pull(*An)
-    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
-    e2e = replica_throughput(points, Ke, e2e_s, world)
-    e2e_check = max(float((Ah[i] - A[i].cpu()).abs().max()) for i in range(3))
+    e2e_serial = replica_throughput(points, Ke, max_over_ranks(pg, time.perf_counter() - t0), world)
+    Ace = [a.cpu() for a in A]
+    e2e_check = max(float((Ah[i] - Ace[i]).abs().max()) for i in range(3))
+
+    def setup_e2e(h):
+        h.setup3d(nc, (0, 0, 0), dx, w["reg"])
+        h.set_return_curl(True)
+        h.set_precision("fp32")
+    Kp = 3 * max(1, (Ke + 2) // 3)
+    pipe_s, pipe_out = e2e_handles(psg, setup_e2e, Bn, Kp, pg)
+    e2e = replica_throughput(points, Kp, max_over_ranks(pg, pipe_s), world)
+    for outs in pipe_out:
+        e2e_check = max(e2e_check, max(float(np.abs(outs[i] - Ace[i].numpy()).max()) for i in range(3)))
 
     # roofline of the dominant kernel (fp32 path), live CUDA-event durations
     byt = algorithmic_bytes(nc, P, 3, 3, 8, 4)
@@ -580,7 +649,11 @@ def run_ours(args, w):
         "mixed_vs_fp64_speedup": value / value64,
         "rel_l2_fp32_vs_fp64": rel,
         "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": 3 * points * 8,
-                "d2h_bytes_per_step": 3 * points * 8, "max_abs_diff_vs_device": e2e_check},
+                "d2h_bytes_per_step": 3 * points * 8, "steps": Kp,
+                "method": "three handles, each on its own stream and host thread, take the steps in turn "
+                          "through the blocking ps_push / ps_solve3d / ps_pull with pinned host buffers",
+                "serial_value": e2e_serial, "serial_steps": Ke,
+                "max_abs_diff_vs_device": e2e_check},
         "gpu_launches": K * launches,
         "clocks": clocks,
         "setup_s": setup_s,
