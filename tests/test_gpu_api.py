@@ -165,3 +165,66 @@ def test_repeated_setup_and_many_handles(native, oracle):
     assert rel_l2([a], [ref[0]]) < 1e-12
     for ps in handles:
         ps.close()
+
+
+def test_concurrent_handles_on_threads(native):
+    """Independent handles, each on its own stream and host thread, solving at
+    the same time (the multi-instance use of the Fortran API's handle table):
+    every result equals the same solve run alone."""
+    import threading
+
+    import torch
+    nc, dx = (48, 40, 56), (0.04, 0.05, 0.035)
+    shape = (nc[2], nc[1], nc[0])
+    rng = np.random.default_rng(21)
+    cases = [((0, 0, 0), "curl"), ((1, 1, 0), "grad"), ((0, 0, 1), "div")]
+    B = [[rng.standard_normal(shape) for _ in range(3)] for _ in cases]
+
+    def make(j):
+        bc, opt = cases[j]
+        ps = native.PoissonSolver()
+        ps.setup3d(nc, bc, dx, 4)
+        getattr(ps, f"set_return_{opt}")(True)
+        ps.set_precision("fp32" if j % 2 else "fp64")
+        return ps
+
+    alone = []
+    for j in range(len(cases)):
+        ps = make(j)
+        ps.push(*B[j])
+        ps.solve3d()
+        A = [np.zeros(shape) for _ in range(3)]
+        ps.pull(*A)
+        alone.append(A)
+        ps.close()
+    handles, streams = [], []
+    for j in range(len(cases)):
+        ps = make(j)
+        s = torch.cuda.Stream()
+        ps.set_stream(s.cuda_stream)
+        handles.append(ps)
+        streams.append(s)
+    got = [[[np.zeros(shape) for _ in range(3)] for _ in range(4)] for _ in cases]
+    errors = []
+
+    def worker(j):
+        try:
+            for r in range(4):
+                handles[j].push(*B[j])
+                handles[j].solve3d()
+                handles[j].pull(*got[j][r])
+        except Exception as e:
+            errors.append(e)
+
+    th = [threading.Thread(target=worker, args=(j,)) for j in range(len(cases))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors
+    for j in range(len(cases)):
+        for r in range(4):
+            for c in range(3):
+                assert np.array_equal(got[j][r][c], alone[j][c])
+    for ps in handles:
+        ps.close()
