@@ -130,7 +130,8 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
     const int nq = nloc * nin;  // component loads of this CTA
 
     // thread 0: start load q (tile q / nin, component q % nin) into buffer q & 1
-    // once load q - 2 has been read by every thread
+    // once load q - 2 has been read by every thread (it is called while load
+    // q - 2 is being transformed, so a load has about two transforms to land)
     int issued = 0;
     auto issue = [&](int q) -> bool {
         const int s = q & 1;
@@ -179,7 +180,6 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
         // forward transforms; components 0 .. nin-2 parked in TMEM
         for (int c = 0; c < nin; ++c) {
             const int q = i * nin + c, s = q & 1;
-            if (tid == 0 && q >= 1 && q + 1 < nq) ok = issue(q + 1);
             ok = warp_ok(ok && mbar_wait(full0 + 8 * s, (q >> 1) & 1));
             if (!ok) break;
             if (tid == 0) consumed = q + 1;
@@ -189,6 +189,10 @@ __global__ void __launch_bounds__(ZQ_THREADS, 1)
             for (int r = 0; r < 16; ++r) v0[0][r] = *reinterpret_cast<const C *>(stg + T0::in_pos(t, 0, r) * 64);
             mbar_arrive(empty0 + 8 * s);
             dft32_half<false>(v0[0]);
+            // refill this buffer with load q + 2 once every thread has read it
+            if (tid == 0 && q + 2 < nq) ok = issue(q + 2);
+            ok = warp_ok(ok);
+            if (!ok) break;
             write_line<L, 0>(line, t, v0);
             __syncwarp();
             middle_stages<L, 1, false, true>(line, TW, t, 1, 0);
