@@ -170,7 +170,7 @@ def padded(nc, bc):
 
 # ---------------------------------------------------------------------------
 def algorithmic_bytes(n, P, cin, cout, w, g=None):
-    """Bytes each pass must move at minimum (SURVEY-style accounting): real FP64
+    """Bytes each pass must move at minimum: real FP64
     I/O once, half-spectrum working arrays once per read and write, the real even
     kernel read once as an octant. w = complex working bytes, g = kernel bytes."""
     Nx, Ny, Nz = n

@@ -38,7 +38,8 @@ enum {
     PS_ERR_MEMORY = 4,      /* device or host allocation failed */
     PS_ERR_CUDA = 5,        /* a CUDA call failed */
     PS_ERR_STATE = 6,       /* call out of order (e.g. solve before setup/push) */
-    PS_ERR_UNSUPPORTED = 7, /* outside what this build implements (e.g. 2D) */
+    PS_ERR_UNSUPPORTED = 7, /* outside what the library implements (e.g. a padded
+                               transform length above 8192) */
     PS_ERR_TIMEOUT = 8      /* a kernel's bounded wait for an asynchronous copy ran
                                out (reported by the next synchronising call:
                                ps_pull, ps_pull_device, ps_synchronize) */
