@@ -1,5 +1,6 @@
 """The C ABI library without a GPU: it loads, exports every symbol the header
 declares, and the drop-in C++ header compiles and links against it."""
+import ctypes
 import os
 import re
 import shutil
@@ -47,6 +48,13 @@ def test_status_strings_and_null_handles(native):
     assert lib.ps_destroy(None) == _lib.PS_OK
     assert lib.ps_setup2d(None, None, None, None, 0) == _lib.PS_ERR_ARGUMENT
     assert lib.ps_partition_count(None) == 0
+    # the Fortran-style entry points and the kernel family check the handle first
+    ext = (ctypes.c_int * 3)(4, 4, 4)
+    off = (ctypes.c_int * 3)(0, 0, 0)
+    assert lib.ps_push_interleaved(None, None, 1, ext, off) == _lib.PS_ERR_ARGUMENT
+    assert lib.ps_pull_interleaved(None, None, 1, None, 0, ext, off) == _lib.PS_ERR_ARGUMENT
+    assert lib.ps_smooth3d(None, 0.1) == _lib.PS_ERR_ARGUMENT
+    assert lib.ps_set_kernel(None, _lib.PS_KERNEL_GAUSSIAN, 0.0) == _lib.PS_ERR_ARGUMENT
 
 
 DROPIN_CLIENT = r"""
