@@ -30,6 +30,19 @@ def test_error_statuses(native):
         ps.setup3d((0, 8, 8), (0, 0, 0), (0.1,) * 3)
     assert e.value.status == _lib.PS_ERR_ARGUMENT
     with pytest.raises(PSError) as e:
+        ps.setup3d((8, 8, 8), (0, 0, 0), (0.1, float("nan"), 0.1))
+    assert e.value.status == _lib.PS_ERR_ARGUMENT
+    with pytest.raises(PSError) as e:
+        ps.setup3d((8, 8, 8), (0, 0, 0), (0.1,) * 3, -2)
+    assert e.value.status == _lib.PS_ERR_ARGUMENT
+    # the largest padded transform is 8192 points: 4097 unbounded cells pad to 8194
+    with pytest.raises(PSError) as e:
+        ps.setup3d((4097, 4, 4), (0, 0, 0), (0.1,) * 3)
+    assert e.value.status == _lib.PS_ERR_UNSUPPORTED
+    with pytest.raises(PSError) as e:
+        ps.setup2d((4, 8193), (1, 1), (0.1, 0.1))
+    assert e.value.status == _lib.PS_ERR_UNSUPPORTED
+    with pytest.raises(PSError) as e:
         ps.setup2d((8, 8), (0, 2), (0.1, 0.1))
     assert e.value.status == _lib.PS_ERR_BOUNDARY
     ps.setup2d((8, 8), (0, 0), (0.1, 0.1))
