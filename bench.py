@@ -220,12 +220,28 @@ class ClockSampler:
 
     def __init__(self, gpu_index):
         self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.skip = 0
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
                  "-i", str(gpu_index)], stdout=self.tmp, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+
+    def _lines(self):
+        self.tmp.flush()
+        with open(self.tmp.name) as f:
+            return sum(1 for line in f if line.strip())
+
+    def mark(self, timeout_s=5.0):
+        """Wait (bounded) until the sampler has written a row, then count the
+        rows so far: stop() keeps only the rows written after this call."""
+        if self.proc is None:
+            return
+        t0 = time.perf_counter()
+        while self._lines() == 0 and time.perf_counter() - t0 < timeout_s and self.proc.poll() is None:
+            time.sleep(0.02)
+        self.skip = self._lines()
 
     def stop(self):
         if self.proc is None:
@@ -238,7 +254,7 @@ class ClockSampler:
         self.tmp.flush()
         rows = []
         with open(self.tmp.name) as f:
-            for line in f:
+            for line in [x for x in f if x.strip()][self.skip:]:
                 p = [s.strip() for s in line.split(",")]
                 if len(p) >= 9:
                     rows.append(p)
@@ -550,6 +566,8 @@ def run_ours(args, w):
         ps.pass_times(reset=True)
         ps.set_pass_timing(True)
         clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
+            clocks.mark()
         barrier(pg)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -699,6 +717,8 @@ def run_mixed(args, w):
             step()
         torch.cuda.synchronize()
         clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
+            clocks.mark()
         barrier(pg)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -804,6 +824,8 @@ def run_batch(args, w):
             b.solve()
         torch.cuda.synchronize()
         clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
+            clocks.mark()
         barrier(pg)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -901,7 +923,7 @@ def run_batch(args, w):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rings512")
