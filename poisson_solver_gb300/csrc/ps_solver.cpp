@@ -245,8 +245,7 @@ const Plan &Solver::plan(int L, int prec, int emax)
 static int pick_lines(int prec, int tpl, const std::function<size_t(int)> &smem, const char *env = nullptr,
                       int pref = 0, int max_threads = MAX_THREADS)
 {
-    static int limit = 0;
-    if (!limit) limit = max_smem_per_block() - 1024;  // room for the static stage table
+    static const int limit = max_smem_per_block() - 1024;  // room for the static stage table
     int B = pref > 0 ? pref : (prec == PREC_FP64 ? 8 : 16);
     if (const char *v = env ? getenv(env) : nullptr) {
         const int want = atoi(v);
@@ -856,8 +855,7 @@ size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Pl
 
 bool Solver::pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan &pl) const
 {
-    static int limit = 0;
-    if (!limit) limit = max_smem_per_block() - 1024;  // room for static shared data
+    static const int limit = max_smem_per_block() - 1024;  // room for static shared data
     const int tpl = pl.dev.tpl, nt = B * tpl;
     int max_threads = MAX_THREADS;
     if (pass == 2 && fam == 't') max_threads = wide::ZT_MAX_THREADS;

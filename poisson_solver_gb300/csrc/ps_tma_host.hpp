@@ -48,16 +48,13 @@ inline bool encode_spectrum(CUtensorMap *m, const void *p, int mx, int rows, int
 
 inline int sm_count()
 {
-    static int n = 0;
-    if (!n) {
+    static const int n = [] {
         int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
-            n = v;
-        else
-            n = 1;
+        const bool ok = cudaGetDevice(&dev) == cudaSuccess &&
+                        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0;
         cudaGetLastError();
-    }
+        return ok ? v : 1;
+    }();
     return n;
 }
 
