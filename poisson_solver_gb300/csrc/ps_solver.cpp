@@ -1305,11 +1305,13 @@ void Solver::pull_interleaved(double *a, int ncomp_a, double *b, int ncomp_b, co
 {
     check_setup();
     const size_t elems = field_elems();
+    // both arrays are checked before either is written
+    if (a) check_box(n, ncomp_a, ext, off);
+    if (b) check_box(n, ncomp_b, ext, off);
     for (int which = 0; which < 2; ++which) {
         double *arr = which == 0 ? a : b;
         const int ncomp = which == 0 ? ncomp_a : ncomp_b;
         if (!arr) continue;
-        check_box(n, ncomp, ext, off);
         // solution components the solve produced, or the returned right-hand
         // side; components not there are written as zero (pull.f:340-365)
         const double *src[3] = {nullptr, nullptr, nullptr};

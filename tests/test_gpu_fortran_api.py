@@ -113,3 +113,31 @@ def test_interleaved_push_pull_with_ghosts(native, ncomp, opts):
     assert np.all(a_out[mask] == 7.0) and np.all(b_out[mask] == 7.0)
     ps.close()
     ps2.close()
+
+
+def test_interleaved_errors_leave_arrays_untouched(native):
+    import ctypes
+
+    from poisson_solver_gb300 import _lib as L
+    nc, dx = (6, 5, 4), (0.1, 0.1, 0.1)
+    ps = native.PoissonSolver()
+    ps.setup3d(nc, (0, 0, 0), dx, 0)
+    lib, h = ps._lib, ps._h
+    dp = ctypes.POINTER(ctypes.c_double)
+    ext = (ctypes.c_int * 3)(*nc)
+    off = (ctypes.c_int * 3)(0, 0, 0)
+    b = np.random.default_rng(5).standard_normal((nc[2], nc[1], nc[0], 1))
+    # extents too small for the field at its offset; more than three components
+    small = (ctypes.c_int * 3)(nc[0] - 1, nc[1], nc[2])
+    assert lib.ps_push_interleaved(h, b.ctypes.data_as(dp), 1, small, off) == L.PS_ERR_ARGUMENT
+    assert lib.ps_push_interleaved(h, b.ctypes.data_as(dp), 4, ext, off) == L.PS_ERR_ARGUMENT
+    assert lib.ps_push_interleaved(h, b.ctypes.data_as(dp), 1, ext, off) == L.PS_OK
+    assert lib.ps_solve3d(h) == L.PS_OK
+    # a bad second array: the call fails before writing the first
+    a = np.full((nc[2], nc[1], nc[0], 1), 7.0)
+    rb = np.zeros((nc[2], nc[1], nc[0], 5))
+    assert lib.ps_pull_interleaved(h, a.ctypes.data_as(dp), 1, rb.ctypes.data_as(dp), 5, ext, off) == L.PS_ERR_ARGUMENT
+    assert np.all(a == 7.0)
+    assert lib.ps_pull_interleaved(h, a.ctypes.data_as(dp), 1, None, 0, ext, off) == L.PS_OK
+    assert not np.all(a == 7.0)
+    ps.close()
