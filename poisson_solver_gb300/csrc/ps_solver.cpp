@@ -912,7 +912,7 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
 
 void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
 {
-    const int prec = precision, axis = axis_of(pass);
+    const int prec = precision;
     const Plan &pl = plan(pass_len(pass), prec, family_emax(pass, c.fam));
     switch (pass) {
     case 0: {

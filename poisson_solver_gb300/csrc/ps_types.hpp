@@ -16,7 +16,7 @@ enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
 // fused z pass holds three components in shared memory, so its FP32 variant
 // uses 8 to double the threads per line at the same footprint.
 __host__ __device__ constexpr int e_max(int prec) { return prec == PREC_FP64 ? 8 : 16; }
-__host__ __device__ constexpr int e_max_z(int prec) { return 8; }
+__host__ __device__ constexpr int e_max_z(int /*prec*/) { return 8; }
 
 // One 1D transform length as the kernels see it (see ps_fft.cuh).
 struct FftPlanDev {
