@@ -1073,11 +1073,36 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
         if (opt_timing) PS_CK(cudaEventRecord(ev[i], stream));
     };
     mark(0);
+    // PS_XY_FUSION=1: where x and y both run the bulk-copy kernels on
+    // unbounded axes of one length, their forward passes run as one launch
+    // (k_xyq), whose y tiles read a chunk's x output from L2. Same results;
+    // at 512^3 it is slower than the two launches (4.0 against 2.9 ms: its x
+    // tiles run at 8 warps an SM with unstaged FP64 loads), so it is opt-in.
+    bool xy_fused = false;
+    if (dims == 3 && precision == PREC_FP32) {
+        const char *env = getenv("PS_XY_FUSION");
+        const PassChoice c0 = choice(0, pa), c1 = choice(1, pa);
+        if (env && atoi(env) == 1 && c0.fam == 'q' && c1.fam == 'q') {
+            pa.x.plan = plan(pass_len(0), precision, family_emax(0, 'q')).dev;
+            pa.x.B = c0.B;
+            pa.y.plan = plan(pass_len(1), precision, family_emax(1, 'q')).dev;
+            pa.y.B = c1.B;
+            xy_fused = wide::xyq_supported(pa.x, pa.y, n[2]);
+        }
+    }
     // x forward, y forward, z (forward, spectral operation, inverse), then
     // y inverse and x inverse of the written outputs
     for (int pass = 0; pass < NPASS; ++pass) {
-        // 2D: the fused pass transforms y itself
-        if ((pass < 3 || write_mask) && !(dims == 2 && (pass == 1 || pass == 3))) launch_pass(pass, choice(pass, pa), pa);
+        if (xy_fused && pass == 0) {
+            xy_counts.ensure(sizeof(int) * 3 * (size_t)n[2]);
+            PS_CK(wide::launch_xyq(pa.x, pa.y, n[2], static_cast<int *>(status.p), static_cast<int *>(xy_counts.p),
+                                   stream));
+        } else if (xy_fused && pass == 1) {
+            // done with pass 0
+        } else if ((pass < 3 || write_mask) && !(dims == 2 && (pass == 1 || pass == 3))) {
+            // 2D: the fused pass transforms y itself
+            launch_pass(pass, choice(pass, pa), pa);
+        }
         mark(pass + 1);
     }
     return write_mask;

@@ -90,6 +90,7 @@ struct Solver {
     DevBuf stage;               // packed interleaved fields for push/pull_interleaved
     DevBuf work[3];         // per-component spectra [Nz][Py][Mx], pass precision
     DevBuf fb[3], fa[3], fr[3];  // handle-owned fields: pushed B, solution A, returned B
+    DevBuf xy_counts;            // per chunk of z-planes: x lines written (fused x-y forward pass)
     DevBuf status;               // int[4]: [0] bit 0 set by a kernel whose bounded wait timed out,
                                  // [1] tile counter of the dynamically scheduled kernels
 

@@ -199,6 +199,22 @@ bool yq_supported(int prec, int inverse, int L, int n_in, int n_out);
 int yq_lines(int L);
 size_t smem_lines_yq(int inverse, int L, int n_in, int n_out, int ntw_entries);
 cudaError_t launch_yq(int inverse, const ColArgs &a, int nplanes, int *status, cudaStream_t st);
+// The x and y forward passes fused in one persistent launch (both axes
+// unbounded, one length, FP32, the x output in place in the y pass's
+// spectra); counts: an int a chunk of z-planes per component.
+struct XyPlan {
+    int zc;      // z-planes a chunk
+    int nzc;     // chunks a component
+    int nchunk;  // nzc * components
+    int nxl;     // x tiles a chunk
+    int nxt;     // y column groups a plane
+    int nyt;     // y tiles a chunk
+    int ntiles;  // nchunk * (nxl + nyt)
+    int *count;  // per chunk: x-tile warps whose lines are written
+};
+bool xyq_supported(const XFwdArgs &xa, const ColArgs &a, int nplanes);
+int xyq_chunk_planes(int nplanes);
+cudaError_t launch_xyq(const XFwdArgs &xa, const ColArgs &a, int nplanes, int *status, int *counts, cudaStream_t st);
 // x passes, a warp per line group (ps_kernels_xq.cu): L = 256..1024, not
 // mirrored; xq_lines(L) lines a CTA. n = n_in (forward) or n_out (inverse).
 bool xq_supported(int prec, int inverse, int L, int n, int mirror);
