@@ -322,8 +322,9 @@ int yq_half(int inverse, int L, int n_in, int n_out)
 // y spectra, so it does not make a round trip through DRAM: the pair of
 // passes moves the FP64 input and the y output only. Opt-in (PS_XY_FUSION=1):
 // with one CTA of 8 compute warps an SM its x tiles, which load their FP64
-// rows straight from global memory, run far below the 24-warp k_xfq, and the
-// launch takes 4.0 ms at 512^3 against 2.9 ms for the two passes.
+// rows from global memory (an L2 bulk prefetch started when the tile is handed
+// out), run far below the 24-warp k_xfq, and the launch takes 3.8 ms at 512^3
+// against 2.9 ms for the two passes.
 template <int L> struct Xy {
     using Q = Yq<L, false, true>;
     static constexpr int TPL = L / 32;
@@ -437,7 +438,16 @@ __global__ void __launch_bounds__(YQ_THREADS, 1)
                 xy_decode(p, j, is_y, k, t);
                 itile[s] = j;
                 if (!is_y) {
-                    mbar_arrive(full0 + 8 * s);  // an x tile: the index alone
+                    // an x tile: its rows are one contiguous run of the input;
+                    // start pulling them into L2, then hand over the index
+                    const int c = k / p.nzc, z0 = (k - c * p.nzc) * p.zc;
+                    const long long r0 = 2LL * t * X::NL, rows_chunk = (long long)p.zc * xa.rows_y;
+                    const long long nrows = rows_chunk - r0 < 2LL * X::NL ? rows_chunk - r0 : 2LL * X::NL;
+                    const double *src = pick3(xa.in, c) + ((long long)z0 * xa.rows_y + r0) * xa.in_stride;
+                    const unsigned bytes = (unsigned)(nrows * xa.in_stride * 8);
+                    if (nrows > 0 && (bytes & 15u) == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+                    mbar_arrive(full0 + 8 * s);
                 } else {
                     // every x line of the chunk written, then copies that see them
                     if (!wait_count(p.count + k, p.nxl * X::WARPS)) {
