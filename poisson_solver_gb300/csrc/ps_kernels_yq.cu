@@ -323,7 +323,7 @@ int yq_half(int inverse, int L, int n_in, int n_out)
 // passes moves the FP64 input and the y output only. Opt-in (PS_XY_FUSION=1):
 // with one CTA of 8 compute warps an SM its x tiles, which load their FP64
 // rows from global memory (an L2 bulk prefetch started when the tile is handed
-// out), run far below the 24-warp k_xfq, and the launch takes 3.8 ms at 512^3
+// out), run far below the 24-warp k_xfq, and the launch takes 3.55 ms at 512^3
 // against 2.9 ms for the two passes.
 template <int L> struct Xy {
     using Q = Yq<L, false, true>;
@@ -334,26 +334,32 @@ template <int L> struct Xy {
     static_assert(NL == Q::B, "x lines and y columns share the line buffers");
 };
 
-// tile j of the queue -> (is_y, chunk, index within the chunk's block)
+// tile j of the queue -> (is_y, chunk, index within the chunk's block). The
+// queue is X_0 .. X_{D-1}, then [X_{s+D}][Y_s] for s < K - D, then
+// Y_{K-D} .. Y_{K-1}: a chunk's y tiles come D chunks of x tiles after its
+// own x tiles (D = p.delay, at most K), enough to cover the tiles in flight.
 __device__ __forceinline__ void xy_decode(const XyPlan &p, int j, bool &is_y, int &k, int &t)
 {
-    const int nx = p.nxl, seg = p.nxl + p.nyt;
-    if (j < nx) {
+    const int nx = p.nxl, ny = p.nyt, seg = nx + ny, K = p.nchunk;
+    const int D = p.delay < K ? p.delay : K;
+    if (j < D * nx) {
         is_y = false;
-        k = 0;
-        t = j;
+        k = j / nx;
+        t = j - k * nx;
         return;
     }
-    const int jj = j - nx, s = jj / seg, off = jj - s * seg;
-    if (s < p.nchunk - 1) {
+    const int jj = j - D * nx, nseg = K - D;
+    if (jj < nseg * seg) {
+        const int s = jj / seg, off = jj - s * seg;
         is_y = off >= nx;
-        k = is_y ? s : s + 1;
+        k = is_y ? s : s + D;
         t = is_y ? off - nx : off;
-    } else {
-        is_y = true;
-        k = p.nchunk - 1;
-        t = off;
+        return;
     }
+    const int j2 = jj - nseg * seg;
+    is_y = true;
+    k = nseg + j2 / ny;
+    t = j2 - (j2 / ny) * ny;
 }
 
 // Bounded wait until *cnt >= target (acquire); false after 1 s or 2^26 polls.
@@ -625,6 +631,13 @@ cudaError_t launch_xyq_t(const XFwdArgs &xa, const ColArgs &a, int nplanes, int 
     p.ntiles = p.nchunk * (p.nxl + p.nyt);
     p.count = counts;
     const int grid = p.ntiles < tma::sm_count() ? p.ntiles : tma::sm_count();
+    // y tiles trail their x tiles by enough chunks to cover the tiles in
+    // flight (about three a CTA), within about 48 MB of x output held in L2
+    const long long chunk_bytes = (long long)zc * xa.rows_y * xa.ld * 8;
+    int delay = (3 * grid + p.nxl - 1) / p.nxl;
+    const int cap = (int)((48LL << 20) / (chunk_bytes > 0 ? chunk_bytes : 1));
+    if (delay > cap) delay = cap;
+    p.delay = delay < 1 ? 1 : delay;
     const size_t sm = Q::bytes(a.plan.ntw);
     cudaError_t e = cudaFuncSetAttribute(k_xyq<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;

@@ -1076,7 +1076,7 @@ int Solver::solve(const double *const Bin[3], double *const Aout[3], bool filter
     // PS_XY_FUSION=1: where x and y both run the bulk-copy kernels on
     // unbounded axes of one length, their forward passes run as one launch
     // (k_xyq), whose y tiles read a chunk's x output from L2. Same results;
-    // at 512^3 it is slower than the two launches (3.8 against 2.9 ms: its x
+    // at 512^3 it is slower than the two launches (3.55 against 2.9 ms: its x
     // tiles run at 8 warps an SM with unstaged FP64 loads), so it is opt-in.
     bool xy_fused = false;
     if (dims == 3 && precision == PREC_FP32) {

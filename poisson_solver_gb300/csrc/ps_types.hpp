@@ -210,6 +210,7 @@ struct XyPlan {
     int nxt;     // y column groups a plane
     int nyt;     // y tiles a chunk
     int ntiles;  // nchunk * (nxl + nyt)
+    int delay;   // chunks of x tiles between a chunk's x tiles and its y tiles
     int *count;  // per chunk: x-tile warps whose lines are written
 };
 bool xyq_supported(const XFwdArgs &xa, const ColArgs &a, int nplanes);
