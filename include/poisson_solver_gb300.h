@@ -258,6 +258,9 @@ int ps_batch_destroy(ps_batch *b);
 int ps_batch_add(ps_batch *b, const int ncell[3], const int bc[3], const double dx[3], int reg_order, int *index);
 int ps_batch_count(const ps_batch *b, int *count);
 int ps_batch_set_option(ps_batch *b, int index, int option, int value);
+/* ps_set_kernel for problem index (its kernel is rebuilt as a new setup:
+ * push its fields after this call). */
+int ps_batch_set_kernel(ps_batch *b, int index, int family, double width);
 int ps_batch_push(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
 int ps_batch_push_device(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
 int ps_batch_solve(ps_batch *b);

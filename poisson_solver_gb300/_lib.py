@@ -92,6 +92,7 @@ SIGNATURES = {
     "ps_batch_add": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_double), _i, _ip]),
     "ps_batch_count": (_i, [_vp, _ip]),
     "ps_batch_set_option": (_i, [_vp, _i, _i, _i]),
+    "ps_batch_set_kernel": (_i, [_vp, _i, _i, ctypes.c_double]),
     "ps_batch_push": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_push_device": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_solve": (_i, [_vp]),

@@ -79,6 +79,13 @@ struct Batch {
         dirty = true;
     }
 
+    // kernel family of problem i: its kernel is rebuilt, as a new setup
+    void set_kernel(int i, int family, double width)
+    {
+        at(i).set_kernel(family, width);
+        dirty = true;
+    }
+
     void push(int i, const double *const B[3], cudaMemcpyKind kind)
     {
         Solver &s = at(i);
@@ -378,6 +385,11 @@ int ps_batch_count(const ps_batch *h, int *count)
 int ps_batch_set_option(ps_batch *h, int index, int option, int value)
 {
     return bguarded(h, [&](ps::Batch &b) { b.set_option(index, option, value); });
+}
+
+int ps_batch_set_kernel(ps_batch *h, int index, int family, double width)
+{
+    return bguarded(h, [&](ps::Batch &b) { b.set_kernel(index, family, width); });
 }
 
 int ps_batch_push(ps_batch *h, int index, const double *bx, const double *by, const double *bz)

@@ -297,6 +297,11 @@ class PoissonBatch:
     def set_return_curl(self, i: int, toggle: bool):
         self._call("ps_batch_set_option", int(i), L.PS_OPT_CURL, int(bool(toggle)))
 
+    def set_kernel(self, i: int, family: str, width: float = 0.0):
+        """Kernel family of problem i ('spectral' or 'gaussian'); push after it."""
+        v = {"spectral": L.PS_KERNEL_SPECTRAL, "gaussian": L.PS_KERNEL_GAUSSIAN}[family]
+        self._call("ps_batch_set_kernel", int(i), v, float(width))
+
     def set_reprojection(self, i: int, toggle: bool):
         self._call("ps_batch_set_option", int(i), L.PS_OPT_REPROJECT, int(bool(toggle)))
 

@@ -172,3 +172,30 @@ def test_batch_device_pointers_on_a_stream(native, oracle):
         ref, _ = oracle.solve3d(nc, bc, _dx(nc), [f.cpu().numpy(), None, None], 2)
         assert rel_l2([o.cpu().numpy()], [ref[0]]) < FP64_TOL
     b.close()
+
+
+def test_batch_gaussian_family_equals_single_solves(native):
+    """Problems switched to the Gaussian-regularised kernel family solve in
+    the batch exactly as alone (FP64), next to problems that keep the
+    reference's kernels."""
+    b = native.PoissonBatch("fp64")
+    data, fam = [], []
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS[:6]):
+        b.add(nc, bc, _dx(nc), (0, 2, 6)[i % 3])
+        family = "gaussian" if i % 2 == 0 else "spectral"
+        b.set_kernel(i, family, 0.0)
+        for k, v in opts.items():
+            getattr(b, "set_return_" + k)(i, v)
+        B = _fields(nc, comps, 40 + i, zero_mean=bc == (1, 1, 0))
+        b.push(i, *B)
+        data.append(B)
+        fam.append(family)
+    b.solve()
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS[:6]):
+        single, _ = native.solve(nc, bc, _dx(nc), data[i], (0, 2, 6)[i % 3], kernel=fam[i], **opts)
+        got = _pull(b, i)
+        for g, s in zip(got, single):
+            assert (g is None) == (s is None)
+            if g is not None:
+                assert np.array_equal(g, s), (i, nc, bc, opts, fam[i])
+    b.close()
