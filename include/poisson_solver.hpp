@@ -113,6 +113,17 @@ public:
     void set_precision(int precision) { report(ps_set_option(h_, PS_OPT_PRECISION, precision), "set_precision"); }
     void set_kernel(int family, double width = 0.0) { report(ps_set_kernel(h_, family, width), "set_kernel"); }
     void smooth3d(double width) { report(ps_smooth3d(h_, width), "smooth3d"); }
+    /* One array holding ncomp components interleaved (component fastest),
+     * allocated extents ext[3] (x, y, z), field box at offset[3]
+     * (poisson_solver_push.f / poisson_solver_pull.f). */
+    void push_interleaved(const double *b, int ncomp, const int ext[3], const int offset[3])
+    {
+        report(ps_push_interleaved(h_, b, ncomp, ext, offset), "push_interleaved");
+    }
+    void pull_interleaved(double *a, int ncomp_a, double *b, int ncomp_b, const int ext[3], const int offset[3])
+    {
+        report(ps_pull_interleaved(h_, a, ncomp_a, b, ncomp_b, ext, offset), "pull_interleaved");
+    }
     int last_status() const { return status_; }
     ps_solver *handle() { return h_; }
 };

@@ -74,6 +74,14 @@ int main(int argc, char** argv) {
   poisson.push(B[0], B[1], B[2]);
   poisson.solve3d();
   poisson.pull(A[0], A[1], A[2], B[0], B[1], B[2]);
+  // the extensions: kernel family, interleaved ghost-offset arrays, smoothing
+  int ext[3] = {20, 18, 16}, off[3] = {2, 1, 0};
+  double *I = new double[3 * 20 * 18 * 16]();
+  poisson.set_kernel(PS_KERNEL_GAUSSIAN);
+  poisson.push_interleaved(I, 3, ext, off);
+  poisson.smooth3d(0.2);
+  poisson.solve3d();
+  poisson.pull_interleaved(I, 3, nullptr, 0, ext, off);
   MPI_Finalize();
   return poisson.last_status();
 }
