@@ -241,3 +241,24 @@ def test_concurrent_handles_on_threads(native):
                 assert np.array_equal(got[j][r][c], alone[j][c])
     for ps in handles:
         ps.close()
+
+
+def test_dropin_client_runs(native, tmp_path):
+    """The header-only C++ class, compiled into a client shaped like the
+    reference's validation programs and extended with the kernel family,
+    interleaved arrays and smooth3d, runs on the GPU with every call OK."""
+    import os
+    import subprocess
+
+    from conftest import ROOT
+    from poisson_solver_gb300 import _lib
+    from test_abi import DROPIN_CLIENT
+    src = tmp_path / "client.cpp"
+    src.write_text(DROPIN_CLIENT)
+    exe = tmp_path / "client"
+    cmd = ["g++", "-std=c++11", "-O1", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "oracle", "mpi_stub"),
+           str(src), "-o", str(exe), _lib.lib_path(), f"-Wl,-rpath,{os.path.dirname(_lib.lib_path())}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stdout + run.stderr
