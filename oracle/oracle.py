@@ -22,7 +22,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libps_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpsref.so")
-DEFAULT_REF = "/root/reference"
+REF_SOURCE_LINK = os.path.join(HERE, "_ref", "source")  # written by the reference build
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -30,10 +30,18 @@ _libs: dict[str, ctypes.CDLL] = {}
 
 
 def build(reference_root: str | None = None) -> None:
-    """Compile the port (always) and the reference library (when its sources exist)."""
-    ref = reference_root or os.environ.get("PS_REFERENCE_ROOT", DEFAULT_REF)
-    subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile"), f"REF={ref}", "all"],
-                   check=True, cwd=HERE)
+    """Compile the port (always) and the reference library (when reference_root,
+    or else $PS_REFERENCE_ROOT, names a reference checkout that exists)."""
+    ref = reference_root or os.environ.get("PS_REFERENCE_ROOT", "")
+    cmd = ["make", "-s", "-f", os.path.join(HERE, "Makefile")]
+    if ref and os.path.isdir(ref):
+        cmd.append(f"REF={ref}")
+    subprocess.run(cmd + ["all"], check=True, cwd=HERE)
+
+
+def reference_root() -> str | None:
+    """The reference checkout the reference library was built from, if any."""
+    return os.path.realpath(REF_SOURCE_LINK) if os.path.isdir(REF_SOURCE_LINK) else None
 
 
 def available(kind: str = "port") -> bool:

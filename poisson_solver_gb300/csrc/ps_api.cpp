@@ -20,8 +20,7 @@ template <typename F> int guarded(ps_solver *h, F &&f)
 {
     if (!h) return PS_ERR_ARGUMENT;
     try {
-        int cur = -1;
-        if (cudaGetDevice(&cur) == cudaSuccess && cur != h->s.device) cudaSetDevice(h->s.device);
+        ps::DeviceScope scope(h->s.device);
         f(h->s);
         h->s.last_error.clear();
         return PS_OK;
@@ -58,8 +57,7 @@ int ps_create(ps_solver **out)
 int ps_destroy(ps_solver *h)
 {
     if (!h) return PS_OK;
-    int cur = -1;
-    if (cudaGetDevice(&cur) == cudaSuccess && cur != h->s.device) cudaSetDevice(h->s.device);
+    ps::DeviceScope scope(h->s.device);
     if (h->s.stream) cudaStreamSynchronize(h->s.stream);
     delete h;
     return PS_OK;

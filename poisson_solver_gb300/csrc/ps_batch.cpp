@@ -321,8 +321,7 @@ template <typename F> int bguarded(ps_batch *h, F &&f)
     if (!h || !h->b) return PS_ERR_ARGUMENT;
     ps::Batch &b = *h->b;
     try {
-        int cur = -1;
-        if (cudaGetDevice(&cur) == cudaSuccess && cur != b.device) cudaSetDevice(b.device);
+        ps::DeviceScope scope(b.device);
         f(b);
         b.last_error.clear();
         return PS_OK;
@@ -361,8 +360,12 @@ int ps_batch_create(ps_batch **out, int precision)
 int ps_batch_destroy(ps_batch *h)
 {
     if (!h) return PS_OK;
-    if (h->b) cudaSetDevice(h->b->device);
-    delete h;
+    if (h->b) {
+        ps::DeviceScope scope(h->b->device);
+        delete h;
+    } else {
+        delete h;
+    }
     return PS_OK;
 }
 

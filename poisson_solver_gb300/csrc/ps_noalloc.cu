@@ -10,7 +10,8 @@
 // into the library:
 //
 //   g_noalloc_scratch   32 MiB of spectra (complex FP64)
-//   g_noalloc_twiddles   1 MiB of FFT twiddle factors
+//   g_noalloc_twiddles   1 MiB of FFT twiddle factors, recomputed on the
+//                        device in the call's stream by every call
 //
 // Both are file-scope __device__ arrays, so every GPU that loads this part of
 // the library holds them until the process exits. The kernel octant comes
@@ -18,7 +19,9 @@
 // handle, device inputs and device outputs.
 //
 // Limits and rules:
-//   * Transforms are FP64, whatever PS_OPT_PRECISION says.
+//   * Transforms are FP64, whatever PS_OPT_PRECISION says, with the plans
+//     the handle's own FP64 solve uses (Bluestein for lengths with a prime
+//     factor of 17 or more).
 //   * The problem must fit: (components in use) x Nz x Py x (Px/2+1) x 16
 //     bytes <= 32 MiB (e.g. a 64^3 unbounded 3-component curl solve needs
 //     25.6 MiB). Larger problems fail with PS_ERR_UNSUPPORTED and say why.
@@ -34,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 
@@ -61,7 +65,6 @@ struct Symbols {
 };
 std::mutex g_mu;
 Symbols g_symbols[kMaxDevices];
-double2 g_host_twiddles[kTwiddleElems];  // staging for the upload, guarded by g_mu
 
 Symbols device_symbols()
 {
@@ -84,13 +87,77 @@ Symbols device_symbols()
     return s;
 }
 
-// FP64 plan of length L written into fixed storage: the same radix order and
-// twiddles as Solver::plan builds for PREC_FP64, without heap allocation.
-void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_table)
+// The twiddle tables are computed on the device, in the call's stream, as
+// runs ("segments") of one of four kinds:
+//   SEG_STAGE  e^{-2 pi i j r / (m R)} for j < m, r = 1..R-1 (a stage's twiddles)
+//   SEG_ROOTS  e^{-2 pi i q / R} for q < R (a direct prime-radix stage)
+//   SEG_CHIRP  c[k] = e^{-i pi k^2 / Lt} for k < Lt (Bluestein chirp)
+//   SEG_KSPEC  K[k] = DFT_M(conj c wrapped onto M points)[k] / M for k < M
+enum SegKind { SEG_STAGE = 0, SEG_ROOTS = 1, SEG_CHIRP = 2, SEG_KSPEC = 3 };
+struct Seg {
+    int kind;
+    int off;    // first table entry
+    int count;  // entries
+    int a, b;   // STAGE: m, R; ROOTS: -, R; CHIRP: Lt, -; KSPEC: Lt, M
+};
+constexpr int kMaxSegs = 3 * (2 * MAX_STAGES + 2);
+struct FillArgs {
+    Seg seg[kMaxSegs];
+    int nseg;
+    double2 *table;
+};
+
+// e^{-2 pi i e / N} from the exactly reduced fraction e / N (angle in (-pi, pi]).
+__device__ double2 na_root(long long e, long long N)
 {
-    d = FftPlanDev{};
-    d.L = L;
-    int rad[MAX_STAGES], nr = 0;
+    e %= N;
+    if (e < 0) e += N;
+    if (2 * e > N) e -= N;
+    double sn, cs;
+    sincospi(2.0 * (double)e / (double)N, &sn, &cs);
+    return make_double2(cs, -sn);
+}
+
+__global__ void k_noalloc_twiddles(const __grid_constant__ FillArgs a)
+{
+    const Seg sg = a.seg[blockIdx.y];
+    double2 *out = a.table + sg.off;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < sg.count; i += gridDim.x * blockDim.x) {
+        double2 v;
+        if (sg.kind == SEG_STAGE) {
+            const int j = i / (sg.b - 1), r = i % (sg.b - 1) + 1;
+            v = na_root((long long)j * r, (long long)sg.a * sg.b);
+        } else if (sg.kind == SEG_ROOTS) {
+            v = na_root(i, sg.b);
+        } else if (sg.kind == SEG_CHIRP) {
+            const long long Lt = sg.a;
+            v = na_root(((long long)i * i) % (2 * Lt), 2 * Lt);
+        } else {
+            // conj c[n] sits at n and (n > 0) at M - n; their two DFT terms
+            // add to 2 cos(2 pi n k / M) conj c[n].
+            const long long Lt = sg.a, M = sg.b;
+            double re = 0.0, im = 0.0;
+            for (long long n = 0; n < Lt; ++n) {
+                const double2 c = na_root(-((n * n) % (2 * Lt)), 2 * Lt);  // conj c[n]
+                const double w = n == 0 ? 1.0 : 2.0 * na_root((n * i) % M, M).x;
+                re += w * c.x;
+                im += w * c.y;
+            }
+            v = make_double2(re / (double)M, im / (double)M);
+        }
+        out[i] = v;
+    }
+}
+
+// Stage order of the FP64 plans (Solver::plan with radices up to 8): primes
+// above 7 (direct DFT stages), 7s, 5s, 3s, 8s, then one 4 or 2.
+void factor_fp64(int L, int rad[MAX_STAGES], int &nr)
+{
+    nr = 0;
+    auto push = [&](int r) {
+        if (nr == MAX_STAGES) throw Error(PS_ERR_UNSUPPORTED, "transform length has too many factors");
+        rad[nr++] = r;
+    };
     int x = L, p2 = 0;
     int big[MAX_STAGES], nbig = 0, odd[3] = {0, 0, 0};
     while (x > 1 && x % 2 == 0) { x /= 2; ++p2; }
@@ -104,28 +171,54 @@ void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_t
             x /= p;
         }
     if (x > 1) big[nbig++] = x;
-    auto push = [&](int r) {
-        if (nr == MAX_STAGES) throw Error(PS_ERR_UNSUPPORTED, "transform length has too many factors");
-        rad[nr++] = r;
-    };
     for (int i = 0; i < nbig; ++i) push(big[i]);
     for (int i = 2; i >= 0; --i)
         for (int k = 0; k < odd[i]; ++k) push(small_primes[i]);
     while (p2 >= 3) { push(8); p2 -= 3; }
     if (p2 == 2) push(4);
     if (p2 == 1) push(2);
+}
 
-    const long double pi = 3.141592653589793238462643383279502884L;
-    auto root = [&](long long e, long long N) {
-        e %= N;
-        const long double a = 2.0L * pi * (long double)e / (long double)N;
-        return make_double2((double)cosl(a), (double)-sinl(a));
-    };
-    auto put = [&](double2 v) {
-        if (used >= kTwiddleElems) throw Error(PS_ERR_UNSUPPORTED, "twiddle tables exceed the 1 MiB of the no-allocation solve");
-        g_host_twiddles[used++] = v;
-    };
+int largest_prime(int x)
+{
+    int f = 1;
+    for (int p = 2; (long long)p * p <= x; ++p)
+        while (x % p == 0) {
+            f = p;
+            x /= p;
+        }
+    return x > 1 ? (x > f ? x : f) : f;
+}
+
+// FP64 plan of transform length Lt laid out in the fixed twiddle array: the
+// plan Solver::plan builds for PREC_FP64 (same radix order, table layout and
+// Bluestein switch for lengths above 16 with a prime factor of 17 or more),
+// with the table entries described as segments for k_noalloc_twiddles
+// instead of being computed on the host.
+void describe_fp64_plan(int Lt, FftPlanDev &d, size_t &used, FillArgs &fill, const double2 *dev_table)
+{
+    d = FftPlanDev{};
+    const bool blue = Lt > 16 && largest_prime(Lt) >= 17 && !getenv("PS_NO_BLUESTEIN");
+    int L = Lt;
+    if (blue) {
+        L = 1;
+        while (L < 2 * Lt - 1) L <<= 1;
+    }
+    d.L = L;
+    d.blue = blue ? 1 : 0;
+    d.lb = Lt;
+    int rad[MAX_STAGES], nr = 0;
+    if (L > 1) factor_fp64(L, rad, nr);
+
     const size_t base = used;
+    auto segment = [&](int kind, int count, int a, int b) {
+        if (count <= 0) return;
+        if (used + (size_t)count > kTwiddleElems)
+            throw Error(PS_ERR_UNSUPPORTED, "twiddle tables exceed the 1 MiB of the no-allocation solve");
+        if (fill.nseg == kMaxSegs) throw Error(PS_ERR_UNSUPPORTED, "too many twiddle segments");
+        fill.seg[fill.nseg++] = Seg{kind, (int)used, count, a, b};
+        used += (size_t)count;
+    };
     const int emax = e_max(PREC_FP64);
     int m = 1, tpl = 1;
     d.nstages = nr;
@@ -135,8 +228,7 @@ void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_t
         d.m[s] = m;
         d.lm[s] = (m & (m - 1)) == 0 ? __builtin_ctz((unsigned)m) : -1;
         d.tw[s] = (int)(used - base);
-        for (int j = 0; j < m; ++j)
-            for (int r = 1; r < R; ++r) put(root((long long)j * r, (long long)m * R));
+        segment(SEG_STAGE, m * (R - 1), m, R);
         const int nbf = L / R;
         const bool fixed = R == 2 || R == 3 || R == 4 || R == 5 || R == 7 || R == 8;
         if (fixed) {
@@ -146,15 +238,21 @@ void describe_fp64_plan(int L, FftPlanDev &d, size_t &used, const double2 *dev_t
         } else {
             d.generic = 1;
             d.gw[s] = (int)(used - base);
-            for (int q = 0; q < R; ++q) put(root(q, R));
+            segment(SEG_ROOTS, R, 0, R);
             const int g = L < 64 ? L : 64;  // the direct DFT spreads a line's L outputs over its threads
             tpl = tpl > g ? tpl : g;
         }
         m *= R;
     }
-    if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length too large");
     d.tpl = tpl;
-    d.ntw = (int)(used - base);
+    d.ntw = (int)(used - base);  // the part the kernels stage in shared memory
+    if (blue) {
+        d.chirp = (int)(used - base);
+        segment(SEG_CHIRP, Lt, Lt, 0);
+        d.kspec = (int)(used - base);
+        segment(SEG_KSPEC, L, Lt, L);
+    }
+    if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length too large");
     d.table = dev_table + base;
 }
 
@@ -211,12 +309,15 @@ int solve_noalloc(Solver &s, const double *const Bin[3], double *const Aout[3])
 
     FftPlanDev px, py, pz;
     size_t used = 0;
-    describe_fp64_plan(P[0], px, used, sym.twiddles);
-    describe_fp64_plan(P[1], py, used, sym.twiddles);
-    describe_fp64_plan(P[2], pz, used, sym.twiddles);
-    if (used)
-        PS_NA_CK(cudaMemcpyToSymbolAsync(g_noalloc_twiddles, g_host_twiddles, used * sizeof(double2), 0,
-                                         cudaMemcpyHostToDevice, s.stream));
+    FillArgs fill{};
+    fill.table = sym.twiddles;
+    describe_fp64_plan(P[0], px, used, fill, sym.twiddles);
+    describe_fp64_plan(P[1], py, used, fill, sym.twiddles);
+    describe_fp64_plan(P[2], pz, used, fill, sym.twiddles);
+    if (fill.nseg) {
+        k_noalloc_twiddles<<<dim3(8, fill.nseg), 256, 0, s.stream>>>(fill);
+        PS_NA_CK(cudaGetLastError());
+    }
     const int prec = PREC_FP64;
 
     XFwdArgs xa{};

@@ -21,6 +21,27 @@ struct Error : std::runtime_error {
     Error(int st, const std::string &msg) : std::runtime_error(msg), status(st) {}
 };
 
+// Makes a handle's device current for one ABI call and gives the calling
+// thread back its own current device afterwards.
+struct DeviceScope {
+    int saved = -1;
+    explicit DeviceScope(int device)
+    {
+        if (cudaGetDevice(&saved) != cudaSuccess) {
+            cudaGetLastError();
+            saved = -1;
+        }
+        if (saved != device) cudaSetDevice(device);
+        else saved = -1;  // nothing to restore
+    }
+    ~DeviceScope()
+    {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 // Grow-only device allocation.
 struct DevBuf {
     void *p = nullptr;

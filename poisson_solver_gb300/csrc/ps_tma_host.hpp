@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 
@@ -46,16 +47,27 @@ inline bool encode_spectrum(CUtensorMap *m, const void *p, int mx, int rows, int
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// SM count of the current device, cached per device ordinal (a process may
+// hold handles on GPUs of different models).
 inline int sm_count()
 {
-    static const int n = [] {
-        int dev = 0, v = 0;
-        const bool ok = cudaGetDevice(&dev) == cudaSuccess &&
-                        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0;
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];  // 0: not yet read
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
         cudaGetLastError();
-        return ok ? v : 1;
-    }();
-    return n;
+        return 1;
+    }
+    if (dev < kMaxDevices) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int v = 0;
+    const bool ok = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0;
+    cudaGetLastError();
+    if (!ok) return 1;
+    if (dev < kMaxDevices) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
 }
 
 }  // namespace tma

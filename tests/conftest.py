@@ -16,8 +16,9 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle():
+    import __graft_entry__
+    __graft_entry__.build_oracle()
     from oracle import oracle as o
-    o.build()
     return o
 
 

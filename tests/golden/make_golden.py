@@ -65,7 +65,7 @@ def make_inputs(name, ncell, comps, zero_mean):
 
 def main():
     if not oracle.available("reference"):
-        oracle.build()
+        oracle.build(os.environ.get("PS_REFERENCE_ROOT", "/root/reference"))
     for name, ncell, bc, dx, reg, opts, comps, zm in CASES + CASES2D:
         B = make_inputs(name, ncell, comps, zm)
         solve = oracle.solve3d if len(ncell) == 3 else oracle.solve2d

@@ -11,7 +11,13 @@ import pytest
 from conftest import ROOT
 
 HEADER = os.path.join(ROOT, "include", "poisson_solver_gb300.h")
-REF_TESTS = os.path.join(os.environ.get("PS_REFERENCE_ROOT", "/root/reference"), "c++", "test")
+
+
+def ref_tests_dir():
+    """The reference's own test programs, where the oracle build found the reference."""
+    from oracle import oracle
+    root = os.environ.get("PS_REFERENCE_ROOT") or oracle.reference_root()
+    return os.path.join(root, "c++", "test") if root else None
 
 
 def declared_functions():
@@ -101,9 +107,10 @@ def test_dropin_header_compiles_and_links(native, tmp_path):
 
 @pytest.mark.parametrize("prog", ["unbounded3d", "periodic3d", "mixed_ppf3d", "mixed_ffp3d",
                                   "unbounded2d", "periodic2d", "mixed2d"])
-def test_reference_validation_programs_build_unchanged(native, tmp_path, prog):
+def test_reference_validation_programs_build_unchanged(native, oracle, tmp_path, prog):
     """The reference's own 3D and 2D test programs compile and link, unmodified, against the drop-in."""
-    src = os.path.join(REF_TESTS, prog, "sources", "main.cpp")
+    tests_dir = ref_tests_dir()
+    src = os.path.join(tests_dir, prog, "sources", "main.cpp") if tests_dir else ""
     if not os.path.exists(src):
         pytest.skip("reference test sources not present")
     from poisson_solver_gb300 import _lib
