@@ -367,37 +367,52 @@ def replica_throughput(points_per_rank, steps, elapsed_s_max, world):
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(n, reg, reps=2):
-    """Oracle port (the reference algorithm, one thread) on an n^3 sample: Mpts/s of solve3d."""
+def ring_sample(w, n):
+    """The workload's source (same rings, same seed) sampled on an n^3 grid of the same domain."""
+    ws = dict(w)
+    ws["n"] = n
+    return [b.numpy() for b in make_source(ws, "cpu")]
+
+
+def cpu_sample(w, n, reps=2, threads=0):
+    """Oracle port (the reference algorithm) on an n^3 sample of the workload's
+    source, its pencils shared over `threads` host threads (0: every core):
+    (Mpts/s of push + solve3d, best seconds, threads used)."""
     from oracle import oracle
-    w = dict(WORKLOADS["rings512"])
-    w["n"] = n
-    B = [b.numpy() for b in make_source(w, "cpu")]
+    used = oracle.set_threads(threads)
+    B = ring_sample(w, n)
     dx = 2.0 / n
     best = None
     for _ in range(reps):
-        _, sec = oracle.solve3d_timed((n, n, n), (0, 0, 0), (dx,) * 3, B, reg, curl=True)
+        _, sec = oracle.solve3d_timed((n, n, n), (0, 0, 0), (dx,) * 3, B, w["reg"], curl=True)
         best = sec[1] if best is None else min(best, sec[1])
-    return n ** 3 / best / 1e6, best
+    return n ** 3 / best / 1e6, best, used
 
 
-def _ref_worker(args):
-    n, reg, steps, warmup = args
+def oracle_parity(psg, w, n=128):
+    """The GPU solve (FP64 and FP32 transforms) against the oracle on an n^3
+    sample of the workload's source: relative L2 and maximum error (max
+    |A - A_ref| / max |A_ref|) of each."""
     from oracle import oracle
-    rng = np.random.default_rng(n)
-    B = [rng.standard_normal((n, n, n)) for _ in range(3)]
-    dx = 2.0 / n
-    times = []
-    for s in range(warmup + steps):
-        _, sec = oracle.solve3d_timed((n, n, n), (0, 0, 0), (dx,) * 3, B, reg, curl=True)
-        if s >= warmup:
-            times.append(sec[1])
-    return times
+    oracle.set_threads(0)
+    B = ring_sample(w, n)
+    nc, dx = (n, n, n), (2.0 / n,) * 3
+    ref, _ = oracle.solve3d(nc, (0, 0, 0), dx, B, w["reg"], curl=True)
+    out = {"grid": [n, n, n], "source": "the same rings and seed sampled at %d^3" % n}
+    for prec in ("fp64", "fp32"):
+        got, _ = psg.solve(nc, (0, 0, 0), dx, B, w["reg"], curl=True, precision=prec)
+        num = sum(float(np.sum((g - r) ** 2)) for g, r in zip(got, ref))
+        den = sum(float(np.sum(r ** 2)) for r in ref)
+        dmax = max(float(np.abs(g - r).max()) for g, r in zip(got, ref))
+        rmax = max(float(np.abs(r).max()) for r in ref)
+        out[prec] = {"rel_l2": (num / den) ** 0.5, "max_err": dmax / rmax}
+    return out
 
 
 def _ref_batch_worker(args):
     nc, bc, ncomp, blobs, reg, steps, warmup = args
     from oracle import oracle
+    oracle.set_threads(1)  # one problem per process and core
     B = [b.numpy() for b in batch_source(nc, blobs, "cpu")] + [None] * (3 - ncomp)
     dx = tuple(2.0 / n for n in nc)
     times = []
@@ -442,6 +457,7 @@ def run_reference_batch(args, w, world):
 def _ref_mixed_worker(args):
     nc, reg, steps, warmup, seed = args
     from oracle import oracle
+    oracle.set_threads(1)  # one sample per process and core
     w = dict(WORKLOADS["mixed512"])
     w["n"], w["seed"] = nc, seed
     B, dx = mixed_source(w, "cpu")
@@ -491,25 +507,30 @@ def run_reference(args, w):
         return run_reference_batch(args, w, world)
     if w.get("kind") == "mixed":
         return run_reference_mixed(args, w, world)
-    import multiprocessing as mp
     from oracle import oracle
     oracle.build()
-    cores = os.cpu_count() or 1
-    n = 64
-    ctx = mp.get_context("spawn")
+    n = 128
+    cores = oracle.set_threads(0)
+    B = ring_sample(w, n)
+    dx = 2.0 / n
     t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_ref_worker, [(n, w["reg"], args.steps, args.warmup)] * cores)
+    times = []
+    for s in range(args.warmup + args.steps):
+        _, sec = oracle.solve3d_timed((n, n, n), (0, 0, 0), (dx,) * 3, B, w["reg"], curl=True)
+        if s >= args.warmup:
+            times.append(sec[1])
     wall = time.perf_counter() - t0
-    slowest = max(sum(t) for t in res)
-    value = cores * n ** 3 * args.steps / slowest / 1e6
-    sample = (f"{cores} concurrent single-thread solves of a {n}^3 sample of the workload "
-              f"(padded {2 * n}^3, 3 components, curl, reg {w['reg']}), solve3d time only")
+    total = sum(times)
+    value = n ** 3 * args.steps / total / 1e6
+    sample = (f"the workload's source (same rings and seed) sampled at {n}^3 (padded {2 * n}^3, 3 components, "
+              f"curl, reg {w['reg']}); one solve a step, its pencils shared over {cores} host threads "
+              f"(the reference shares them over MPI ranks); push + solve3d time, kernel build excluded")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": slowest / args.steps * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": w["desc"], "sample_grid": [n, n, n]},
+        "data": "synthetic", "config": {"workload": w["desc"], "sample_grid": [n, n, n],
+                                        "source_seed": w["seed"], "reg_order": w["reg"], "output": "curl"},
         "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
@@ -597,6 +618,7 @@ def run_ours(args, w):
     num = sum(float(torch.sum((a - b) ** 2)) for a, b in zip(A, A64))
     den = sum(float(torch.sum(b ** 2)) for b in A64)
     rel = (num / den) ** 0.5
+    max_err = max(float((a - b).abs().max()) for a, b in zip(A, A64)) / max(float(b.abs().max()) for b in A64)
 
     # end to end through the public API with pinned host buffers
     ps.set_precision("fp32")
@@ -639,14 +661,17 @@ def run_ours(args, w):
 
     if rank != 0:
         return 0
-    cpu = None
+    cpu = parity = None
     if world == 1 and not args.no_cpu:
-        log("[rank 0] CPU baseline (oracle port, one thread)")
-        ns = 128  # 4-12 s a solve on one host core: a bounded sample of the workload
-        cv, ct = cpu_sample(ns, w["reg"], reps=2)
-        cpu = {"value": cv, "unit": "Mpts/s", "cores": 1, "kind": "port",
-               "sample": f"{ns}^3 sample of the workload (padded {2 * ns}^3, 3 components, curl, reg {w['reg']}), "
-                         f"oracle/ps_oracle.c solve3d on one host thread, best of 2: {ct:.2f} s"}
+        log("[rank 0] GPU solve vs the oracle at 128^3")
+        parity = oracle_parity(psg, w, 128)
+        log("[rank 0] CPU baseline (oracle port on the host cores)")
+        ns = 128  # about a second a solve on the host cores: a bounded sample of the workload
+        cv, ct, used = cpu_sample(w, ns, reps=2)
+        cpu = {"value": cv, "unit": "Mpts/s", "cores": used, "kind": "port",
+               "sample": f"the workload's source sampled at {ns}^3 (padded {2 * ns}^3, 3 components, curl, "
+                         f"reg {w['reg']}), oracle/ps_oracle.c push + solve3d with its pencils shared over "
+                         f"{used} host threads, best of 2: {ct:.2f} s"}
     line = {
         "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms32_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -666,6 +691,8 @@ def run_ours(args, w):
         "fp64": {"value": value64, "ms_per_step": ms64_max / K64, "passes_ms": dict(zip(PASS_NAMES, pass64))},
         "mixed_vs_fp64_speedup": value / value64,
         "rel_l2_fp32_vs_fp64": rel,
+        "max_err_fp32_vs_fp64": max_err,
+        "parity_vs_oracle": parity,
         "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": 3 * points * 8,
                 "d2h_bytes_per_step": 3 * points * 8, "steps": Kp,
                 "method": "three handles, each on its own stream and host thread, take the steps in turn "
@@ -888,12 +915,14 @@ def run_batch(args, w):
     cpu = None
     if world == 1 and not args.no_cpu:
         from oracle import oracle
+        used = oracle.set_threads(0)
         nc, bc, nco, bl = min(probs, key=lambda p: np.prod(padded(p[0], p[1])))
         B = [t.cpu().numpy() for t in batch_source(nc, bl, "cpu")] + [None] * (3 - nco)
         _, sec = oracle.solve3d_timed(nc, bc, tuple(2.0 / n for n in nc), B, w["reg"])
-        cpu = {"value": int(np.prod(nc)) / sec[1] / 1e6, "unit": "Mpts/s", "cores": 1, "kind": "port",
+        cpu = {"value": int(np.prod(nc)) / sec[1] / 1e6, "unit": "Mpts/s", "cores": used, "kind": "port",
                "sample": f"the smallest problem of the batch ({nc[0]}x{nc[1]}x{nc[2]}, bc {bc}, {nco} components), "
-                         f"oracle/ps_oracle.c solve3d on one host thread: {sec[1]:.2f} s"}
+                         f"oracle/ps_oracle.c push + solve3d with its pencils shared over {used} host threads: "
+                         f"{sec[1]:.2f} s"}
     line = {
         "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms32_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

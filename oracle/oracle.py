@@ -96,6 +96,14 @@ def _lib(kind: str) -> ctypes.CDLL:
     return lib
 
 
+def set_threads(n: int) -> int:
+    """Threads of the port's solves (n <= 0: all cores); returns the count in use."""
+    lib = _lib("port")
+    lib.oracle_set_threads(ctypes.c_int(int(n)))
+    lib.oracle_threads.restype = ctypes.c_int
+    return int(lib.oracle_threads())
+
+
 def _fn(kind: str, name: str):
     return getattr(_lib(kind), ("oracle_" if kind == "port" else "ref_") + name)
 

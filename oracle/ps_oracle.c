@@ -30,7 +30,33 @@
 
 #include "ps_oracle.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 typedef double complex cplx;
+
+/* Threads: pencils (and kernel samples) are shared out over OpenMP threads.
+ * Each pencil's arithmetic is the same whichever thread runs it, so results
+ * do not depend on the thread count; the reference spreads the same pencils
+ * over MPI ranks. */
+void oracle_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int oracle_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
 
 static const double PI = 3.1415926535897932;
 static const double EULER_GAMMA = 0.5772156649015329;
@@ -243,22 +269,26 @@ static void transform_axis(cplx *a, const int p[3], int axis, int shift, int inv
 {
     int n = p[axis];
     size_t stride = axis == 0 ? 1 : axis == 1 ? (size_t)p[0] : (size_t)p[0] * p[1];
-    cplx *pen = malloc(sizeof(cplx) * (size_t)n), *w = malloc(sizeof(cplx) * (size_t)n);
     int o1 = axis == 0 ? p[1] : p[0];
     int o2 = axis == 2 ? p[1] : p[2];
-    for (int b = 0; b < o2; ++b) {
-        for (int q = 0; q < o1; ++q) {
-            size_t base;
-            if (axis == 0) base = ((size_t)b * p[1] + q) * p[0];
-            else if (axis == 1) base = (size_t)b * p[1] * p[0] + q;
-            else base = (size_t)b * p[0] + q;
-            for (int m = 0; m < n; ++m) pen[m] = a[base + m * stride];
-            if (shift) fft_shift(pen, n);
-            glassman(pen, w, n, inverse);
-            for (int m = 0; m < n; ++m) a[base + m * stride] = pen[m];
+#pragma omp parallel
+    {
+        cplx *pen = malloc(sizeof(cplx) * (size_t)n), *w = malloc(sizeof(cplx) * (size_t)n);
+#pragma omp for collapse(2) schedule(static)
+        for (int b = 0; b < o2; ++b) {
+            for (int q = 0; q < o1; ++q) {
+                size_t base;
+                if (axis == 0) base = ((size_t)b * p[1] + q) * p[0];
+                else if (axis == 1) base = (size_t)b * p[1] * p[0] + q;
+                else base = (size_t)b * p[0] + q;
+                for (int m = 0; m < n; ++m) pen[m] = a[base + m * stride];
+                if (shift) fft_shift(pen, n);
+                glassman(pen, w, n, inverse);
+                for (int m = 0; m < n; ++m) a[base + m * stride] = pen[m];
+            }
         }
+        free(pen); free(w);
     }
-    free(pen); free(w);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -371,6 +401,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         c[0] = 1.0;
         for (int n = 1; n <= nc - 1; ++n) c[n] = c[n - 1] * 1.0 / (double)n;
         K->zeta = malloc(sizeof(double) * np);
+#pragma omp parallel for collapse(2) schedule(static)
         for (int k = 0; k < p[2]; ++k)
             for (int j = 0; j < p[1]; ++j)
                 for (int i = 0; i < p[0]; ++i) {
@@ -394,9 +425,10 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         double sigma = h / PI;
         double xmin[3];
         for (int d = 0; d < 3; ++d) xmin[d] = -(0.5 * (double)p[d]) * dx[d];
+#pragma omp parallel for collapse(2) schedule(dynamic, 4)
         for (int k = 0; k < p[2]; ++k) {
-            double z = xmin[2] + (double)k * dx[2];
             for (int j = 0; j < p[1]; ++j) {
+                double z = xmin[2] + (double)k * dx[2];
                 double y = xmin[1] + (double)j * dx[1];
                 for (int i = 0; i < p[0]; ++i) {
                     double x = xmin[0] + (double)i * dx[0];
@@ -429,6 +461,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         }
         fft_shift(pen, n);
         glassman(pen, w, n, 0);
+#pragma omp parallel for collapse(2) schedule(static)
         for (int k = 0; k < p[2]; ++k)
             for (int j = 0; j < p[1]; ++j)
                 for (int i = 0; i < p[0]; ++i) {
@@ -451,6 +484,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         double sigma = h2 / PI;
         double C2 = log(2.0 * sigma) - EULER_GAMMA;
         double xmin0 = -(0.5 * (double)p[0]) * dx[0], xmin1 = -(0.5 * (double)p[1]) * dx[1];
+#pragma omp parallel for schedule(dynamic, 4)
         for (int j = 0; j < p[1]; ++j) {
             double y = xmin1 + (double)j * dx[1];
             for (int i = 0; i < p[0]; ++i) {
@@ -463,6 +497,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         }
         transform_axis(G2, p2, 0, 1, 0);
         transform_axis(G2, p2, 1, 1, 0);
+#pragma omp parallel for collapse(2) schedule(static)
         for (int k = 0; k < p[2]; ++k)
             for (int j = 0; j < p[1]; ++j)
                 for (int i = 0; i < p[0]; ++i) {
@@ -501,6 +536,7 @@ static int kernel_build(kernel_t *K, const int ncell[3], const int bc[3], const 
         free(pen); free(w);
     } else {
         /* Periodic (greens3d.cpp:478-521): 1/|k|^2 with the zero mode removed. */
+#pragma omp parallel for collapse(2) schedule(static)
         for (int k = 0; k < p[2]; ++k)
             for (int j = 0; j < p[1]; ++j)
                 for (int i = 0; i < p[0]; ++i) {
@@ -614,137 +650,151 @@ static int solve_core(const int ncell[3], const int bc[3], const double dx[3], i
     }
     int lmax = px > py ? px : py;
     if (nfft > lmax) lmax = nfft;
-    cplx *pen = malloc(sizeof(cplx) * (size_t)lmax), *w = malloc(sizeof(cplx) * (size_t)lmax);
-    cplx *pr[3], *pl[3];
-    for (int c = 0; c < 3; ++c) {
-        pr[c] = malloc(sizeof(cplx) * (size_t)nfft);
-        pl[c] = malloc(sizeof(cplx) * (size_t)nfft);
-    }
 
     /* push (push.cpp:284-368): real input, x zero-padded to Px; rows j >= Ny
      * stay zero, as the x-to-y pencil map leaves them (map.cpp:376-384). */
     for (int c = 0; c < 3; ++c) {
         if (!r[c]) continue;
+#pragma omp parallel for collapse(2) schedule(static)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i)
                     rhs[c][((size_t)k * py + j) * px + i] = CMPLX(B[c][((size_t)k * ny + j) * nx + i], 0.0);
     }
 
-    /* x forward (solve3d.cpp:118-173), rows j < Ny. */
-    for (int c = 0; c < 3; ++c) {
-        if (!r[c]) continue;
-        for (int k = 0; k < nz; ++k)
-            for (int j = 0; j < ny; ++j) glassman(rhs[c] + ((size_t)k * py + j) * px, w, px, 0);
-    }
-    /* y forward (solve3d.cpp:183-237). */
-    for (int c = 0; c < 3; ++c) {
-        if (!r[c]) continue;
-        for (int k = 0; k < nz; ++k)
-            for (int i = 0; i < px; ++i) {
-                cplx *base = rhs[c] + (size_t)k * py * px + i;
-                for (int j = 0; j < py; ++j) pen[j] = base[(size_t)j * px];
-                glassman(pen, w, py, 0);
-                for (int j = 0; j < py; ++j) base[(size_t)j * px] = pen[j];
-            }
-    }
+#pragma omp parallel
+    {
+        cplx *pen = malloc(sizeof(cplx) * (size_t)lmax), *w = malloc(sizeof(cplx) * (size_t)lmax);
+        cplx *pr[3], *pl[3];
+        for (int c = 0; c < 3; ++c) {
+            pr[c] = malloc(sizeof(cplx) * (size_t)nfft);
+            pl[c] = malloc(sizeof(cplx) * (size_t)nfft);
+        }
 
-    /* z forward, spectral operation, z inverse (solve3d.cpp:243-440). */
-    const cplx *ikX = K.ik[0], *ikY = K.ik[1], *ikZ = K.ik[2];
-    for (int i = 0; i < px; ++i) {
-        for (int j = 0; j < py; ++j) {
-            for (int c = 0; c < 3; ++c) {
-                if (!r[c]) continue;
-                for (int k = 0; k < nz; ++k) pr[c][k] = rhs[c][((size_t)k * py + j) * px + i];
-                for (int k = nz; k < nfft; ++k) pr[c][k] = CMPLX(0.0, 0.0);
-                glassman(pr[c], w, nfft, 0);
-            }
-            /* grad reads component d, or component x where d was not pushed
-             * (2D: always x, solve2d.cpp:298-299) */
-            const cplx *gY = (r[1] && !two_d) ? pr[1] : pr[0], *gZ = r[2] ? pr[2] : pr[0];
-            for (int k = 0; k < nfft; ++k) {
-                size_t q = ((size_t)k * py + j) * px + i;
-                if (K.zeta && !K.gm)
-                    for (int c = 0; c < 3; ++c)
-                        if (r[c]) pr[c][k] *= K.zeta[q];
-                cplx G = K.G[q];
-                if (two_d) {
-                    /* solve2d.cpp:292-325 */
-                    if (grad) {
+        /* x forward (solve3d.cpp:118-173), rows j < Ny. */
+        for (int c = 0; c < 3; ++c) {
+            if (!r[c]) continue;
+#pragma omp for collapse(2) schedule(static)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j) glassman(rhs[c] + ((size_t)k * py + j) * px, w, px, 0);
+        }
+        /* y forward (solve3d.cpp:183-237). */
+        for (int c = 0; c < 3; ++c) {
+            if (!r[c]) continue;
+#pragma omp for collapse(2) schedule(static)
+            for (int k = 0; k < nz; ++k)
+                for (int i = 0; i < px; ++i) {
+                    cplx *base = rhs[c] + (size_t)k * py * px + i;
+                    for (int j = 0; j < py; ++j) pen[j] = base[(size_t)j * px];
+                    glassman(pen, w, py, 0);
+                    for (int j = 0; j < py; ++j) base[(size_t)j * px] = pen[j];
+                }
+        }
+
+        /* z forward, spectral operation, z inverse (solve3d.cpp:243-440). */
+        const cplx *ikX = K.ik[0], *ikY = K.ik[1], *ikZ = K.ik[2];
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < px; ++i) {
+            for (int j = 0; j < py; ++j) {
+                for (int c = 0; c < 3; ++c) {
+                    if (!r[c]) continue;
+                    for (int k = 0; k < nz; ++k) pr[c][k] = rhs[c][((size_t)k * py + j) * px + i];
+                    for (int k = nz; k < nfft; ++k) pr[c][k] = CMPLX(0.0, 0.0);
+                    glassman(pr[c], w, nfft, 0);
+                }
+                /* grad reads component d, or component x where d was not pushed
+                 * (2D: always x, solve2d.cpp:298-299) */
+                const cplx *gY = (r[1] && !two_d) ? pr[1] : pr[0], *gZ = r[2] ? pr[2] : pr[0];
+                for (int k = 0; k < nfft; ++k) {
+                    size_t q = ((size_t)k * py + j) * px + i;
+                    if (K.zeta && !K.gm)
+                        for (int c = 0; c < 3; ++c)
+                            if (r[c]) pr[c][k] *= K.zeta[q];
+                    cplx G = K.G[q];
+                    if (two_d) {
+                        /* solve2d.cpp:292-325 */
+                        if (grad) {
+                            pl[0][k] = ikX[i] * G * pr[0][k];
+                            pl[1][k] = ikY[j] * G * pr[0][k];
+                        } else if (div) {
+                            pl[0][k] = G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k]);
+                        } else if (curl) {
+                            pl[0][k] = ikY[j] * G * pr[2][k];
+                            pl[1][k] = -ikX[i] * G * pr[2][k];
+                        } else {
+                            for (int c = 0; c < 3; ++c)
+                                if (l[c]) pl[c][k] = G * pr[c][k];
+                        }
+                    } else if (grad) {
                         pl[0][k] = ikX[i] * G * pr[0][k];
-                        pl[1][k] = ikY[j] * G * pr[0][k];
+                        pl[1][k] = ikY[j] * G * gY[k];
+                        pl[2][k] = ikZ[k] * G * gZ[k];
                     } else if (div) {
-                        pl[0][k] = G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k]);
+                        pl[0][k] = G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k] + ikZ[k] * pr[2][k]);
                     } else if (curl) {
-                        pl[0][k] = ikY[j] * G * pr[2][k];
-                        pl[1][k] = -ikX[i] * G * pr[2][k];
+                        pl[0][k] = G * (ikY[j] * pr[2][k] - ikZ[k] * pr[1][k]);
+                        pl[1][k] = G * (ikZ[k] * pr[0][k] - ikX[i] * pr[2][k]);
+                        pl[2][k] = G * (ikX[i] * pr[1][k] - ikY[j] * pr[0][k]);
                     } else {
                         for (int c = 0; c < 3; ++c)
                             if (l[c]) pl[c][k] = G * pr[c][k];
                     }
-                } else if (grad) {
-                    pl[0][k] = ikX[i] * G * pr[0][k];
-                    pl[1][k] = ikY[j] * G * gY[k];
-                    pl[2][k] = ikZ[k] * G * gZ[k];
-                } else if (div) {
-                    pl[0][k] = G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k] + ikZ[k] * pr[2][k]);
-                } else if (curl) {
-                    pl[0][k] = G * (ikY[j] * pr[2][k] - ikZ[k] * pr[1][k]);
-                    pl[1][k] = G * (ikZ[k] * pr[0][k] - ikX[i] * pr[2][k]);
-                    pl[2][k] = G * (ikX[i] * pr[1][k] - ikY[j] * pr[0][k]);
-                } else {
-                    for (int c = 0; c < 3; ++c)
-                        if (l[c]) pl[c][k] = G * pr[c][k];
+                    /* the Gaussian family filters the returned right-hand side after
+                     * the kernel has acted on the unfiltered one */
+                    const int rp = reproject && r[0] && r[1] && r[2];
+                    cplx div_psi = rp ? G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k] + ikZ[k] * pr[2][k]) : 0.0;
+                    if (K.gm)
+                        for (int c = 0; c < 3; ++c)
+                            if (r[c]) pr[c][k] *= K.zeta[q];
+                    if (rp) {
+                        pr[0][k] += ikX[i] * div_psi;
+                        pr[1][k] += ikY[j] * div_psi;
+                        pr[2][k] += ikZ[k] * div_psi;
+                    }
                 }
-                /* the Gaussian family filters the returned right-hand side after
-                 * the kernel has acted on the unfiltered one */
-                const int rp = reproject && r[0] && r[1] && r[2];
-                cplx div_psi = rp ? G * (ikX[i] * pr[0][k] + ikY[j] * pr[1][k] + ikZ[k] * pr[2][k]) : 0.0;
-                if (K.gm)
-                    for (int c = 0; c < 3; ++c)
-                        if (r[c]) pr[c][k] *= K.zeta[q];
-                if (rp) {
-                    pr[0][k] += ikX[i] * div_psi;
-                    pr[1][k] += ikY[j] * div_psi;
-                    pr[2][k] += ikZ[k] * div_psi;
-                }
-            }
-            for (int c = 0; c < 3; ++c) {
-                if (r[c]) glassman(pr[c], w, nfft, 1);
-                if (l[c]) glassman(pl[c], w, nfft, 1);
-            }
-            for (int k = 0; k < nz; ++k) {
-                size_t q = ((size_t)k * py + j) * px + i;
                 for (int c = 0; c < 3; ++c) {
-                    if (r[c]) rhs[c][q] = pr[c][k] / (double)nfft;
-                    if (l[c]) lhs[c][q] = pl[c][k] / (double)nfft;
+                    if (r[c]) glassman(pr[c], w, nfft, 1);
+                    if (l[c]) glassman(pl[c], w, nfft, 1);
+                }
+                for (int k = 0; k < nz; ++k) {
+                    size_t q = ((size_t)k * py + j) * px + i;
+                    for (int c = 0; c < 3; ++c) {
+                        if (r[c]) rhs[c][q] = pr[c][k] / (double)nfft;
+                        if (l[c]) lhs[c][q] = pl[c][k] / (double)nfft;
+                    }
                 }
             }
         }
-    }
 
-    /* y inverse (solve3d.cpp:447-530). */
-    for (int f = 0; f < 6; ++f) {
-        cplx *a = f < 3 ? rhs[f] : lhs[f - 3];
-        if (!a) continue;
-        for (int k = 0; k < nz; ++k)
-            for (int i = 0; i < px; ++i) {
-                cplx *base = a + (size_t)k * py * px + i;
-                for (int j = 0; j < py; ++j) pen[j] = base[(size_t)j * px];
-                glassman(pen, w, py, 1);
-                for (int j = 0; j < py; ++j) base[(size_t)j * px] = pen[j] / (double)py;
-            }
-    }
-    /* y-to-x pencil map keeps rows j < Ny; x inverse (solve3d.cpp:541-629). */
-    for (int f = 0; f < 6; ++f) {
-        cplx *a = f < 3 ? rhs[f] : lhs[f - 3];
-        if (!a) continue;
-        for (int k = 0; k < nz; ++k)
-            for (int j = 0; j < ny; ++j) {
-                cplx *row = a + ((size_t)k * py + j) * px;
-                glassman(row, w, px, 1);
-                for (int i = 0; i < px; ++i) row[i] = row[i] / (double)px;
-            }
+        /* y inverse (solve3d.cpp:447-530). */
+        for (int f = 0; f < 6; ++f) {
+            cplx *a = f < 3 ? rhs[f] : lhs[f - 3];
+            if (!a) continue;
+#pragma omp for collapse(2) schedule(static)
+            for (int k = 0; k < nz; ++k)
+                for (int i = 0; i < px; ++i) {
+                    cplx *base = a + (size_t)k * py * px + i;
+                    for (int j = 0; j < py; ++j) pen[j] = base[(size_t)j * px];
+                    glassman(pen, w, py, 1);
+                    for (int j = 0; j < py; ++j) base[(size_t)j * px] = pen[j] / (double)py;
+                }
+        }
+        /* y-to-x pencil map keeps rows j < Ny; x inverse (solve3d.cpp:541-629). */
+        for (int f = 0; f < 6; ++f) {
+            cplx *a = f < 3 ? rhs[f] : lhs[f - 3];
+            if (!a) continue;
+#pragma omp for collapse(2) schedule(static)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j) {
+                    cplx *row = a + ((size_t)k * py + j) * px;
+                    glassman(row, w, px, 1);
+                    for (int i = 0; i < px; ++i) row[i] = row[i] / (double)px;
+                }
+        }
+        for (int c = 0; c < 3; ++c) {
+            free(pr[c]); free(pl[c]);
+        }
+        free(pen); free(w);
     }
 
     double t2 = now_s();
@@ -761,9 +811,8 @@ static int solve_core(const int ncell[3], const int bc[3], const double dx[3], i
     }
 
     for (int c = 0; c < 3; ++c) {
-        free(rhs[c]); free(lhs[c]); free(pr[c]); free(pl[c]);
+        free(rhs[c]); free(lhs[c]);
     }
-    free(pen); free(w);
     kernel_free(&K);
     if (seconds) {
         seconds[0] = t1 - t0;        /* setup3d: kernel build */

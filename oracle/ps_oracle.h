@@ -20,6 +20,11 @@ extern "C" {
  * dir < 0 forward (e^{-2 pi i jk/n}), dir > 0 inverse. */
 int oracle_fft(int n, int dir, double *data);
 
+/* OpenMP threads the solves and kernel builds share their pencils over
+ * (n <= 0 leaves the default: all cores); results do not depend on it. */
+void oracle_set_threads(int n);
+int oracle_threads(void);
+
 /* Sine integral Si(x) and the integral of (1 - J0(t))/t from 0 to x, as the
  * reference evaluates them. */
 double oracle_sine_int(double x);
