@@ -43,7 +43,7 @@ typedef double complex cplx;
 void oracle_set_threads(int n)
 {
 #ifdef _OPENMP
-    if (n > 0) omp_set_num_threads(n);
+    omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
 #else
     (void)n;
 #endif

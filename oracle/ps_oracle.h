@@ -21,7 +21,7 @@ extern "C" {
 int oracle_fft(int n, int dir, double *data);
 
 /* OpenMP threads the solves and kernel builds share their pencils over
- * (n <= 0 leaves the default: all cores); results do not depend on it. */
+ * (n <= 0: one a core); results do not depend on it. */
 void oracle_set_threads(int n);
 int oracle_threads(void);
 

@@ -248,6 +248,7 @@ int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, 
                   : c.fam == 'w' ? PS_FAMILY_WIDE
                   : c.fam == 't' ? PS_FAMILY_TMEM
                   : c.fam == 'q' ? PS_FAMILY_TMA
+                  : c.fam == 'c' ? PS_FAMILY_TC
                                  : PS_FAMILY_RUNTIME;
         *lines = c.B;
     });

@@ -307,346 +307,6 @@ int yq_half(int inverse, int L, int n_in, int n_out)
 }
 
 
-// ---------------------------------------------------------------------------
-// Fused x and y forward passes (x and y both unbounded, of the same length L;
-// FP32). One persistent launch takes two kinds of tile from one queue:
-//   x tiles: NL row pairs of a chunk of zc z-planes of one component, a warp
-//     per line as in k_xfq (FP64 rows straight from global memory, half
-//     spectra stored with plain stores);
-//   y tiles: 8 (32 / TPL) columns of one plane, as k_yq's forward tiles.
-// Chunk k's y tiles follow chunk k + 1's x tiles in the queue
-// ([X0][X1][Y0][X2][Y1]...[Y_{K-1}]), and the load warp starts a y tile's
-// copies only once every x line of its chunk has been written (a per-chunk
-// counter, waited for with a bounded spin). A chunk's x output is then still
-// in L2 when its y tiles read it and overwrite it in place with the padded
-// y spectra, so it does not make a round trip through DRAM: the pair of
-// passes moves the FP64 input and the y output only. Opt-in (PS_XY_FUSION=1):
-// with one CTA of 8 compute warps an SM its x tiles, which load their FP64
-// rows from global memory (an L2 bulk prefetch started when the tile is handed
-// out), run far below the 24-warp k_xfq, and the launch takes 3.55 ms at 512^3
-// against 2.9 ms for the two passes.
-template <int L> struct Xy {
-    using Q = Yq<L, false, true>;
-    static constexpr int TPL = L / 32;
-    static constexpr int NL = YQ_COMPUTE / TPL;           // x lines (row pairs) a tile
-    static constexpr int KPER = (L / 2 + 1 + TPL - 1) / TPL;  // half-spectrum elements a thread
-    static constexpr int WARPS = YQ_COMPUTE / 32;          // count increments an x tile
-    static_assert(NL == Q::B, "x lines and y columns share the line buffers");
-};
-
-// tile j of the queue -> (is_y, chunk, index within the chunk's block). The
-// queue is X_0 .. X_{D-1}, then [X_{s+D}][Y_s] for s < K - D, then
-// Y_{K-D} .. Y_{K-1}: a chunk's y tiles come D chunks of x tiles after its
-// own x tiles (D = p.delay, at most K), enough to cover the tiles in flight.
-__device__ __forceinline__ void xy_decode(const XyPlan &p, int j, bool &is_y, int &k, int &t)
-{
-    const int nx = p.nxl, ny = p.nyt, seg = nx + ny, K = p.nchunk;
-    const int D = p.delay < K ? p.delay : K;
-    if (j < D * nx) {
-        is_y = false;
-        k = j / nx;
-        t = j - k * nx;
-        return;
-    }
-    const int jj = j - D * nx, nseg = K - D;
-    if (jj < nseg * seg) {
-        const int s = jj / seg, off = jj - s * seg;
-        is_y = off >= nx;
-        k = is_y ? s : s + D;
-        t = is_y ? off - nx : off;
-        return;
-    }
-    const int j2 = jj - nseg * seg;
-    is_y = true;
-    k = nseg + j2 / ny;
-    t = j2 - (j2 / ny) * ny;
-}
-
-// Bounded wait until *cnt >= target (acquire); false after 1 s or 2^26 polls.
-__device__ __noinline__ bool wait_count(const int *cnt, int target)
-{
-    const uint64_t t0 = globaltimer();
-    for (uint32_t i = 0; i < (1u << 26); ++i) {
-        int v;
-        asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
-        if (v >= target) return true;
-        if ((i & 63) == 63) {
-            if (globaltimer() - t0 > WAIT_LIMIT_NS) return false;
-            __nanosleep(128);
-        }
-    }
-    return false;
-}
-
-template <int L>
-__global__ void __launch_bounds__(YQ_THREADS, 1)
-    k_xyq(const XFwdArgs xa, const ColArgs a, const __grid_constant__ YqMaps maps, const XyPlan p, int *status)
-{
-    using C = float2;
-    using PL = WP<L>;
-    using X = Xy<L>;
-    using Q = typename X::Q;
-    constexpr int LAST = PL::NST - 1;
-    using T0 = St<L, 0>;
-    using TL = St<L, LAST>;
-    static_assert(T0::U == 1 && T0::R == 32 && PL::NST == 2, "two radix-32 stages");
-    static_assert(T0::NBF % 8 == 0 && TL::M % 8 == 0 && TL::TPL % 8 == 0 && TL::U * TL::TPL <= TL::M,
-                  "staged rows share t's swizzle term");
-
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    const uint32_t sb = smem_u32(base);
-    C *TW = reinterpret_cast<C *>(base + Q::TWO);
-    const uint32_t full0 = sb + Q::bars(PL::NTW), empty0 = full0 + 16, ofull0 = full0 + 32, oempty0 = full0 + 48;
-    volatile int *itile = reinterpret_cast<volatile int *>(base + Q::bars(PL::NTW) + 64);
-    volatile int *otile = itile + 2;
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (tid == 0) {
-        for (int s = 0; s < 2; ++s) {
-            mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, YQ_COMPUTE);
-            mbar_init(ofull0 + 8 * s, YQ_COMPUTE);
-            mbar_init(oempty0 + 8 * s, 1);
-        }
-        fence_mbar_init();
-    }
-    load_twiddles<C, PL::NTW>(TW, a.plan.table);
-    __syncthreads();
-
-    // y tile t of chunk k -> component, plane, first column
-    auto ytile = [&](int k, int t, int &c, int &z, int &x0) {
-        c = k / p.nzc;
-        z = (k - c * p.nzc) * p.zc + t / p.nxt;
-        x0 = (t % p.nxt) * Q::B;
-    };
-    bool ok = true;
-
-    if (warp == LOAD_WARP) {
-        if (lane == 0) {
-            int last[2] = {-1, -1};
-            int jn = atomicAdd(status + 1, 1);
-            for (int q = 0;; ++q) {
-                const int s = q % Q::NIN;
-                if (q >= Q::NIN && !mbar_wait(empty0 + 8 * s, ((q / Q::NIN) - 1) & 1)) {
-                    ok = false;
-                    break;
-                }
-                last[s] = -1;
-                const int j = jn;
-                if (j >= p.ntiles) {
-                    itile[s] = -1;
-                    mbar_arrive(full0 + 8 * s);
-                    break;
-                }
-                bool is_y;
-                int k, t;
-                xy_decode(p, j, is_y, k, t);
-                itile[s] = j;
-                if (!is_y) {
-                    // an x tile: its rows are one contiguous run of the input;
-                    // start pulling them into L2, then hand over the index
-                    const int c = k / p.nzc, z0 = (k - c * p.nzc) * p.zc;
-                    const long long r0 = 2LL * t * X::NL, rows_chunk = (long long)p.zc * xa.rows_y;
-                    const long long nrows = rows_chunk - r0 < 2LL * X::NL ? rows_chunk - r0 : 2LL * X::NL;
-                    const double *src = pick3(xa.in, c) + ((long long)z0 * xa.rows_y + r0) * xa.in_stride;
-                    const unsigned bytes = (unsigned)(nrows * xa.in_stride * 8);
-                    if (nrows > 0 && (bytes & 15u) == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
-                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-                    mbar_arrive(full0 + 8 * s);
-                } else {
-                    // every x line of the chunk written, then copies that see them
-                    if (!wait_count(p.count + k, p.nxl * X::WARPS)) {
-                        ok = false;
-                        break;
-                    }
-                    asm volatile("fence.proxy.async.global;" ::: "memory");
-                    int c, z, x0;
-                    ytile(k, t, c, z, x0);
-                    mbar_arrive_expect_tx(full0 + 8 * s, Q::IN_BYTES);
-                    for (int g = 0; g < Q::G; ++g)
-                        for (int bz = 0; bz < Q::NBI; ++bz)
-                            tma_load_3d(sb + Q::IN0 + s * Q::IN_BYTES + g * Q::IN_GROUP + bz * Q::BI * 64,
-                                        &maps.in[c], 2 * (x0 + 8 * g), bz * Q::BI, z, full0 + 8 * s);
-                    last[s] = q;
-                }
-                jn = atomicAdd(status + 1, 1);
-            }
-            for (int s = 0; s < Q::NIN; ++s)
-                if (last[s] >= 0) mbar_wait(full0 + 8 * s, (last[s] / Q::NIN) & 1);
-        }
-    } else if (warp == STORE_WARP) {
-        if (lane == 0) {
-            for (int q = 0;; ++q) {
-                const int so = q % Q::NOUT;
-                if (!mbar_wait(ofull0 + 8 * so, (q / Q::NOUT) & 1)) {
-                    ok = false;
-                    break;
-                }
-                const int j = otile[so];
-                if (j < 0) break;
-                bool is_y;
-                int k, t, c, z, x0;
-                xy_decode(p, j, is_y, k, t);
-                ytile(k, t, c, z, x0);
-                for (int g = 0; g < Q::G; ++g) {
-                    if (x0 + 8 * g >= a.Mx) break;
-                    for (int bz = 0; bz < Q::NBO; ++bz)
-                        tma_store_3d(&maps.out[c], 2 * (x0 + 8 * g), bz * Q::BO, z,
-                                     sb + Q::OUT0 + so * Q::OUT_BYTES + g * Q::OUT_GROUP + bz * Q::BO * 64);
-                }
-                bulk_commit();
-                bulk_wait_read<Q::NOUT - 1>();
-                if (q + 1 >= Q::NOUT) mbar_arrive(oempty0 + 8 * ((q + 1 - Q::NOUT) % Q::NOUT));
-            }
-            bulk_wait_all();
-        }
-    } else {
-        const int b = tid / Q::TPL, t = tid % Q::TPL;  // column (y) or line (x) of the CTA, thread of it
-        C *line = reinterpret_cast<C *>(base + Q::LINES) + b * Q::LDP;
-        const int c8 = b & 7, sw = swizzle64_col(t, c8);
-        const long long rows_chunk = (long long)p.zc * xa.rows_y;
-        int q = 0, qo = 0;
-        for (;; ++q) {
-            const int s = q % Q::NIN;
-            ok = warp_ok(mbar_wait(full0 + 8 * s, (q / Q::NIN) & 1));
-            if (!ok) break;
-            const int j = itile[s];
-            if (j < 0) break;
-            bool is_y;
-            int k, tt;
-            xy_decode(p, j, is_y, k, tt);
-            if (!is_y) {
-                mbar_arrive(empty0 + 8 * s);  // nothing staged
-                // line b of x tile tt: rows ra, ra + 1 of the chunk
-                const int c = k / p.nzc, z0 = (k - c * p.nzc) * p.zc;
-                const long long ra = 2 * ((long long)tt * X::NL + b), rb = ra + 1;
-                const bool va = ra < rows_chunk, vb = rb < rows_chunk;
-                const long long Ra = (long long)z0 * xa.rows_y + ra, Rb = Ra + 1;
-                const double *in = pick3(xa.in, c);
-                {
-                    const double *pa = in + Ra * xa.in_stride + t, *pb = pa + xa.in_stride;
-                    C v[1][32];
-#pragma unroll
-                    for (int r = 0; r < 16; ++r)
-                        v[0][r] = C{va ? (float)pa[r * X::TPL] : 0.f, vb ? (float)pb[r * X::TPL] : 0.f};
-                    dft32_half<false>(v[0]);
-                    write_line<L, 0>(line, t, v);
-                }
-                __syncwarp();
-                {
-                    C v[TL::U][TL::R];
-                    read_line<L, LAST>(line, t, v);
-                    twiddle_dft<L, LAST, false>(v, TW, t);
-                    write_line<L, LAST>(line, t, v);
-                }
-                __syncwarp();
-                if (va) {
-                    C *out = reinterpret_cast<C *>(pick3(xa.out, c));
-                    const long long za = Ra / xa.rows_y, zb = Rb / xa.rows_y;
-                    C *outa = out + (za * xa.out_y + (Ra - za * xa.rows_y)) * xa.ld + t;
-                    C *outb = out + (zb * xa.out_y + (Rb - zb * xa.rows_y)) * xa.ld + t;
-#pragma unroll
-                    for (int jj = 0; jj < X::KPER; ++jj) {
-                        const int kk = t + jj * X::TPL;
-                        if (kk < a.Mx) {
-                            const C zv = line[skw(kk)], wv = line[skw((L - kk) & (L - 1))];
-                            outa[jj * X::TPL] = C{0.5f * (zv.x + wv.x), 0.5f * (zv.y - wv.y)};
-                            if (vb) outb[jj * X::TPL] = C{0.5f * (zv.y + wv.y), 0.5f * (wv.x - zv.x)};
-                        }
-                    }
-                }
-                // the warp's stores are visible on the GPU before its count
-                __threadfence();
-                __syncwarp();
-                if (lane == 0) atomicAdd(p.count + k, 1);
-                continue;
-            }
-            // a y tile, as k_yq's forward (the zero-padded half of the rows pruned)
-            unsigned char *stg = base + Q::IN0 + s * Q::IN_BYTES + (b >> 3) * Q::IN_GROUP;
-            C v[TL::U][TL::R];
-            {
-                C v0[1][32];
-#pragma unroll
-                for (int r = 0; r < 16; ++r)
-                    v0[0][r] = *reinterpret_cast<const C *>(stg + sw + T0::in_pos(t, 0, r) * 64);
-                mbar_arrive(empty0 + 8 * s);
-                dft32_half<false>(v0[0]);
-                write_line<L, 0>(line, t, v0);
-                __syncwarp();
-                read_line<L, LAST>(line, t, v);
-                twiddle_dft<L, LAST, false>(v, TW, t);
-                __syncwarp();  // the next tile rewrites the line
-            }
-            const int so = qo % Q::NOUT;
-            if (qo >= Q::NOUT) {
-                ok = warp_ok(mbar_wait(oempty0 + 8 * so, ((qo / Q::NOUT) - 1) & 1));
-                if (!ok) break;
-            }
-            unsigned char *ostg = base + Q::OUT0 + so * Q::OUT_BYTES + (b >> 3) * Q::OUT_GROUP;
-#pragma unroll
-            for (int u = 0; u < TL::U; ++u)
-#pragma unroll
-                for (int r = 0; r < TL::R; ++r)
-                    *reinterpret_cast<C *>(ostg + sw + TL::out_pos(t, u, r) * 64) = v[u][r];
-            if (tid == 0) otile[so] = j;
-            fence_proxy_async_smem();
-            mbar_arrive(ofull0 + 8 * so);
-            ++qo;
-        }
-        if (ok) {  // end marker for the store warp
-            const int so = qo % Q::NOUT;
-            if (qo >= Q::NOUT) ok = warp_ok(mbar_wait(oempty0 + 8 * so, ((qo / Q::NOUT) - 1) & 1));
-            if (ok) {
-                if (tid == 0) otile[so] = -1;
-                mbar_arrive(ofull0 + 8 * so);
-            }
-        }
-    }
-    if (!ok && lane == 0) atomicOr(status, 1);
-}
-
-template <int L>
-cudaError_t launch_xyq_t(const XFwdArgs &xa, const ColArgs &a, int nplanes, int *status, int *counts, int zc,
-                         cudaStream_t st)
-{
-    using Q = Yq<L, false, true>;
-    using X = Xy<L>;
-    YqMaps maps;
-    memset(&maps, 0, sizeof(maps));
-    for (int c = 0; c < a.ncomp; ++c) {
-        if (!tma::encode_spectrum(&maps.in[c], a.data[c], a.Mx, L, nplanes, a.axis_stride * 8, a.outer_stride * 8,
-                                  Q::BI, 1) ||
-            !tma::encode_spectrum(&maps.out[c], a.data[c], a.Mx, L, nplanes, a.axis_stride * 8, a.outer_stride * 8,
-                                  Q::BO, 1))
-            return cudaErrorInvalidValue;
-    }
-    XyPlan p;
-    p.zc = zc;
-    p.nzc = nplanes / zc;
-    p.nchunk = p.nzc * a.ncomp;
-    p.nxl = (int)(((long long)zc * xa.rows_y / 2 + X::NL - 1) / X::NL);
-    p.nxt = (a.Mx + Q::B - 1) / Q::B;
-    p.nyt = zc * p.nxt;
-    p.ntiles = p.nchunk * (p.nxl + p.nyt);
-    p.count = counts;
-    const int grid = p.ntiles < tma::sm_count() ? p.ntiles : tma::sm_count();
-    // y tiles trail their x tiles by enough chunks to cover the tiles in
-    // flight (about three a CTA), within about 48 MB of x output held in L2
-    const long long chunk_bytes = (long long)zc * xa.rows_y * xa.ld * 8;
-    int delay = (3 * grid + p.nxl - 1) / p.nxl;
-    const int cap = (int)((48LL << 20) / (chunk_bytes > 0 ? chunk_bytes : 1));
-    if (delay > cap) delay = cap;
-    p.delay = delay < 1 ? 1 : delay;
-    const size_t sm = Q::bytes(a.plan.ntw);
-    cudaError_t e = cudaFuncSetAttribute(k_xyq<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(status + 1, 0, sizeof(int), st)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(counts, 0, sizeof(int) * p.nchunk, st)) != cudaSuccess) return e;
-    k_xyq<L><<<grid, YQ_THREADS, sm, st>>>(xa, a, maps, p, status);
-    return cudaGetLastError();
-}
-
 }  // namespace
 
 bool yq_supported(int prec, int inverse, int L, int n_in, int n_out)
@@ -666,36 +326,6 @@ size_t smem_lines_yq(int inverse, int L, int n_in, int n_out, int ntw_entries)
     case 512: return yq_bytes<512>(inverse, half, ntw_entries);
     case 1024: return yq_bytes<1024>(inverse, half, ntw_entries);
     default: return 0;
-    }
-}
-
-bool xyq_supported(const XFwdArgs &xa, const ColArgs &a, int nplanes)
-{
-    return yq_supported(PREC_FP32, 0, a.L, a.n_in, a.n_out) && yq_half(0, a.L, a.n_in, a.n_out) == 1 &&
-           xa.L == a.L && 2 * xa.n_in == xa.L && !xa.mirror && xa.ncomp == a.ncomp && xa.rows_y == a.n_in &&
-           xa.rows_z == nplanes && xa.out_y == a.L && xa.ld == a.axis_stride && xa.B == xq_lines(xa.L) &&
-           a.B == yq_lines(a.L) && xa.plan.L == a.plan.L && xa.plan.ntw == a.plan.ntw &&
-           (long long)xa.out_y * xa.ld == a.outer_stride;
-}
-
-int xyq_chunk_planes(int nplanes)
-{
-    for (int zc : {4, 2, 1})
-        if (nplanes % zc == 0) return zc;
-    return 1;
-}
-
-cudaError_t launch_xyq(const XFwdArgs &xa, const ColArgs &a, int nplanes, int *status, int *counts, cudaStream_t st)
-{
-    if (!status || !counts || !xyq_supported(xa, a, nplanes)) return cudaErrorInvalidConfiguration;
-    for (int c = 0; c < a.ncomp; ++c)
-        if (xa.out[c] != a.data[c]) return cudaErrorInvalidValue;  // in place: the y pass reads the x output
-    const int zc = xyq_chunk_planes(nplanes);
-    switch (a.L) {
-    case 256: return launch_xyq_t<256>(xa, a, nplanes, status, counts, zc, st);
-    case 512: return launch_xyq_t<512>(xa, a, nplanes, status, counts, zc, st);
-    case 1024: return launch_xyq_t<1024>(xa, a, nplanes, status, counts, zc, st);
-    default: return cudaErrorInvalidValue;
     }
 }
 

@@ -60,8 +60,9 @@ struct Plan {
 };
 
 // Kernel family and lines per CTA of one pass: 'r' run-time, 'p' length-
-// specialised, 'w' wide, 't' tensor-memory fused z, 'q' fused z fed by tiled
-// bulk copies.
+// specialised, 'w' wide, 't' tensor-memory fused z, 'q' a warp per line or
+// column group (y and z fed by tiled bulk copies), 'c' fused z with its DFT
+// stages on the tensor cores.
 struct PassChoice {
     char fam;
     int B;
@@ -111,7 +112,6 @@ struct Solver {
     DevBuf stage;               // packed interleaved fields for push/pull_interleaved
     DevBuf work[3];         // per-component spectra [Nz][Py][Mx], pass precision
     DevBuf fb[3], fa[3], fr[3];  // handle-owned fields: pushed B, solution A, returned B
-    DevBuf xy_counts;            // per chunk of z-planes: x lines written (fused x-y forward pass)
     DevBuf status;               // int[4]: [0] bit 0 set by a kernel whose bounded wait timed out,
                                  // [1] tile counter of the dynamically scheduled kernels
 

@@ -199,23 +199,6 @@ bool yq_supported(int prec, int inverse, int L, int n_in, int n_out);
 int yq_lines(int L);
 size_t smem_lines_yq(int inverse, int L, int n_in, int n_out, int ntw_entries);
 cudaError_t launch_yq(int inverse, const ColArgs &a, int nplanes, int *status, cudaStream_t st);
-// The x and y forward passes fused in one persistent launch (both axes
-// unbounded, one length, FP32, the x output in place in the y pass's
-// spectra); counts: an int a chunk of z-planes per component.
-struct XyPlan {
-    int zc;      // z-planes a chunk
-    int nzc;     // chunks a component
-    int nchunk;  // nzc * components
-    int nxl;     // x tiles a chunk
-    int nxt;     // y column groups a plane
-    int nyt;     // y tiles a chunk
-    int ntiles;  // nchunk * (nxl + nyt)
-    int delay;   // chunks of x tiles between a chunk's x tiles and its y tiles
-    int *count;  // per chunk: x-tile warps whose lines are written
-};
-bool xyq_supported(const XFwdArgs &xa, const ColArgs &a, int nplanes);
-int xyq_chunk_planes(int nplanes);
-cudaError_t launch_xyq(const XFwdArgs &xa, const ColArgs &a, int nplanes, int *status, int *counts, cudaStream_t st);
 // x passes, a warp per line group (ps_kernels_xq.cu): L = 256..1024, not
 // mirrored; xq_lines(L) lines a CTA. n = n_in (forward) or n_out (inverse).
 bool xq_supported(int prec, int inverse, int L, int n, int mirror);
@@ -224,6 +207,17 @@ size_t smem_lines_xq(int L, int ntw_entries);
 cudaError_t launch_xfq(const XFwdArgs &a, cudaStream_t st);
 cudaError_t launch_xiq(const XInvArgs &a, cudaStream_t st);
 }  // namespace wide
+
+// Fused z pass with the DFT stages on the tensor cores (ps_kernels_ztc.cu):
+// FP32 spectra, unbounded z of L = 1024 (n_in = n_out = 512), 8 columns a
+// tile, one persistent CTA per SM. A wait that times out sets bit 0 of
+// *status.
+namespace tc {
+constexpr int ZTC_LINES = 8;
+bool ztc_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_out);
+size_t smem_ztc();
+cudaError_t launch_ztc(const ZArgs &a, int ny, int *status, cudaStream_t st);
+}  // namespace tc
 
 // Kernel-build helpers (ps_greens.cu), all FP64.
 // Kernel family of the build: gm = 0 is the reference's spectrally truncated

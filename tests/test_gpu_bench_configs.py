@@ -93,12 +93,15 @@ def test_mixed_fourier_modes_128x128x64(native, oracle, op):
     check(native, nc, bc, dx, B, ref, w["reg"], **{op: True})
 
 
-@pytest.mark.parametrize("nc", [(64, 64, 512), (64, 512, 64), (512, 64, 64)])
-def test_tile_queue_kernels_length_1024_many_tiles(native, oracle, monkeypatch, nc):
+@pytest.mark.parametrize("nc,zfam", [((64, 64, 512), "tma"), ((64, 512, 64), "tma"), ((512, 64, 64), "tma"),
+                                     ((64, 64, 512), "tc")])
+def test_tile_queue_kernels_length_1024_many_tiles(native, oracle, monkeypatch, nc, zfam):
     """Transform length 1024 along one axis with the bulk-copy kernels on
-    every pass: each persistent CTA takes several tiles, so the staging
-    buffers' phase wrap and the tile counter are exercised."""
+    every pass (and the tensor-core z kernel): each persistent CTA takes
+    several tiles, so the staging buffers' phase wrap and the tile order are
+    exercised."""
     monkeypatch.setenv("PS_KERNELS", "tma")
+    monkeypatch.setenv("PS_KERNELS_Z", zfam)
     rng = np.random.default_rng(sum(nc))
     B = [rng.standard_normal((nc[2], nc[1], nc[0])) for _ in range(3)]
     dx = (2.0 / nc[0], 2.0 / nc[1], 2.0 / nc[2])
@@ -114,4 +117,4 @@ def test_tile_queue_kernels_length_1024_many_tiles(native, oracle, monkeypatch, 
     axis = int(np.argmax(nc))
     passes = {0: (0, 4), 1: (1, 3), 2: (2,)}[axis]
     for p in passes:
-        assert fams[p][0] == "tma", fams
+        assert fams[p][0] == (zfam if p == 2 else "tma"), fams

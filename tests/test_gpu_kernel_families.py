@@ -3,6 +3,8 @@ wide kernels cover (Pz = 256 .. 2048), for every spectral operation.
 
 The families: the warp-per-column kernel fed by tiled bulk copies
 (PS_KERNELS_Z=tma, the default on unbounded z of 256..1024 points), the
+kernel with its DFT stages on the tensor cores (PS_KERNELS_Z=tc: unbounded z
+of 1024 points, the (4, 6, 512) shape here), the
 tensor-memory fused kernel (PS_KERNELS_Z=tmem, the default elsewhere), the
 shared-memory fused kernel (PS_KERNELS_Z=wide) and the length-specialised
 one (PS_KERNELS_Z=p2). A family that does not cover a shape falls back to
@@ -39,7 +41,7 @@ OPS = [
     (dict(curl=True), (0, 1, 2)),
 ]
 
-FAMILIES = ["tmem", "wide", "p2", "tma"]
+FAMILIES = ["tmem", "wide", "p2", "tma", "tc"]
 
 
 def _fields(nc, comps, seed):
@@ -143,22 +145,3 @@ def test_fp32_x_family_vs_oracle(native, oracle, monkeypatch, xi, family):
     # those modes too, so the relative error is larger (1.9e-5 measured).
     tol = 5e-5 if nc == (512, 3, 5) else FP32_TOL
     assert rel_l2(got, ref) < tol
-
-
-@pytest.mark.parametrize("nc,ncomp,opt", [((128, 128, 128), 3, "curl"), ((128, 128, 7), 1, None),
-                                          ((256, 256, 6), 3, "div"), ((128, 128, 10), 2, None)])
-def test_fused_xy_forward_matches_separate_passes(native, monkeypatch, nc, ncomp, opt):
-    """The x and y forward passes fused in one launch (unbounded x and y of
-    one bulk-copy length) give the same bits as the two launches."""
-    rng = np.random.default_rng(sum(nc) + ncomp)
-    B = [rng.standard_normal((nc[2], nc[1], nc[0])) for _ in range(ncomp)] + [None] * (3 - ncomp)
-    kw = {opt: True} if opt else {}
-    dx = (0.02, 0.021, 0.03)
-    monkeypatch.delenv("PS_XY_FUSION", raising=False)
-    A0, R0 = native.solve(nc, (0, 0, 0), dx, B, reg_order=4, precision="fp32", want_rhs=True, **kw)
-    monkeypatch.setenv("PS_XY_FUSION", "1")
-    A1, R1 = native.solve(nc, (0, 0, 0), dx, B, reg_order=4, precision="fp32", want_rhs=True, **kw)
-    for x, y in zip(A0 + R0, A1 + R1):
-        assert (x is None) == (y is None)
-        if x is not None:
-            assert np.array_equal(x, y)

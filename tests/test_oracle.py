@@ -215,3 +215,28 @@ def test_smooth3d_fourier_mode(oracle, s):
     # error against the input's size: the factor reaches 4e-7 at s = 0.4
     for o in (out[0], out[2]):
         assert np.linalg.norm(o - want) <= 1e-14 * np.linalg.norm(f)
+
+
+# ---------------------------------------------------------------------------
+# The port shares its pencils over threads; each pencil's arithmetic is the
+# same on any thread, so the thread count cannot change a bit of the result.
+@pytest.mark.parametrize("bc,opts", [((0, 0, 0), dict(curl=True)), ((1, 1, 0), dict(grad=True)),
+                                     ((0, 0, 1), dict(div=True, reproject=True))])
+def test_port_results_do_not_depend_on_threads(oracle, bc, opts):
+    nc, dx = (14, 10, 12), (0.1, 0.12, 0.09)
+    rng = np.random.default_rng(31)
+    B = [rng.standard_normal((nc[2], nc[1], nc[0])) for _ in range(3)]
+    if bc == (1, 1, 0):
+        B = [b - b.mean(axis=(1, 2), keepdims=True) for b in B]
+    try:
+        oracle.set_threads(1)
+        A1, R1 = oracle.solve3d(nc, bc, dx, B, 4, want_rhs=True, **opts)
+        used = oracle.set_threads(4)
+        A4, R4 = oracle.solve3d(nc, bc, dx, B, 4, want_rhs=True, **opts)
+    finally:
+        oracle.set_threads(0)
+    assert used == 4
+    for x, y in zip(A1 + R1, A4 + R4):
+        assert (x is None) == (y is None)
+        if x is not None:
+            assert np.array_equal(x, y)
