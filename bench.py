@@ -189,6 +189,35 @@ def algorithmic_bytes(n, P, cin, cout, w, g=None):
     ]
 
 
+def nominal_flops(P, cin, cout):
+    """FP64 flops of one solve by the usual FFT count, 2.5 N log2 N a complex
+    transform of N = Px Py Pz points per component transformed, no credit for
+    pruned zeros: (cin + cout) 2.5 N log2 N."""
+    N = int(np.prod(P))
+    return (cin + cout) * 2.5 * N * np.log2(N)
+
+
+def fp64_peak_tflops(dev):
+    """The GPU's FP64 rate as cuBLAS DGEMM reaches it (torch.matmul on two
+    4096^2 float64 matrices, best of 5 after a warm-up), in TFLOP/s."""
+    import torch
+    n = 4096
+    a = torch.randn((n, n), dtype=torch.float64, device=dev)
+    b = torch.randn((n, n), dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -619,6 +648,31 @@ def run_ours(args, w):
     den = sum(float(torch.sum(b ** 2)) for b in A64)
     rel = (num / den) ** 0.5
     max_err = max(float((a - b).abs().max()) for a, b in zip(A, A64)) / max(float(b.abs().max()) for b in A64)
+    # the FP64 solve against the GPU's FP64 rate (not in the timed regions)
+    f64_flops = nominal_flops(P, 3, 3)
+    f64_peak = fp64_peak_tflops(dev)
+
+    # the same FP32 solve with the z pass's DFT stages on the tensor cores
+    # (the opt-in family), beside the headline: time, pass times and error
+    tc = None
+    if not os.environ.get("PS_KERNELS_Z"):
+        Atc = [torch.empty_like(b) for b in B]
+        os.environ["PS_KERNELS_Z"] = "tc"
+        try:
+            if ps.pass_config(7)[2][0] == "tc":
+                Ktc = max(3, K // 3)
+                log(f"[rank {rank}] tensor-core z pass: {Ktc} steps")
+                mstc, passtc, _ = timed_loop("fp32", Ktc, 2, Atc)
+                num = sum(float(torch.sum((a - b) ** 2)) for a, b in zip(Atc, A64))
+                tc = {"kernel": "z pass k_ztc (tcgen05.mma, split-FP16 operands, FP32 accumulation; PS_KERNELS_Z=tc)",
+                      "value": replica_throughput(points, Ktc, max_over_ranks(pg, mstc) / 1e3, world),
+                      "ms_per_step": mstc / Ktc, "steps": Ktc, "passes_ms": dict(zip(PASS_NAMES, passtc)),
+                      "rel_l2_vs_fp64": (num / den) ** 0.5,
+                      "max_err_vs_fp64": max(float((a - b).abs().max()) for a, b in zip(Atc, A64)) /
+                                         max(float(b.abs().max()) for b in A64)}
+        finally:
+            del os.environ["PS_KERNELS_Z"]
+        del Atc
 
     # end to end through the public API with pinned host buffers
     ps.set_precision("fp32")
@@ -688,11 +742,17 @@ def run_ours(args, w):
                      "traffic": traffic, "algorithmic_bytes": byt[top], "ms": pass32[top]},
         "passes_ms": dict(zip(PASS_NAMES, pass32)),
         "solve_gbs_algorithmic": solve_gbs,
-        "fp64": {"value": value64, "ms_per_step": ms64_max / K64, "passes_ms": dict(zip(PASS_NAMES, pass64))},
+        "fp64": {"value": value64, "ms_per_step": ms64_max / K64, "passes_ms": dict(zip(PASS_NAMES, pass64)),
+                 "roofline": {"bound": "fp64", "achieved": f64_flops / (ms64_max / K64 * 1e-3) / 1e12,
+                              "peak": f64_peak, "peak_kind": "measured: cuBLAS DGEMM 4096^3 (torch.matmul)",
+                              "unit": "TFLOP/s", "frac": f64_flops / (ms64_max / K64 * 1e-3) / 1e12 / f64_peak,
+                              "flops": f64_flops,
+                              "flops_rule": "(C_in + C_out) 2.5 N log2 N, N = Px Py Pz, no credit for pruned zeros"}},
         "mixed_vs_fp64_speedup": value / value64,
         "rel_l2_fp32_vs_fp64": rel,
         "max_err_fp32_vs_fp64": max_err,
         "parity_vs_oracle": parity,
+        "tensor_core_z": tc,
         "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": 3 * points * 8,
                 "d2h_bytes_per_step": 3 * points * 8, "steps": Kp,
                 "method": "three handles, each on its own stream and host thread, take the steps in turn "

@@ -18,6 +18,21 @@ def test_algorithmic_bytes_match_the_published_accounting():
     assert abs(sum(bench.algorithmic_bytes((256,) * 3, (512,) * 3, 3, 3, 16, 8)) / 10.64e9 - 1) < 0.01
 
 
+def test_nominal_flops_match_the_published_count():
+    # 512^3 curl (3 -> 3 components on 1024^3 padded points): 4.8e11 FP64 flops a solve
+    assert bench.nominal_flops((1024,) * 3, 3, 3) == pytest.approx(6 * 2.5 * 2 ** 30 * 30)
+    assert abs(bench.nominal_flops((1024,) * 3, 3, 3) / 4.8e11 - 1) < 0.01
+
+
+def test_reference_sample_is_the_workload_source():
+    # the CPU legs solve the benchmark's own rings (same seed) on a smaller grid
+    a = bench.ring_sample(bench.WORKLOADS["rings512"], 32)
+    b = bench.ring_sample(bench.WORKLOADS["rings512"], 32)
+    assert len(a) == 3 and a[0].shape == (32, 32, 32)
+    assert all((x == y).all() for x, y in zip(a, b))
+    assert max(float(abs(x).max()) for x in a) > 0
+
+
 def test_replica_throughput():
     assert bench.replica_throughput(1e6, 10, 2.0, 4) == pytest.approx(20.0)
 
