@@ -659,6 +659,7 @@ def run_ours(args, w):
         Atc = [torch.empty_like(b) for b in B]
         os.environ["PS_KERNELS_Z"] = "tc"
         try:
+            ps.set_precision("fp32")
             if ps.pass_config(7)[2][0] == "tc":
                 Ktc = max(3, K // 3)
                 log(f"[rank {rank}] tensor-core z pass: {Ktc} steps")
