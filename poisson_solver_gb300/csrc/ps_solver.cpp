@@ -814,9 +814,6 @@ bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
             return wide::yq_supported(prec, pass == 3, L, c.n_in, c.n_out);
         }
         return pass == 2 && pa.z.kern_zf && wide::zq_supported(prec, L, op, pa.z.nin, pa.z.nout, pa.z.n_in, pa.z.n_out);
-    case 'd':
-        return pass == 2 && dims == 3 && pa.z.kern_zf &&
-               wide::zq2_supported(prec, L, op, pa.z.nin, pa.z.nout, pa.z.n_in, pa.z.n_out);
     case 'c':
         return pass == 2 && dims == 3 && pa.z.kern_zf &&
                tc::ztc_supported(prec, L, op, pa.z.nin, pa.z.nout, pa.z.n_in, pa.z.n_out);
@@ -826,7 +823,6 @@ bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
 
 int Solver::family_emax(int pass, char fam) const
 {
-    if (fam == 'd') return 16;  // radix 16, 16, 4
     if (fam == 'w' || fam == 't' || fam == 'q' || fam == 'c') return 32;
     if (pass == 2) {
         if (fam == 'p') {
@@ -847,7 +843,6 @@ size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Pl
         if (fam == 't') return wide::smem_lines_zt(L, B, ntw);
         if (fam == 'q') return wide::smem_lines_zq(L, ntw);
         if (fam == 'c') return tc::smem_ztc();
-        if (fam == 'd') return wide::smem_zq2();
         if (fam == 'w') return wide::smem_lines(L, B, nbuf, ntw, true);
         if (fam == 'p') return p2::smem_lines(prec, L, B, nbuf, ntw);
         return smem_z(prec, pl.dev, B, nbuf);
@@ -874,7 +869,6 @@ bool Solver::pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan
     if ((pass == 0 || pass == 4) && B > MAX_LINES) return false;
     if (pass == 2 && fam == 't' && nt % 32 != 0) return false;           // whole warps
     if (fam == 'c') return B == tc::ZTC_LINES && pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
-    if (fam == 'd') return B == wide::ZQ2_LINES && pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
     if (fam == 'q')  // fixed lines per length; no static shared memory
         return B == (pass == 2 ? wide::zq_lines(pl.dev.L) : axis_of(pass) == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L)) &&
                pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
@@ -896,7 +890,6 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     else if (f && strcmp(f, "tmem") == 0 && family_ok(pass, 't', pa)) fam = 't';
     else if (f && strcmp(f, "tma") == 0 && family_ok(pass, 'q', pa)) fam = 'q';
     else if (f && strcmp(f, "tc") == 0 && family_ok(pass, 'c', pa)) fam = 'c';
-    else if (f && strcmp(f, "tma2") == 0 && family_ok(pass, 'd', pa)) fam = 'd';
     // 'q' at 512^3: z 6.0 against 7.7 ms for 't'; y 1.67 / 2.01 against 2.51 / 2.31 ms for 'w';
     // x 1.25 / 1.20 against 1.33 / 1.45 ms for 'p'
     else if (family_ok(pass, 'q', pa)) fam = 'q';
@@ -915,7 +908,6 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     }
     const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam));
     if (fam == 'c') pref = tc::ZTC_LINES;
-    if (fam == 'd') pref = wide::ZQ2_LINES;
     if (fam == 'q')  // fixed by the length
         pref = pass == 2 ? wide::zq_lines(pl.dev.L) : axis == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L);
     int B = pref;
@@ -960,7 +952,6 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
         const int ny = dims == 2 ? 1 : P[1];  // rows of columns (2D: one row of x columns)
         if (c.fam == 'q') PS_CK(wide::launch_zq(a, ny, static_cast<int *>(status.p), stream));
         else if (c.fam == 'c') PS_CK(tc::launch_ztc(a, ny, static_cast<int *>(status.p), stream));
-        else if (c.fam == 'd') PS_CK(wide::launch_zq2(a, ny, static_cast<int *>(status.p), stream));
         else if (c.fam == 't') PS_CK(wide::launch_zt(a, ny, stream));
         else if (c.fam == 'w') PS_CK(wide::launch_z(a, ny, stream));
         else if (c.fam == 'p') PS_CK(p2::launch_z(a, ny, family_emax(2, 'p'), stream));

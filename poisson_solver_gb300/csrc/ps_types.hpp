@@ -189,12 +189,6 @@ bool zq_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_ou
 int zq_lines(int L);
 size_t smem_lines_zq(int L, int ntw_entries);
 cudaError_t launch_zq(const ZArgs &a, int ny, int *status, cudaStream_t st);
-// the same pass with two warps a column (ps_kernels_zq2.cu): L = 1024 only,
-// 16 values a thread (radix 16, 16, 4), ZQ2_LINES columns a CTA of 512 threads
-constexpr int ZQ2_LINES = 8;
-bool zq2_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_out);
-size_t smem_zq2();
-cudaError_t launch_zq2(const ZArgs &a, int ny, int *status, cudaStream_t st);
 // y passes, a warp per column group, tiled bulk copies (ps_kernels_yq.cu):
 // unbounded y (forward n_in = L / 2, inverse n_out = L / 2) or periodic y
 // (n_in = n_out = L), L = 256..1024, a

@@ -94,7 +94,7 @@ def test_mixed_fourier_modes_128x128x64(native, oracle, op):
 
 
 @pytest.mark.parametrize("nc,zfam", [((64, 64, 512), "tma"), ((64, 512, 64), "tma"), ((512, 64, 64), "tma"),
-                                     ((64, 64, 512), "tc"), ((64, 64, 512), "tma2")])
+                                     ((64, 64, 512), "tc")])
 def test_tile_queue_kernels_length_1024_many_tiles(native, oracle, monkeypatch, nc, zfam):
     """Transform length 1024 along one axis with the bulk-copy kernels on
     every pass (and the tensor-core z kernel): each persistent CTA takes
