@@ -264,6 +264,15 @@ int ps_batch_set_kernel(ps_batch *b, int index, int family, double width);
 int ps_batch_push(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
 int ps_batch_push_device(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
 int ps_batch_solve(ps_batch *b);
+/* Tune the batch's launch shapes (no reference counterpart): for the x, y
+ * and z launches in turn, time the bound on a CTA's threads (64, 128, 256)
+ * and the lines a CTA each problem starts from (2 .. 32) on the pushed
+ * problems, and keep the fastest for this batch. Every problem must have been
+ * pushed. Results do not change (each line's arithmetic is the same whatever
+ * the shape); the pushed fields are kept, the outputs and work buffers are
+ * overwritten. Later solves, and rebuilds after adds, options or pushes,
+ * use the tuned shapes. */
+int ps_batch_autotune(ps_batch *b);
 int ps_batch_pull(ps_batch *b, int index, double *ax, double *ay, double *az);
 int ps_batch_pull_device(ps_batch *b, int index, double *ax, double *ay, double *az);
 int ps_batch_set_stream(ps_batch *b, void *stream);

@@ -96,6 +96,7 @@ SIGNATURES = {
     "ps_batch_push": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_push_device": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_solve": (_i, [_vp]),
+    "ps_batch_autotune": (_i, [_vp]),
     "ps_batch_pull": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_pull_device": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_set_stream": (_i, [_vp, _vp]),

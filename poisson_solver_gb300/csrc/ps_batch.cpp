@@ -43,6 +43,12 @@ struct Batch {
         size_t smem = 0;
     };
     PassExec ex[5];
+    // Launch shape of the x (passes 0 and 4), y (1 and 3) and z (2)
+    // launches: the bound on a CTA's threads and the lines a CTA each problem
+    // starts from (halved until it fits). ps_batch_autotune times the
+    // choices; the defaults are the untuned shape.
+    int cap[3] = {BATCH_MAX_THREADS, BATCH_MAX_THREADS, BATCH_MAX_THREADS};
+    int start[3] = {16, 16, 16};
     std::vector<int> write_masks;  // outputs of each problem in the captured solve
     bool dirty = true;
     cudaGraph_t graph = nullptr;
@@ -120,10 +126,9 @@ struct Batch {
     // two) that fit nt threads and the largest usual shared-memory size, so
     // that its CTAs leave as few threads idle as the smem budget allows.
     template <typename SmemFn>
-    static void choose_lines(const std::vector<int> &tpl, const SmemFn &smem, int max_lines, std::vector<int> &B,
-                             int &nt, size_t &smem_max)
+    static void choose_lines(const std::vector<int> &tpl, const SmemFn &smem, int max_lines, int max_threads,
+                             int start_lines, std::vector<int> &B, int &nt, size_t &smem_max)
     {
-        const int start_lines = 16;
         const size_t limit = (size_t)max_smem_per_block() - 2048;  // room for static shared data
         const int n = (int)tpl.size();
         B.assign(n, 1);
@@ -131,8 +136,8 @@ struct Batch {
         size_t cap = 0;
         for (int p = 0; p < n; ++p) {
             int b = std::min(start_lines, max_lines);
-            while (b > 1 && (b * tpl[p] > BATCH_MAX_THREADS || smem(p, b) > limit)) b >>= 1;
-            if (b * tpl[p] > BATCH_MAX_THREADS || smem(p, b) > limit)
+            while (b > 1 && (b * tpl[p] > max_threads || smem(p, b) > limit)) b >>= 1;
+            if (b * tpl[p] > max_threads || smem(p, b) > limit)
                 throw Error(PS_ERR_UNSUPPORTED, "a transform of the batch is too long for one CTA");
             nt = std::max(nt, b * tpl[p]);
             cap = std::max(cap, smem(p, b));
@@ -157,7 +162,37 @@ struct Batch {
         PS_BCK(cudaMemcpy(e.tiles.p, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice));
     }
 
+    // Pass k of every problem as one launch on stream st.
+    cudaError_t launch(int k, cudaStream_t st) const
+    {
+        const int prec = precision;
+        const PassExec &e = ex[k];
+        switch (k) {
+        case 0:
+            return launch_xfwd_batch(prec, (const XFwdArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
+                                     e.smem, st);
+        case 1:
+        case 3:
+            return launch_col_batch(prec, k == 3, (const ColArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles,
+                                    e.nt, e.smem, st);
+        case 2:
+            return launch_z_batch(prec, (const ZArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt, e.smem,
+                                  st);
+        default:
+            return launch_xinv_batch(prec, (const XInvArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
+                                     e.smem, st);
+        }
+    }
+
     void build()
+    {
+        prepare_passes();
+        capture();
+    }
+
+    // The five passes' arguments and tile lists for the current launch
+    // shapes, in device memory.
+    void prepare_passes()
     {
         if (items.empty()) throw Error(PS_ERR_STATE, "the batch holds no problem");
         const int n = (int)items.size(), prec = precision;
@@ -189,14 +224,14 @@ struct Batch {
             ty[p] = ply[p]->dev.tpl;
             tz[p] = plz[p]->dev.tpl;
         }
-        choose_lines(tx, [&](int p, int B) { return smem_x(prec, plx[p]->dev, B); }, MAX_LINES, Bx, ex[0].nt,
-                     ex[0].smem);
-        choose_lines(ty, [&](int p, int B) { return smem_col(prec, ply[p]->dev, B); }, MAX_LINES, By, ex[1].nt,
-                     ex[1].smem);
+        choose_lines(tx, [&](int p, int B) { return smem_x(prec, plx[p]->dev, B); }, MAX_LINES, cap[0], start[0], Bx,
+                     ex[0].nt, ex[0].smem);
+        choose_lines(ty, [&](int p, int B) { return smem_col(prec, ply[p]->dev, B); }, MAX_LINES, cap[1], start[1], By,
+                     ex[1].nt, ex[1].smem);
         choose_lines(
             tz,
             [&](int p, int B) { return smem_z(prec, plz[p]->dev, B, std::max(pa[p].z.nin, pa[p].z.nout)); },
-            MAX_LINES, Bz, ex[2].nt, ex[2].smem);
+            MAX_LINES, cap[2], start[2], Bz, ex[2].nt, ex[2].smem);
         ex[3].nt = ex[1].nt;
         ex[3].smem = ex[1].smem;
         ex[4].nt = ex[0].nt;
@@ -250,8 +285,11 @@ struct Batch {
         upload(ex[2], az, t2);
         upload(ex[3], ayi, t3);
         upload(ex[4], axi, t4);
+    }
 
-        // capture the five launches
+    // Capture the five launches into the graph that solve() replays.
+    void capture()
+    {
         release_graph();
         cudaStream_t cs = stream;
         bool own = false;
@@ -262,20 +300,8 @@ struct Batch {
             own = true;
         }
         PS_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
-        cudaError_t e = launch_xfwd_batch(prec, (const XFwdArgs *)ex[0].args.p, (const BatchTile *)ex[0].tiles.p,
-                                          ex[0].ntiles, ex[0].nt, ex[0].smem, cs);
-        if (e == cudaSuccess)
-            e = launch_col_batch(prec, 0, (const ColArgs *)ex[1].args.p, (const BatchTile *)ex[1].tiles.p, ex[1].ntiles,
-                                 ex[1].nt, ex[1].smem, cs);
-        if (e == cudaSuccess)
-            e = launch_z_batch(prec, (const ZArgs *)ex[2].args.p, (const BatchTile *)ex[2].tiles.p, ex[2].ntiles,
-                               ex[2].nt, ex[2].smem, cs);
-        if (e == cudaSuccess)
-            e = launch_col_batch(prec, 1, (const ColArgs *)ex[3].args.p, (const BatchTile *)ex[3].tiles.p, ex[3].ntiles,
-                                 ex[3].nt, ex[3].smem, cs);
-        if (e == cudaSuccess)
-            e = launch_xinv_batch(prec, (const XInvArgs *)ex[4].args.p, (const BatchTile *)ex[4].tiles.p,
-                                  ex[4].ntiles, ex[4].nt, ex[4].smem, cs);
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = launch(k, cs);
         cudaGraph_t g = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(cs, &g);
         if (own) cudaStreamDestroy(cs);
@@ -286,6 +312,66 @@ struct Batch {
         }
         graph = g;
         PS_BCK(cudaGraphInstantiate(&exec, graph, 0));
+        dirty = false;
+    }
+
+    // Time the launch shapes of each axis's batched launches (the CTA size
+    // bound and the lines a CTA each problem starts from) on the pushed
+    // problems and keep the fastest; the per-line arithmetic, and so every
+    // result, does not depend on the shape. Leaves the graph built.
+    void autotune()
+    {
+        prepare_passes();  // buffers, plans and kernels of every problem
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        PS_BCK(cudaEventCreate(&e0));
+        PS_BCK(cudaEventCreate(&e1));
+        auto finish = [&] {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        };
+        try {
+            static const int passes[3][2] = {{0, 4}, {1, 3}, {2, -1}};
+            for (int ax = 0; ax < 3; ++ax) {
+                int best_cap = cap[ax], best_start = start[ax];
+                float best_ms = -1.f;
+                for (int c : {64, 128, 256})
+                    for (int l : {2, 4, 8, 16, 32}) {
+                        cap[ax] = c;
+                        start[ax] = l;
+                        try {
+                            prepare_passes();
+                        } catch (const Error &err) {
+                            if (err.status == PS_ERR_UNSUPPORTED) continue;  // a problem does not fit this shape
+                            throw;
+                        }
+                        auto run_axis = [&] {
+                            for (int k : passes[ax])
+                                if (k >= 0) PS_BCK(launch(k, stream));
+                        };
+                        run_axis();  // warm-up (and the one-time attribute setup)
+                        PS_BCK(cudaEventRecord(e0, stream));
+                        const int reps = 3;
+                        for (int r = 0; r < reps; ++r) run_axis();
+                        PS_BCK(cudaEventRecord(e1, stream));
+                        PS_BCK(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        PS_BCK(cudaEventElapsedTime(&ms, e0, e1));
+                        if (best_ms < 0.f || ms < best_ms) {
+                            best_ms = ms;
+                            best_cap = c;
+                            best_start = l;
+                        }
+                    }
+                cap[ax] = best_cap;
+                start[ax] = best_start;
+            }
+        } catch (...) {
+            finish();
+            dirty = true;
+            throw;
+        }
+        finish();
+        build();
         dirty = false;
     }
 
@@ -414,6 +500,11 @@ int ps_batch_push_device(ps_batch *h, int index, const double *bx, const double 
 int ps_batch_solve(ps_batch *h)
 {
     return bguarded(h, [&](ps::Batch &b) { b.solve(); });
+}
+
+int ps_batch_autotune(ps_batch *h)
+{
+    return bguarded(h, [&](ps::Batch &b) { b.autotune(); });
 }
 
 int ps_batch_pull(ps_batch *h, int index, double *ax, double *ay, double *az)

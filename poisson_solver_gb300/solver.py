@@ -315,6 +315,11 @@ class PoissonBatch:
     def solve(self):
         self._call("ps_batch_solve")
 
+    def autotune(self):
+        """Time the batched launches' shapes on the pushed problems and keep
+        the fastest (results unchanged)."""
+        self._call("ps_batch_autotune")
+
     def pull(self, i: int, ax=None, ay=None, az=None):
         s = self._shapes[i]
         self._call("ps_batch_pull", int(i), _host_ptr(ax, s, "Ax", True), _host_ptr(ay, s, "Ay", True),

@@ -199,3 +199,32 @@ def test_batch_gaussian_family_equals_single_solves(native):
             if g is not None:
                 assert np.array_equal(g, s), (i, nc, bc, opts, fam[i])
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_autotuned_batch_gives_the_same_results(native, precision):
+    """ps_batch_autotune picks launch shapes by timing; every line's
+    arithmetic is the same in any shape, so the tuned solve equals the untuned
+    one bit for bit, and later solves with new data stay correct."""
+    b, data = _make(native, precision)
+    b.solve()
+    before = [_pull(b, i) for i in range(len(PROBLEMS))]
+    b.autotune()
+    b.solve()
+    after = [_pull(b, i) for i in range(len(PROBLEMS))]
+    for x, y in zip(before, after):
+        for u, v in zip(x, y):
+            assert (u is None) == (v is None)
+            if u is not None:
+                assert np.array_equal(u, v)
+    # new pushed data on the tuned shapes, against single-problem solves
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS):
+        B = _fields(nc, comps, 7000 + i, zero_mean=bc == (1, 1, 0))
+        b.push(i, *B)
+        data[i] = B
+    b.solve()
+    tol = FP64_TOL if precision == "fp64" else FP32_TOL
+    for i, (nc, bc, comps, opts) in enumerate(PROBLEMS):
+        ref, _ = native.solve(nc, bc, _dx(nc), data[i], (0, 2, 6)[i % 3], precision=precision, **opts)
+        got = _pull(b, i)
+        assert rel_l2(got, ref) < tol
