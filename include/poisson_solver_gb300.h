@@ -222,7 +222,7 @@ int ps_get_pass_times(ps_solver *h, double ms[5], int *nsolves, int reset);
  * configuration on the same GPU model reuse them. Without tuning a measured
  * default is used. ps_get_pass_config reports the family and lines a solve
  * with component_mask would run for pass 0..4. */
-enum { PS_FAMILY_RUNTIME = 0, PS_FAMILY_P2 = 1, PS_FAMILY_WIDE = 2, PS_FAMILY_TMEM = 3, PS_FAMILY_TMA = 4, PS_FAMILY_TC = 5, PS_FAMILY_PACKED = 6 };
+enum { PS_FAMILY_RUNTIME = 0, PS_FAMILY_P2 = 1, PS_FAMILY_WIDE = 2, PS_FAMILY_TMEM = 3, PS_FAMILY_TMA = 4, PS_FAMILY_TC = 5 };
 int ps_autotune(ps_solver *h, int component_mask);
 int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, int *lines);
 

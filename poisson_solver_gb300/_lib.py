@@ -46,7 +46,7 @@ PS_FAMILY_P2 = 1
 PS_FAMILY_WIDE = 2
 PS_FAMILY_TMEM = 3
 PS_FAMILY_TMA = 4
-FAMILY_NAMES = {0: "runtime", 1: "p2", 2: "wide", 3: "tmem", 4: "tma", 5: "tc", 6: "packed"}
+FAMILY_NAMES = {0: "runtime", 1: "p2", 2: "wide", 3: "tmem", 4: "tma", 5: "tc"}
 
 PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0
 PS_BATCH_INFO_TILES_PER_SOLVE = 1

@@ -249,7 +249,6 @@ int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, 
                   : c.fam == 't' ? PS_FAMILY_TMEM
                   : c.fam == 'q' ? PS_FAMILY_TMA
                   : c.fam == 'c' ? PS_FAMILY_TC
-                  : c.fam == 'e' ? PS_FAMILY_PACKED
                                  : PS_FAMILY_RUNTIME;
         *lines = c.B;
     });

@@ -785,14 +785,12 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
 // with tensor-memory staging (z only), 'q' a warp per line or column group
 // (x and y: L = 256..1024; z: unbounded axes of 256..1024 points; y and z
 // fed by tiled bulk copies), 'c' the fused z kernel with its DFT stages on
-// the tensor cores (unbounded z of 1024 points; only when PS_KERNELS_Z=tc),
-// 'e' the 'q' z kernel with its transforms in packed pair arithmetic
-// (unbounded z of 1024 points).
+// the tensor cores (unbounded z of 1024 points; only when PS_KERNELS_Z=tc).
 // Defaults, measured at 512^3 (FP32 curl): the 'q' kernels where they apply
 // (x: a warp per line; y, z: bulk copies), else x forward p2 with 2 lines a
 // CTA (2.3 against 3.4 ms for wide), x inverse p2 with 4, y wide with 8 and
 // z tensor-memory with 8.
-// PS_KERNELS, PS_KERNELS_X/_Y/_Z (= tma, packed, tc, tmem, wide, p2 or runtime),
+// PS_KERNELS, PS_KERNELS_X/_Y/_Z (= tma, tc, tmem, wide, p2 or runtime),
 // PS_LINES_X/_XI/_Y/_Z and PS_Z_EM override the defaults; ps_autotune
 // replaces them for one configuration.
 
@@ -819,16 +817,13 @@ bool Solver::family_ok(int pass, char fam, const PassArgs &pa) const
     case 'c':
         return pass == 2 && dims == 3 && pa.z.kern_zf &&
                tc::ztc_supported(prec, L, op, pa.z.nin, pa.z.nout, pa.z.n_in, pa.z.n_out);
-    case 'e':
-        return pass == 2 && dims == 3 && pa.z.kern_zf &&
-               wide::zqp_supported(prec, L, op, pa.z.nin, pa.z.nout, pa.z.n_in, pa.z.n_out);
     default: return false;
     }
 }
 
 int Solver::family_emax(int pass, char fam) const
 {
-    if (fam == 'w' || fam == 't' || fam == 'q' || fam == 'c' || fam == 'e') return 32;
+    if (fam == 'w' || fam == 't' || fam == 'q' || fam == 'c') return 32;
     if (pass == 2) {
         if (fam == 'p') {
             const char *v = getenv("PS_Z_EM");  // 16 measured faster than 8 (13.4 vs 15.4 ms at 512^3)
@@ -848,7 +843,6 @@ size_t Solver::pass_smem(int pass, char fam, int B, const PassArgs &pa, const Pl
         if (fam == 't') return wide::smem_lines_zt(L, B, ntw);
         if (fam == 'q') return wide::smem_lines_zq(L, ntw);
         if (fam == 'c') return tc::smem_ztc();
-        if (fam == 'e') return wide::smem_zqp();
         if (fam == 'w') return wide::smem_lines(L, B, nbuf, ntw, true);
         if (fam == 'p') return p2::smem_lines(prec, L, B, nbuf, ntw);
         return smem_z(prec, pl.dev, B, nbuf);
@@ -875,7 +869,6 @@ bool Solver::pass_fits(int pass, char fam, int B, const PassArgs &pa, const Plan
     if ((pass == 0 || pass == 4) && B > MAX_LINES) return false;
     if (pass == 2 && fam == 't' && nt % 32 != 0) return false;           // whole warps
     if (fam == 'c') return B == tc::ZTC_LINES && pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
-    if (fam == 'e') return B == wide::ZQP_LINES && pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
     if (fam == 'q')  // fixed lines per length; no static shared memory
         return B == (pass == 2 ? wide::zq_lines(pl.dev.L) : axis_of(pass) == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L)) &&
                pass_smem(pass, fam, B, pa, pl) <= (size_t)max_smem_per_block();
@@ -897,7 +890,6 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     else if (f && strcmp(f, "tmem") == 0 && family_ok(pass, 't', pa)) fam = 't';
     else if (f && strcmp(f, "tma") == 0 && family_ok(pass, 'q', pa)) fam = 'q';
     else if (f && strcmp(f, "tc") == 0 && family_ok(pass, 'c', pa)) fam = 'c';
-    else if (f && strcmp(f, "packed") == 0 && family_ok(pass, 'e', pa)) fam = 'e';
     // 'q' at 512^3: z 6.0 against 7.7 ms for 't'; y 1.67 / 2.01 against 2.51 / 2.31 ms for 'w';
     // x 1.25 / 1.20 against 1.33 / 1.45 ms for 'p'
     else if (family_ok(pass, 'q', pa)) fam = 'q';
@@ -916,7 +908,6 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     }
     const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam));
     if (fam == 'c') pref = tc::ZTC_LINES;
-    if (fam == 'e') pref = wide::ZQP_LINES;
     if (fam == 'q')  // fixed by the length
         pref = pass == 2 ? wide::zq_lines(pl.dev.L) : axis == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L);
     int B = pref;
@@ -961,7 +952,6 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
         const int ny = dims == 2 ? 1 : P[1];  // rows of columns (2D: one row of x columns)
         if (c.fam == 'q') PS_CK(wide::launch_zq(a, ny, static_cast<int *>(status.p), stream));
         else if (c.fam == 'c') PS_CK(tc::launch_ztc(a, ny, static_cast<int *>(status.p), stream));
-        else if (c.fam == 'e') PS_CK(wide::launch_zqp(a, ny, static_cast<int *>(status.p), stream));
         else if (c.fam == 't') PS_CK(wide::launch_zt(a, ny, stream));
         else if (c.fam == 'w') PS_CK(wide::launch_z(a, ny, stream));
         else if (c.fam == 'p') PS_CK(p2::launch_z(a, ny, family_emax(2, 'p'), stream));

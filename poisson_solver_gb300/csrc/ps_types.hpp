@@ -206,13 +206,6 @@ int xq_lines(int L);
 size_t smem_lines_xq(int L, int ntw_entries);
 cudaError_t launch_xfq(const XFwdArgs &a, cudaStream_t st);
 cudaError_t launch_xiq(const XInvArgs &a, cudaStream_t st);
-// fused z pass as zq at L = 1024 with the transforms in packed pair
-// arithmetic (ps_kernels_zqp.cu): FP32, n_in = n_out = 512, ZQP_LINES
-// columns a tile. A wait that times out sets bit 0 of *status.
-constexpr int ZQP_LINES = 8;
-bool zqp_supported(int prec, int L, int op, int nin, int nout, int n_in, int n_out);
-size_t smem_zqp();
-cudaError_t launch_zqp(const ZArgs &a, int ny, int *status, cudaStream_t st);
 }  // namespace wide
 
 // Fused z pass with the DFT stages on the tensor cores (ps_kernels_ztc.cu):

@@ -10,8 +10,7 @@ in seconds:
 * the 16-ring source of the 512^3 headline case (reg 10, curl) at 128^3;
 * the bulk-copy (tile-queue) kernels at transform length 1024 along each
   axis in turn, with many tiles per persistent CTA: 64x64x512, 64x512x64 and
-  512x64x64 unbounded curl solves (padded 128x128x1024 and its turns), and
-  the tensor-core and packed z kernels on the first.
+  512x64x64 unbounded curl solves (padded 128x128x1024 and its turns).
 
 Every case states relative L2 and maximum error (max |A - A_ref| over
 max |A_ref|) against the oracle, FP64 and FP32 transforms.
@@ -95,10 +94,10 @@ def test_mixed_fourier_modes_128x128x64(native, oracle, op):
 
 
 @pytest.mark.parametrize("nc,zfam", [((64, 64, 512), "tma"), ((64, 512, 64), "tma"), ((512, 64, 64), "tma"),
-                                     ((64, 64, 512), "tc"), ((64, 64, 512), "packed")])
+                                     ((64, 64, 512), "tc")])
 def test_tile_queue_kernels_length_1024_many_tiles(native, oracle, monkeypatch, nc, zfam):
     """Transform length 1024 along one axis with the bulk-copy kernels on
-    every pass (and the tensor-core and packed z kernels): each persistent CTA takes
+    every pass (and the tensor-core z kernel): each persistent CTA takes
     several tiles, so the staging buffers' phase wrap and the tile order are
     exercised."""
     monkeypatch.setenv("PS_KERNELS", "tma")

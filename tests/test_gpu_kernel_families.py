@@ -4,9 +4,8 @@ wide kernels cover (Pz = 256 .. 2048), for every spectral operation.
 The families: the warp-per-column kernel fed by tiled bulk copies
 (PS_KERNELS_Z=tma, the default on unbounded z of 256..1024 points), the
 kernel with its DFT stages on the tensor cores (PS_KERNELS_Z=tc: unbounded z
-of 1024 points, the (4, 6, 512) shape here), the same warp-per-column kernel
-with its transforms in packed pair arithmetic (PS_KERNELS_Z=packed, the same
-shape), the tensor-memory fused kernel (PS_KERNELS_Z=tmem, the default elsewhere), the
+of 1024 points, the (4, 6, 512) shape here), the
+tensor-memory fused kernel (PS_KERNELS_Z=tmem, the default elsewhere), the
 shared-memory fused kernel (PS_KERNELS_Z=wide) and the length-specialised
 one (PS_KERNELS_Z=p2). A family that does not cover a shape falls back to
 the default. Narrow x-y extents keep the oracle fast while the z
@@ -42,7 +41,7 @@ OPS = [
     (dict(curl=True), (0, 1, 2)),
 ]
 
-FAMILIES = ["tmem", "wide", "p2", "tma", "tc", "packed"]
+FAMILIES = ["tmem", "wide", "p2", "tma", "tc"]
 
 
 def _fields(nc, comps, seed):
