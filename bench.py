@@ -932,10 +932,11 @@ def run_batch(args, w):
     setup_s = time.perf_counter() - t0
     tune_s = None
     if not args.no_autotune:
-        # launch shapes of the batched passes picked by timing (not in the timed region)
+        # plan variants and launch shapes of the batched passes picked by timing (not in the timed region)
         t0 = time.perf_counter()
         b32.autotune()
         tune_s = time.perf_counter() - t0
+    tuning = {ax: dict(zip(("max_threads", "start_lines", "plan_variant"), t)) for ax, t in zip("xyz", b32.tuning())}
     ms32, clocks = timed(b32, K, W, sample_clocks=True)
     ms32_max = max_over_ranks(pg, ms32)
     value = replica_throughput(points, K, ms32_max / 1e3, world)
@@ -1013,6 +1014,7 @@ def run_batch(args, w):
         "clocks": clocks,
         "setup_s": setup_s,
         "autotune_s": tune_s,
+        "batch_tuning": tuning,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

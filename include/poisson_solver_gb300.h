@@ -226,6 +226,19 @@ enum { PS_FAMILY_RUNTIME = 0, PS_FAMILY_P2 = 1, PS_FAMILY_WIDE = 2, PS_FAMILY_TM
 int ps_autotune(ps_solver *h, int component_mask);
 int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, int *lines);
 
+/* The transform plan the same solve runs on pass 0..4: its stage radices in
+ * order (the first `capacity` of *nstages written to radices) and, for a
+ * length transformed by Bluestein's algorithm, the convolution length the
+ * stages run on (*conv_length; 0 otherwise). With FP32 transforms the
+ * run-time kernels have plan variants that ps_autotune times beside the
+ * families and lines: the power-of-two part in radix 16 or radix 8, and
+ * Bluestein's convolution length as the least power of two or the least
+ * 2^a 3^b 5^c >= 2 L - 1. PS_PLAN_X/_Y/_Z (bit 0: radix 8, bit 1: smooth
+ * length) set them for the run-time family and bypass tuned choices. FP64
+ * transforms always take the default plan. No reference counterpart. */
+int ps_get_pass_plan(ps_solver *h, int pass, int component_mask, int *radices, int capacity, int *nstages,
+                     int *conv_length);
+
 /* Copy the FP64 kernel octant K = G * zeta / (Px Py Pz), layout
  * [Pz/2+1][Py/2+1][Px/2+1] (x fastest), to a HOST array. */
 int ps_get_kernel(const ps_solver *h, double *out, long long capacity);
@@ -264,15 +277,20 @@ int ps_batch_set_kernel(ps_batch *b, int index, int family, double width);
 int ps_batch_push(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
 int ps_batch_push_device(ps_batch *b, int index, const double *bx, const double *by, const double *bz);
 int ps_batch_solve(ps_batch *b);
-/* Tune the batch's launch shapes (no reference counterpart): for the x, y
- * and z launches in turn, time the bound on a CTA's threads (64, 128, 256)
- * and the lines a CTA each problem starts from (2 .. 32) on the pushed
+/* Tune the batch (no reference counterpart): for the x, y and z launches in
+ * turn, time the plan variants of every problem's transforms (FP32 batches
+ * only; see ps_get_pass_plan), then the bound on a CTA's threads (64, 128,
+ * 256) and the lines a CTA each problem starts from (2 .. 32) on the pushed
  * problems, and keep the fastest for this batch. Every problem must have been
- * pushed. Results do not change (each line's arithmetic is the same whatever
- * the shape); the pushed fields are kept, the outputs and work buffers are
- * overwritten. Later solves, and rebuilds after adds, options or pushes,
- * use the tuned shapes. */
+ * pushed. FP64 results do not change (each line's arithmetic is the same
+ * whatever the shape); FP32 results change at rounding level when a plan
+ * variant is taken. The pushed fields are kept, the outputs and work buffers
+ * are overwritten. Later solves, and rebuilds after adds, options or pushes,
+ * use the tuned settings. ps_batch_get_tuning reports them for axis 0..2
+ * (x, y, z): the CTA thread bound, the starting lines and the plan variant
+ * (bit 0: radix 8, bit 1: smooth Bluestein length). */
 int ps_batch_autotune(ps_batch *b);
+int ps_batch_get_tuning(const ps_batch *b, int axis, int *max_threads, int *start_lines, int *plan_variant);
 int ps_batch_pull(ps_batch *b, int index, double *ax, double *ay, double *az);
 int ps_batch_pull_device(ps_batch *b, int index, double *ax, double *ay, double *az);
 int ps_batch_set_stream(ps_batch *b, void *stream);

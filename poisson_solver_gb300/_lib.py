@@ -87,6 +87,7 @@ SIGNATURES = {
     "ps_get_pass_times": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _ip, _i]),
     "ps_autotune": (_i, [_vp, _i]),
     "ps_get_pass_config": (_i, [_vp, _i, _i, _ip, _ip]),
+    "ps_get_pass_plan": (_i, [_vp, _i, _i, _ip, _i, _ip, _ip]),
     "ps_batch_create": (_i, [ctypes.POINTER(_vp), _i]),
     "ps_batch_destroy": (_i, [_vp]),
     "ps_batch_add": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_double), _i, _ip]),
@@ -97,6 +98,7 @@ SIGNATURES = {
     "ps_batch_push_device": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_solve": (_i, [_vp]),
     "ps_batch_autotune": (_i, [_vp]),
+    "ps_batch_get_tuning": (_i, [_vp, _i, _ip, _ip, _ip]),
     "ps_batch_pull": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_pull_device": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_set_stream": (_i, [_vp, _vp]),

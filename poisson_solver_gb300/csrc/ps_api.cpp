@@ -254,6 +254,18 @@ int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, 
     });
 }
 
+int ps_get_pass_plan(ps_solver *h, int pass, int component_mask, int *radices, int capacity, int *nstages,
+                     int *conv_length)
+{
+    if (!nstages || !conv_length || capacity < 0 || (capacity > 0 && !radices)) return PS_ERR_ARGUMENT;
+    return guarded(h, [&](ps::Solver &s) {
+        const ps::FftPlanDev &d = s.current_plan(pass, component_mask);
+        *nstages = d.nstages;
+        for (int i = 0; i < d.nstages && i < capacity; ++i) radices[i] = d.radix[i];
+        *conv_length = d.blue ? d.L : 0;
+    });
+}
+
 int ps_get_kernel(const ps_solver *h, double *out, long long capacity)
 {
     if (!out) return PS_ERR_ARGUMENT;

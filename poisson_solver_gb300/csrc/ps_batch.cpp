@@ -49,6 +49,9 @@ struct Batch {
     // choices; the defaults are the untuned shape.
     int cap[3] = {BATCH_MAX_THREADS, BATCH_MAX_THREADS, BATCH_MAX_THREADS};
     int start[3] = {16, 16, 16};
+    // Plan variant (PV_* bits, FP32 only) of every problem's x, y and z
+    // transforms; ps_batch_autotune times them too.
+    int pv[3] = {0, 0, 0};
     std::vector<int> write_masks;  // outputs of each problem in the captured solve
     bool dirty = true;
     cudaGraph_t graph = nullptr;
@@ -214,9 +217,9 @@ struct Batch {
                 }
             }
             write_masks[p] = s.prepare(Bin, Aout, false, pa[p]);
-            plx[p] = &s.plan(s.P[0], prec);
-            ply[p] = &s.plan(s.P[1], prec);
-            plz[p] = &s.plan(s.P[2], prec, e_max_z(prec));  // the z body's element budget
+            plx[p] = &s.plan(s.P[0], prec, 0, pv[0]);
+            ply[p] = &s.plan(s.P[1], prec, 0, pv[1]);
+            plz[p] = &s.plan(s.P[2], prec, e_max_z(prec), pv[2]);  // the z body's element budget
         }
         std::vector<int> tx(n), ty(n), tz(n), Bx, By, Bz;
         for (int p = 0; p < n; ++p) {
@@ -315,10 +318,11 @@ struct Batch {
         dirty = false;
     }
 
-    // Time the launch shapes of each axis's batched launches (the CTA size
-    // bound and the lines a CTA each problem starts from) on the pushed
-    // problems and keep the fastest; the per-line arithmetic, and so every
-    // result, does not depend on the shape. Leaves the graph built.
+    // Time the plan variants (FP32) and then the launch shapes of each
+    // axis's batched launches (the CTA size bound and the lines a CTA each
+    // problem starts from) on the pushed problems and keep the fastest. The
+    // per-line arithmetic does not depend on the shape; a plan variant
+    // changes FP32 results at rounding level. Leaves the graph built.
     void autotune()
     {
         prepare_passes();  // buffers, plans and kernels of every problem
@@ -332,31 +336,53 @@ struct Batch {
         try {
             static const int passes[3][2] = {{0, 4}, {1, 3}, {2, -1}};
             for (int ax = 0; ax < 3; ++ax) {
-                int best_cap = cap[ax], best_start = start[ax];
+                // time the axis's launches in the current settings; < 0 if a
+                // problem does not fit them
+                auto time_axis = [&]() -> float {
+                    try {
+                        prepare_passes();
+                    } catch (const Error &err) {
+                        if (err.status == PS_ERR_UNSUPPORTED) return -1.f;
+                        throw;
+                    }
+                    auto run_axis = [&] {
+                        for (int k : passes[ax])
+                            if (k >= 0) PS_BCK(launch(k, stream));
+                    };
+                    run_axis();  // warm-up (and the one-time attribute setup)
+                    PS_BCK(cudaEventRecord(e0, stream));
+                    const int reps = 3;
+                    for (int r = 0; r < reps; ++r) run_axis();
+                    PS_BCK(cudaEventRecord(e1, stream));
+                    PS_BCK(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    PS_BCK(cudaEventElapsedTime(&ms, e0, e1));
+                    return ms;
+                };
                 float best_ms = -1.f;
+                if (precision == PREC_FP32) {
+                    // z bodies hold 8 elements a thread: no radix-cap variant
+                    const int vmask = ax == 2 ? PV_SMOOTH_M : (PV_HALF_RADIX | PV_SMOOTH_M);
+                    int best_pv = pv[ax];
+                    for (int v = 0; v <= 3; ++v) {
+                        if ((v & ~vmask) != 0) continue;
+                        pv[ax] = v;
+                        const float ms = time_axis();
+                        if (ms >= 0.f && (best_ms < 0.f || ms < best_ms)) {
+                            best_ms = ms;
+                            best_pv = v;
+                        }
+                    }
+                    pv[ax] = best_pv;
+                }
+                int best_cap = cap[ax], best_start = start[ax];
+                best_ms = -1.f;
                 for (int c : {64, 128, 256})
                     for (int l : {2, 4, 8, 16, 32}) {
                         cap[ax] = c;
                         start[ax] = l;
-                        try {
-                            prepare_passes();
-                        } catch (const Error &err) {
-                            if (err.status == PS_ERR_UNSUPPORTED) continue;  // a problem does not fit this shape
-                            throw;
-                        }
-                        auto run_axis = [&] {
-                            for (int k : passes[ax])
-                                if (k >= 0) PS_BCK(launch(k, stream));
-                        };
-                        run_axis();  // warm-up (and the one-time attribute setup)
-                        PS_BCK(cudaEventRecord(e0, stream));
-                        const int reps = 3;
-                        for (int r = 0; r < reps; ++r) run_axis();
-                        PS_BCK(cudaEventRecord(e1, stream));
-                        PS_BCK(cudaEventSynchronize(e1));
-                        float ms = 0.f;
-                        PS_BCK(cudaEventElapsedTime(&ms, e0, e1));
-                        if (best_ms < 0.f || ms < best_ms) {
+                        const float ms = time_axis();
+                        if (ms >= 0.f && (best_ms < 0.f || ms < best_ms)) {
                             best_ms = ms;
                             best_cap = c;
                             best_start = l;
@@ -505,6 +531,16 @@ int ps_batch_solve(ps_batch *h)
 int ps_batch_autotune(ps_batch *h)
 {
     return bguarded(h, [&](ps::Batch &b) { b.autotune(); });
+}
+
+int ps_batch_get_tuning(const ps_batch *h, int axis, int *max_threads, int *start_lines, int *plan_variant)
+{
+    if (!h || !h->b || axis < 0 || axis > 2 || !max_threads || !start_lines || !plan_variant) return PS_ERR_ARGUMENT;
+    const ps::Batch &b = *h->b;
+    *max_threads = b.cap[axis];
+    *start_lines = b.start[axis];
+    *plan_variant = b.pv[axis];
+    return PS_OK;
 }
 
 int ps_batch_pull(ps_batch *h, int index, double *ax, double *ay, double *az)

@@ -505,9 +505,9 @@ __device__ __forceinline__ void fft_stages(C *S, C *W, int sn, int sb, int b, in
 constexpr int IDLE_T = 1 << 28;
 
 // Bluestein's algorithm for a length lb with a large prime factor, on lines
-// of M = P.L >= 2 lb - 1 elements: with c[n] = e^{-i pi n^2 / lb},
-// X[k] = c[k] sum_n (x[n] c[n]) conj(c[k - n]), a circular convolution of
-// length M done by the power-of-two stages (forward, times the precomputed
+// of M = P.L >= 2 lb - 1 elements (a power of two, or 2^a 3^b 5^c): with
+// c[n] = e^{-i pi n^2 / lb}, X[k] = c[k] sum_n (x[n] c[n]) conj(c[k - n]), a
+// circular convolution of length M done by the plan's stages (forward, times the precomputed
 // spectrum K of the wrapped conj(c) scaled by 1/M, unnormalised inverse). The
 // inverse DFT conjugates the chirp and reads K at -k, which is the spectrum of
 // the wrapped c. The chirp and K are read from the plan's global table (each
@@ -532,7 +532,8 @@ __device__ __forceinline__ void bluestein_lines(C *S, C *W, int sn, int sb, int 
     for (int c = 0; c < ncomp; ++c) {
         C *Sb = S + c * cstride + b * sb;
         for (int k = t; k < M; k += tpl) {
-            const C kk = INV ? C{K[(M - k) & (M - 1)].x, -K[(M - k) & (M - 1)].y} : K[k];
+            const int km = k == 0 ? 0 : M - k;
+            const C kk = INV ? C{K[km].x, -K[km].y} : K[k];
             Sb[k * sn] = cmul(Sb[k * sn], kk);
         }
     }

@@ -153,29 +153,75 @@ static void host_fft_pow2(std::vector<std::complex<long double>> &a)
     }
 }
 
+// In-place DFT (e^{-2 pi i nk / M}) of a length M = 2^a 3^b 5^c in extended
+// precision, by recursive decimation in time: the spectrum of a Bluestein
+// kernel on a smooth convolution length.
+static void host_fft_smooth(std::vector<std::complex<long double>> &a)
+{
+    const size_t M = a.size();
+    if (M <= 1) return;
+    const size_t R = M % 2 == 0 ? 2 : M % 3 == 0 ? 3 : 5;
+    const size_t m = M / R;
+    std::vector<std::vector<std::complex<long double>>> sub(R, std::vector<std::complex<long double>>(m));
+    for (size_t n = 0; n < m; ++n)
+        for (size_t r = 0; r < R; ++r) sub[r][n] = a[n * R + r];
+    for (auto &s : sub) host_fft_smooth(s);
+    for (size_t k = 0; k < M; ++k) {
+        std::complex<long double> acc = 0.0L;
+        for (size_t r = 0; r < R; ++r) acc += sub[r][k % m] * root((long long)(r * k % M), (long long)M);
+        a[k] = acc;
+    }
+}
+
 // Lengths with a prime factor of at least this take Bluestein's algorithm
-// (two power-of-two FFTs of M >= 2L - 1 points) instead of a direct prime-
-// radix stage (about R complex products an element).
+// (two FFTs of M >= 2L - 1 points) instead of a direct prime-radix stage
+// (about R complex products an element).
 constexpr int BLUESTEIN_MIN_PRIME = 17;
 
-const Plan &Solver::plan(int L, int prec, int emax)
+static int next_pow2(int n)
+{
+    int m = 1;
+    while (m < n) m <<= 1;
+    return m;
+}
+
+// least 2^a 3^b 5^c >= n
+static int next_smooth(int n)
+{
+    for (int m = n;; ++m) {
+        int x = m;
+        for (int p : {2, 3, 5})
+            while (x % p == 0) x /= p;
+        if (x == 1) return m;
+    }
+}
+
+static bool bluestein_length(int L)
+{
+    return L > 16 && largest_prime_factor(L) >= BLUESTEIN_MIN_PRIME && !getenv("PS_NO_BLUESTEIN");
+}
+
+const Plan &Solver::plan(int L, int prec, int emax, int pv)
 {
     if (emax <= 0) emax = e_max(prec);
-    auto key = std::make_pair(L, prec * 64 + emax);
+    if (prec != PREC_FP32) pv = 0;  // FP64 results do not depend on tuning
+    const int Lt = L;  // the transform length
+    const bool blue = bluestein_length(Lt);
+    if (!blue) pv &= ~PV_SMOOTH_M;
+    if (emax < 16) pv &= ~PV_HALF_RADIX;
+    const auto key = std::make_tuple(L, prec, emax, pv);
     auto it = plans.find(key);
     if (it != plans.end()) return *it->second;
     auto pl = std::make_unique<Plan>();
     FftPlanDev &d = pl->dev;
-    const int Lt = L;  // the transform length
-    const bool blue = L > 16 && largest_prime_factor(L) >= BLUESTEIN_MIN_PRIME && !getenv("PS_NO_BLUESTEIN");
     if (blue) {
-        L = 1;
-        while (L < 2 * Lt - 1) L <<= 1;
+        L = next_pow2(2 * Lt - 1);
+        if (pv & PV_SMOOTH_M) L = std::min(L, next_smooth(2 * Lt - 1));
     }
     d.L = L;
     d.blue = blue ? 1 : 0;
     d.lb = Lt;
-    std::vector<int> rad = L > 1 ? factorize(L, emax) : std::vector<int>{};
+    std::vector<int> rad = L > 1 ? factorize(L, (pv & PV_HALF_RADIX) ? emax / 2 : emax) : std::vector<int>{};
     if ((int)rad.size() > MAX_STAGES) throw Error(PS_ERR_UNSUPPORTED, "transform length has too many factors");
     d.nstages = (int)rad.size();
     std::vector<std::complex<long double>> tab;
@@ -215,7 +261,8 @@ const Plan &Solver::plan(int L, int prec, int emax)
             b[k] = cc;
             if (k > 0) b[L - k] = cc;
         }
-        host_fft_pow2(b);
+        if ((L & (L - 1)) == 0) host_fft_pow2(b);
+        else host_fft_smooth(b);
         d.kspec = (int)tab.size();
         for (int k = 0; k < L; ++k) tab.push_back(b[k] / (long double)L);
     }
@@ -906,7 +953,12 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
         const int want = atoi(v);
         if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) pref = want;
     }
-    const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam));
+    // PS_PLAN_X/_Y/_Z: the run-time family's plan variant (PV_* bits, FP32)
+    static const char *plan_env[3] = {"PS_PLAN_X", "PS_PLAN_Y", "PS_PLAN_Z"};
+    int pv = 0;
+    if (fam == 'r')
+        if (const char *v = getenv(plan_env[axis])) pv = atoi(v) & plan_variants(pass);
+    const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam), pv);
     if (fam == 'c') pref = tc::ZTC_LINES;
     if (fam == 'q')  // fixed by the length
         pref = pass == 2 ? wide::zq_lines(pl.dev.L) : axis == 0 ? wide::xq_lines(pl.dev.L) : wide::yq_lines(pl.dev.L);
@@ -915,13 +967,31 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     if (fam == 't')
         while (B * pl.dev.tpl < 32 && pass_fits(pass, fam, 2 * B, pa, pl)) B *= 2;
     if (!pass_fits(pass, fam, B, pa, pl)) throw Error(PS_ERR_UNSUPPORTED, "transform length too large for one CTA");
-    return PassChoice{fam, B};
+    return PassChoice{fam, B, pv};
+}
+
+const Plan &Solver::pass_plan(int pass, const PassChoice &c)
+{
+    return plan(pass_len(pass), precision, family_emax(pass, c.fam), c.fam == 'r' ? c.pv : 0);
+}
+
+// The plan variants that change the run-time family's plan of a pass (FP32
+// only): a radix cap below an element budget of 16, and a smooth Bluestein
+// length that is shorter than the power of two.
+int Solver::plan_variants(int pass) const
+{
+    if (precision != PREC_FP32) return 0;
+    const int L = pass_len(pass);
+    int v = 0;
+    if (family_emax(pass, 'r') >= 16 && L > 1) v |= PV_HALF_RADIX;
+    if (bluestein_length(L) && next_smooth(2 * L - 1) < next_pow2(2 * L - 1)) v |= PV_SMOOTH_M;
+    return v;
 }
 
 void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
 {
     const int prec = precision;
-    const Plan &pl = plan(pass_len(pass), prec, family_emax(pass, c.fam));
+    const Plan &pl = pass_plan(pass, c);
     switch (pass) {
     case 0: {
         XFwdArgs &a = pa.x;
@@ -973,7 +1043,8 @@ void Solver::launch_pass(int pass, const PassChoice &c, PassArgs &pa)
 
 // ---------------------------------------------------------------------------
 // Tuned choices: in memory for the process, and in a text file (one
-// "key family lines" line a pass) at $PS_TUNE_CACHE, else
+// "key family lines variant" line a pass; files without the variant field
+// read as variant 0) at $PS_TUNE_CACHE, else
 // $XDG_CACHE_HOME/poisson_solver_gb300/tune.txt or
 // $HOME/.cache/poisson_solver_gb300/tune.txt; PS_TUNE_CACHE="" keeps them in
 // memory only.
@@ -1000,10 +1071,15 @@ void tune_load_locked()
     const std::string path = tune_path();
     if (path.empty()) return;
     std::ifstream f(path);
-    std::string key, fam;
-    int B;
-    while (f >> key >> fam >> B)
-        if (fam.size() == 1 && B >= 1 && B <= 64) tune_table[key] = PassChoice{fam[0], B};
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream in(line);
+        std::string key, fam;
+        int B = 0, pv = 0;
+        if (!(in >> key >> fam >> B)) continue;
+        if (!(in >> pv)) pv = 0;
+        if (fam.size() == 1 && B >= 1 && B <= 64 && pv >= 0 && pv <= 3) tune_table[key] = PassChoice{fam[0], B, pv};
+    }
 }
 
 void tune_store_locked(const std::string &key, const PassChoice &c)
@@ -1018,7 +1094,7 @@ void tune_store_locked(const std::string &key, const PassChoice &c)
             if (path[i] == '/' || i == slash) mkdir(path.substr(0, i == slash ? slash : i).c_str(), 0755);
     }
     std::ofstream f(path, std::ios::app);
-    if (f) f << key << ' ' << c.fam << ' ' << c.B << '\n';
+    if (f) f << key << ' ' << c.fam << ' ' << c.B << ' ' << c.pv << '\n';
 }
 
 }  // namespace
@@ -1044,7 +1120,7 @@ std::string Solver::tune_key(int pass, const PassArgs &pa)
 static bool env_override()
 {
     for (const char *v : {"PS_KERNELS", "PS_KERNELS_X", "PS_KERNELS_Y", "PS_KERNELS_Z", "PS_LINES_X", "PS_LINES_XI",
-                          "PS_LINES_Y", "PS_LINES_Z"})
+                          "PS_LINES_Y", "PS_LINES_Z", "PS_PLAN_X", "PS_PLAN_Y", "PS_PLAN_Z"})
         if (getenv(v)) return true;
     return false;
 }
@@ -1055,8 +1131,9 @@ PassChoice Solver::choice(int pass, const PassArgs &pa)
         std::lock_guard<std::mutex> lock(tune_mu);
         tune_load_locked();
         auto it = tune_table.find(tune_key(pass, pa));
-        if (it != tune_table.end() && family_ok(pass, it->second.fam, pa)) {
-            const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, it->second.fam));
+        if (it != tune_table.end() && family_ok(pass, it->second.fam, pa) &&
+            (it->second.pv & ~plan_variants(pass)) == 0) {
+            const Plan &pl = pass_plan(pass, it->second);
             if (pass_fits(pass, it->second.fam, it->second.B, pa, pl)) return it->second;
         }
     }
@@ -1128,28 +1205,35 @@ void Solver::autotune(int in_mask)
         for (int pass = 0; pass < NPASS; ++pass) {
             if (pass >= 3 && !write_mask) continue;
             if (dims == 2 && (pass == 1 || pass == 3)) continue;  // the fused pass transforms y
-            PassChoice best{0, 0};
-            float best_ms = 0.f;
+            // candidates: every family, plan variant (run-time family, FP32)
+            // and line count that fits
+            std::vector<PassChoice> cands;
             for (char fam : {'q', 't', 'w', 'p', 'r'}) {
                 if (!family_ok(pass, fam, pa)) continue;
-                const Plan &pl = plan(pass_len(pass), precision, family_emax(pass, fam));
-                for (int B = 1; B <= 64; B *= 2) {
-                    if (!pass_fits(pass, fam, B, pa, pl)) continue;
-                    const PassChoice c{fam, B};
-                    PassArgs run = pa;
-                    launch_pass(pass, c, run);  // warm-up (and the one-time attribute setup)
-                    PS_CK(cudaEventRecord(e0, stream));
-                    const int reps = 3;
-                    for (int r = 0; r < reps; ++r) launch_pass(pass, c, run);
-                    PS_CK(cudaEventRecord(e1, stream));
-                    PS_CK(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    PS_CK(cudaEventElapsedTime(&ms, e0, e1));
-                    ms /= reps;
-                    if (!best.fam || ms < best_ms) {
-                        best = c;
-                        best_ms = ms;
-                    }
+                const int pvs = fam == 'r' ? plan_variants(pass) : 0;
+                for (int pv = 0; pv <= 3; ++pv) {
+                    if ((pv & ~pvs) != 0) continue;
+                    const Plan &pl = pass_plan(pass, PassChoice{fam, 1, pv});
+                    for (int B = 1; B <= 64; B *= 2)
+                        if (pass_fits(pass, fam, B, pa, pl)) cands.push_back(PassChoice{fam, B, pv});
+                }
+            }
+            PassChoice best{0, 0};
+            float best_ms = 0.f;
+            for (const PassChoice &c : cands) {
+                PassArgs run = pa;
+                launch_pass(pass, c, run);  // warm-up (and the one-time attribute setup)
+                PS_CK(cudaEventRecord(e0, stream));
+                const int reps = 3;
+                for (int r = 0; r < reps; ++r) launch_pass(pass, c, run);
+                PS_CK(cudaEventRecord(e1, stream));
+                PS_CK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                PS_CK(cudaEventElapsedTime(&ms, e0, e1));
+                ms /= reps;
+                if (!best.fam || ms < best_ms) {
+                    best = c;
+                    best_ms = ms;
                 }
             }
             if (best.fam) {
@@ -1183,6 +1267,11 @@ PassChoice Solver::current_choice(int pass, int in_mask)
     PassArgs pa;
     prepare(Bin, Aout, false, pa);
     return choice(pass, pa);
+}
+
+const FftPlanDev &Solver::current_plan(int pass, int in_mask)
+{
+    return pass_plan(pass, current_choice(pass, in_mask)).dev;
 }
 
 // ---------------------------------------------------------------------------

@@ -5,6 +5,7 @@
 
 #include <array>
 #include <map>
+#include <tuple>
 #include <vector>
 #include <memory>
 #include <stdexcept>
@@ -59,13 +60,22 @@ struct Plan {
     DevBuf table;
 };
 
+// Plan variants of the run-time family, tuned for FP32 transforms (FP64
+// always takes the default plan, so FP64 results do not depend on tuning):
+// PV_HALF_RADIX runs the power-of-two part of a length in radices of half the
+// element budget (radix 8 instead of 16: one stage more, two butterflies a
+// thread); PV_SMOOTH_M takes Bluestein's convolution length as the least
+// 2^a 3^b 5^c >= 2 lb - 1 instead of the least power of two.
+enum { PV_HALF_RADIX = 1, PV_SMOOTH_M = 2 };
+
 // Kernel family and lines per CTA of one pass: 'r' run-time, 'p' length-
 // specialised, 'w' wide, 't' tensor-memory fused z, 'q' a warp per line or
 // column group (y and z fed by tiled bulk copies), 'c' fused z with its DFT
-// stages on the tensor cores.
+// stages on the tensor cores; pv the plan variant ('r' only).
 struct PassChoice {
     char fam;
     int B;
+    int pv = 0;
 };
 
 // Arguments of the five passes of one solve, all but the plans and the lines
@@ -119,7 +129,7 @@ struct Solver {
     int produced = 0;  // component mask of fa from the last solve
     int rhs_ready = 0; // fr holds the returned right-hand side of the pushed fb
 
-    std::map<std::pair<int, int>, std::unique_ptr<Plan>> plans;  // (length, precision * 64 + element budget)
+    std::map<std::tuple<int, int, int, int>, std::unique_ptr<Plan>> plans;  // (length, precision, element budget, variant)
 
     // Optional per-pass timing: one set of boundary events per timed solve.
     static constexpr int NPASS = 5;
@@ -178,13 +188,15 @@ struct Solver {
     // configuration (options + in_mask) on zero-filled scratch buffers and
     // keep the fastest (tuned choices outlive the handle; see ps_solver.cpp).
     void autotune(int in_mask);
-    // The family and lines a solve of in_mask would run on a pass.
+    // The family and lines a solve of in_mask would run on a pass, and the
+    // transform plan it runs with.
     PassChoice current_choice(int pass, int in_mask);
+    const FftPlanDev &current_plan(int pass, int in_mask);
 
     size_t device_bytes() const;
     void copy_kernel(double *host, long long capacity) const;
 
-    const Plan &plan(int L, int prec, int emax = 0);  // emax 0: e_max(prec)
+    const Plan &plan(int L, int prec, int emax = 0, int pv = 0);  // emax 0: e_max(prec); pv: PV_* bits
     void ensure_kernel(int prec);
     void ensure_zeta(int prec);
 
@@ -201,6 +213,8 @@ private:
     std::string tune_key(int pass, const PassArgs &pa);
     std::string device_tag;  // device name and SM count, for the tuning key
     void launch_pass(int pass, const PassChoice &c, PassArgs &pa);
+    const Plan &pass_plan(int pass, const PassChoice &c);
+    int plan_variants(int pass) const;  // PV_* bits that change the run-time family's plan of this pass
     void build_kernel();
     void check_setup() const;
     size_t field_elems() const { return (size_t)n[0] * n[1] * n[2]; }

@@ -213,6 +213,17 @@ class PoissonSolver:
             out.append((L.FAMILY_NAMES[f.value], b.value))
         return out
 
+    def pass_plan(self, component_mask: int = 7):
+        """[(stage radices, Bluestein convolution length or 0)] of the five
+        passes a solve would run."""
+        out = []
+        for p in range(5):
+            rad = (ctypes.c_int * 16)()
+            ns, m = ctypes.c_int(), ctypes.c_int()
+            self._call("ps_get_pass_plan", p, int(component_mask), rad, 16, ctypes.byref(ns), ctypes.byref(m))
+            out.append((list(rad[:min(ns.value, 16)]), m.value))
+        return out
+
     def synchronize(self):
         self._call("ps_synchronize")
 
@@ -316,9 +327,19 @@ class PoissonBatch:
         self._call("ps_batch_solve")
 
     def autotune(self):
-        """Time the batched launches' shapes on the pushed problems and keep
-        the fastest (results unchanged)."""
+        """Time the plan variants (FP32) and the batched launches' shapes on
+        the pushed problems and keep the fastest."""
         self._call("ps_batch_autotune")
+
+    def tuning(self):
+        """[(CTA thread bound, starting lines, plan variant)] of the x, y and
+        z launches."""
+        out = []
+        for ax in range(3):
+            t, s, v = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            self._call("ps_batch_get_tuning", ax, ctypes.byref(t), ctypes.byref(s), ctypes.byref(v))
+            out.append((t.value, s.value, v.value))
+        return out
 
     def pull(self, i: int, ax=None, ay=None, az=None):
         s = self._shapes[i]

@@ -1,13 +1,17 @@
-"""ps_autotune: per-pass kernel family and lines per CTA picked by timing.
+"""ps_autotune: per-pass kernel family, lines per CTA and (FP32, run-time
+kernels) plan variant picked by timing.
 
 Tuning runs on zero-filled scratch buffers, so it must leave pushed fields and
 results alone; a tuned solve must agree with the default one to FP32
-rounding (other families and line counts only reorder rounding), and in FP64
-(run-time kernels only, whose per-line arithmetic does not depend on the line
-count) bit for bit. Tuned choices go to the cache file and are reused by a new
-handle of the same configuration.
+rounding (other families, line counts and plans only reorder rounding), and
+in FP64 (run-time kernels only, default plans, whose per-line arithmetic does
+not depend on the line count) bit for bit. Tuned choices go to the cache file
+and are reused by a new handle of the same configuration; a cache line
+without the plan-variant field reads as the default plan.
 """
 import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -63,10 +67,24 @@ def test_autotune_keeps_results_and_persists(native, tmp_path, monkeypatch, prec
         assert np.array_equal(a, b)
     ps.close()
     lines = cache.read_text().strip().splitlines()
-    assert len(lines) == 5 and all(len(l.split()) == 3 for l in lines)
+    assert len(lines) == 5 and all(len(l.split()) == 4 for l in lines)
     # a new handle of the same configuration reads the cache
     ps2 = _solver(native, nc, bc, precision)
     assert ps2.pass_config(7) == tuned
+    ps2.close()
+    # a cache written without the plan-variant field is read (in a new
+    # process: the table is loaded once a process) as the default plan
+    old = tmp_path / "old.txt"
+    old.write_text("".join(" ".join(l.split()[:3]) + "\n" for l in lines))
+    code = ("import poisson_solver_gb300 as p; s = p.PoissonSolver(); "
+            f"s.setup3d({nc}, {bc}, {tuple(2.0 / n for n in nc)}, 2); s.set_return_curl(True); "
+            f"s.set_precision('{precision}'); print(s.pass_config(7))")
+    env = dict(os.environ, PS_TUNE_CACHE=str(old))
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300,
+                         cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == str([(f, b) for f, b in tuned])
+    ps2 = _solver(native, nc, bc, precision)
     # line overrides bypass the tuned table
     monkeypatch.setenv("PS_LINES_Y", "2")
     assert ps2.pass_config(7)[1][1] <= 2
