@@ -419,16 +419,16 @@ def cpu_sample(w, n, reps=2, threads=0):
 
 
 def oracle_parity(psg, w, n=128):
-    """The GPU solve (FP64 and FP32 transforms) against the oracle on an n^3
-    sample of the workload's source: relative L2 and maximum error (max
-    |A - A_ref| / max |A_ref|) of each."""
+    """The GPU solve (FP64, FP32 and double-float transforms) against the
+    oracle on an n^3 sample of the workload's source: relative L2 and maximum
+    error (max |A - A_ref| / max |A_ref|) of each."""
     from oracle import oracle
     oracle.set_threads(0)
     B = ring_sample(w, n)
     nc, dx = (n, n, n), (2.0 / n,) * 3
     ref, _ = oracle.solve3d(nc, (0, 0, 0), dx, B, w["reg"], curl=True)
     out = {"grid": [n, n, n], "source": "the same rings and seed sampled at %d^3" % n}
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32", "df64"):
         got, _ = psg.solve(nc, (0, 0, 0), dx, B, w["reg"], curl=True, precision=prec)
         num = sum(float(np.sum((g - r) ** 2)) for g, r in zip(got, ref))
         den = sum(float(np.sum(r ** 2)) for r in ref)
@@ -648,6 +648,18 @@ def run_ours(args, w):
     den = sum(float(torch.sum(b ** 2)) for b in A64)
     rel = (num / den) ** 0.5
     max_err = max(float((a - b).abs().max()) for a, b in zip(A, A64)) / max(float(b.abs().max()) for b in A64)
+    # the same solve with double-float transforms (FP64-class accuracy on the FP32 pipes)
+    Kdf = max(2, K // 3)
+    log(f"[rank {rank}] double-float timed loop: {Kdf} steps")
+    Adf = [torch.empty_like(a) for a in A64]
+    msdf, passdf, _ = timed_loop("df64", Kdf, 1, Adf)
+    msdf_max = max_over_ranks(pg, msdf)
+    df64 = {"value": replica_throughput(points, Kdf, msdf_max / 1e3, world), "ms_per_step": msdf_max / Kdf,
+            "steps": Kdf, "passes_ms": dict(zip(PASS_NAMES, passdf)),
+            "rel_l2_vs_fp64": (sum(float(torch.sum((a - b) ** 2)) for a, b in zip(Adf, A64)) / den) ** 0.5,
+            "max_err_vs_fp64": max(float((a - b).abs().max()) for a, b in zip(Adf, A64)) /
+                               max(float(b.abs().max()) for b in A64)}
+    del Adf
     # the FP64 solve against the GPU's FP64 rate (not in the timed regions)
     f64_flops = nominal_flops(P, 3, 3)
     f64_peak = fp64_peak_tflops(dev)
@@ -752,6 +764,7 @@ def run_ours(args, w):
         "mixed_vs_fp64_speedup": value / value64,
         "rel_l2_fp32_vs_fp64": rel,
         "max_err_fp32_vs_fp64": max_err,
+        "df64": df64,
         "parity_vs_oracle": parity,
         "tensor_core_z": tc,
         "e2e": {"value": e2e, "unit": "Mpts/s", "h2d_bytes_per_step": 3 * points * 8,

@@ -51,13 +51,16 @@ enum {
     PS_OPT_DIV = 1,        /* value 0/1: return div A    (set_return_div, settings.cpp:15)  */
     PS_OPT_CURL = 2,       /* value 0/1: return curl A   (set_return_curl, settings.cpp:21) */
     PS_OPT_REPROJECT = 3,  /* value 0/1: reproject the returned B (set_reprojection, settings.cpp:26) */
-    PS_OPT_PRECISION = 4,  /* PS_PREC_FP64 (default) or PS_PREC_FP32 transforms */
+    PS_OPT_PRECISION = 4,  /* PS_PREC_FP64 (default), PS_PREC_FP32 or PS_PREC_DF64 transforms */
     PS_OPT_PASS_TIMING = 5 /* value 0/1: time each pass of every solve with CUDA events */
 };
 
 enum {
     PS_PREC_FP64 = 0,  /* all transforms and the spectral operation in FP64 */
-    PS_PREC_FP32 = 1   /* FP64 kernel build, FP32 transforms, FP64 field I/O */
+    PS_PREC_FP32 = 1,  /* FP64 kernel build, FP32 transforms, FP64 field I/O */
+    PS_PREC_DF64 = 2   /* FP64 kernel build, transforms in double-float arithmetic (pairs of FP32
+                          numbers, about 48 bits: FP64-class accuracy, FP32's exponent range), FP64
+                          field I/O; no reference counterpart */
 };
 
 /* Kernel families for ps_set_kernel. */

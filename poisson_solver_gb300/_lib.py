@@ -30,6 +30,7 @@ PS_OPT_PASS_TIMING = 5
 
 PS_PREC_FP64 = 0
 PS_PREC_FP32 = 1
+PS_PREC_DF64 = 2
 
 PS_KERNEL_SPECTRAL = 0
 PS_KERNEL_GAUSSIAN = 1

@@ -59,6 +59,7 @@ struct Batch {
 
     explicit Batch(int prec) : precision(prec)
     {
+        if (prec == PREC_DF64) throw Error(PS_ERR_UNSUPPORTED, "double-float transforms are for single problems");
         if (prec != PREC_FP64 && prec != PREC_FP32) throw Error(PS_ERR_ARGUMENT, "precision must be FP64 or FP32");
         PS_BCK(cudaGetDevice(&device));
     }

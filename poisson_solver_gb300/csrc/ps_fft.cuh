@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ps_dfloat.cuh"
 #include "ps_types.hpp"
 
 namespace ps {
@@ -26,6 +27,7 @@ namespace ps {
 template <typename T> struct CxT;
 template <> struct CxT<double> { using type = double2; };
 template <> struct CxT<float> { using type = float2; };
+template <> struct CxT<dfloat> { using type = dfloat2; };
 
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }

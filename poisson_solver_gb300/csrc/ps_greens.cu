@@ -372,6 +372,16 @@ __global__ void k_to_fp32(const double *in, float *out, size_t n)
         out[q] = (float)in[q];
 }
 
+// double -> double-float (hi, lo) pairs: hi = fl(x), lo = fl(x - hi)
+__global__ void k_to_df(const double *in, float2 *out, size_t n)
+{
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const double x = in[q];
+        const float hi = __double2float_rn(x);
+        out[q] = make_float2(hi, __double2float_rn(x - (double)hi));
+    }
+}
+
 unsigned grid_for(long long n, int threads)
 {
     long long g = (n + threads - 1) / threads;
@@ -415,6 +425,12 @@ cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st)
 cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t st)
 {
     k_to_fp32<<<grid_for((long long)n, 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_df(const double *in, float2 *out, size_t n, cudaStream_t st)
+{
+    k_to_df<<<grid_for((long long)n, 256), 256, 0, st>>>(in, out, n);
     return cudaGetLastError();
 }
 

@@ -1,443 +1,27 @@
-// Pass kernels of the 3D solve: x forward (real-to-half-spectrum, zero-pad
-// fused), y column transforms, the fused z pass (forward, spectral kernel and
-// derivative operator, inverse), and x inverse (half-spectrum-to-real, crop
-// fused). Each CTA stages its lines in shared memory and runs the Stockham
-// stages of ps_fft.cuh on them; global traffic is coalesced along x.
-#include <cuda_runtime.h>
-
-#include "ps_fft.cuh"
-#include "ps_types.hpp"
+// Public launchers of the run-time pass kernels (ps_kernels_body.cuh):
+// grid, block and shared-memory sizes, and the dispatch on the pass
+// precision (FP64 and FP32 instantiated here, double-float in
+// ps_kernels_df.cu).
+#include "ps_kernels_body.cuh"
 
 namespace ps {
 
-namespace {
-
-template <typename T> struct Cplx { using type = typename CxT<T>::type; };
-
-__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
-
-// element budget per thread: x and y passes, and the fused z pass
-template <typename T> constexpr int EMX = e_max(sizeof(T) == 8 ? PREC_FP64 : PREC_FP32);
-template <typename T> constexpr int EMZ = e_max_z(sizeof(T) == 8 ? PREC_FP64 : PREC_FP32);
-
-}  // namespace
-
-// ---------------------------------------------------------------------------
-// x forward. Line l of the CTA carries rows 2l (real part) and 2l+1 (imag
-// part); after the complex transform Z the two half spectra are
-// Xa[k] = (Z[k] + conj Z[L-k]) / 2 and Xb[k] = (Z[k] - conj Z[L-k]) / 2i.
-//
-// The pass bodies take the CTA's tile coordinates and its working thread count
-// nt explicitly, so the same code serves the per-problem launches and the
-// batched ones (one launch over the tiles of many problems, where a CTA may
-// have more threads than the problem of its tile uses). Threads tid >= nt only
-// join the barriers: their line-thread index is set to L, past every
-// butterfly, and the load/store loops skip them.
-template <typename T>
-__device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, int nt)
-{
-    using C = typename Cplx<T>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, ld = a.plan.L + 1;  // lines as long as the plan's working length
-    C *W = a.plan.generic ? S + B * ld : nullptr;
-    const FftPlanDev &plan = a.plan;
-    const C *tws = stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
-    __shared__ StageInfo si;
-    load_stages(si, a.plan);
-    const double *in = pick3(a.in, comp);
-    C *out = reinterpret_cast<C *>(pick3(a.out, comp));
-    const int tid = threadIdx.x;
-    const bool live = tid < nt;
-    const long long rows = (long long)a.rows_y * a.rows_z;
-    const long long row0 = (long long)bx * 2 * B;
-    __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.out_y, a.ld);
-
-    // line l = (row 2l, row 2l+1) as (re, im); zero past n_in and past the last
-    // row. With the mirror flag the rows are those of the kernel octant,
-    // (z, y) -> (min(z, Pz-z), min(y, Py-y)), and n -> min(n, L-n).
-    for (int line = 0; line < B; ++line) {
-        const long long ra = row0 + 2 * line;
-        const bool va = ra < rows, vb = ra + 1 < rows;
-        long long oa = ra * a.in_stride, ob = oa + a.in_stride;
-        if (a.mirror) {
-            if (va) {
-                const int j = (int)(ra % a.rows_y), k = (int)(ra / a.rows_y);
-                oa = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
-            }
-            if (vb) {
-                const int j = (int)((ra + 1) % a.rows_y), k = (int)((ra + 1) / a.rows_y);
-                ob = ((long long)imin(k, a.Pz - k) * a.oct_y + imin(j, a.Py - j)) * a.oct_x;
-            }
-        }
-        C *ln = S + line * ld;
-        for (int n = live ? tid : L; n < L; n += nt) {
-            T xa = (T)0, xb = (T)0;
-            if (n < a.n_in) {
-                const int nn = a.mirror ? imin(n, L - n) : n;
-                if (va) xa = (T)in[oa + nn];
-                if (vb) xb = (T)in[ob + nn];
-            }
-            ln[n] = C{xa, xb};
-        }
-    }
-    __syncthreads();
-    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
-
-    // separate the two half spectra and store
-    const int Mx = a.Mx;
-    for (int line = 0; line < B; ++line) {
-        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
-        if (oa < 0) break;
-        for (int k = live ? tid : Mx; k < Mx; k += nt) {
-            const C z = S[line * ld + k], w = S[line * ld + (k == 0 ? 0 : L - k)];
-            const T h = (T)0.5;
-            out[oa + k] = C{h * (z.x + w.x), h * (z.y - w.y)};
-            if (ob >= 0) out[ob + k] = C{h * (z.y + w.y), h * (w.x - z.x)};
-        }
-    }
-}
-
-template <typename T> __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
-{
-    xfwd_body<T>(a, blockIdx.x, blockIdx.y, blockDim.x);
-}
-
-// ---------------------------------------------------------------------------
-// Column transforms along a strided axis, in place: the CTA takes B adjacent
-// columns (one 128-byte row segment per sample for the default B) of one slab.
-template <typename T, bool INV>
-__device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int comp, int nt)
-{
-    using C = typename Cplx<T>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, Lw = a.plan.L;  // Lw: the plan's working length
-    C *W = a.plan.generic ? S + Lw * B : nullptr;
-    const int lb = __ffs(B) - 1;
-    const FftPlanDev &plan = a.plan;
-    const C *tws = stage_twiddles(plan, S + Lw * B * (a.plan.generic ? 2 : 1));
-    __shared__ StageInfo si;
-    load_stages(si, a.plan);
-    const int x0 = bx * B;
-    const int nb = imin(B, a.Mx - x0);
-    C *base = reinterpret_cast<C *>(pick3(a.data, comp)) + (long long)slab * a.outer_stride + x0;
-    const int tid = threadIdx.x;
-
-    // each thread keeps one column b and walks rows n = t, t + nt/B, ...
-    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : IDLE_T, rstep = nt >> lb;
-    const long long gstep = (long long)rstep * a.axis_stride;
-    {
-        const C *src = base + (long long)t * a.axis_stride + b;
-        const int n_in = b < nb ? a.n_in : 0;
-#pragma unroll 4
-        for (int n = t; n < L; n += rstep, src += gstep) {
-            C v = C{0, 0};
-            if (n < n_in) v = *src;
-            S[n * B + b] = v;
-        }
-    }
-    __syncthreads();
-    fft_lines<INV, EMX<T>>(S, W, B, 1, b, t, plan, tws, si);
-    if (b < nb) {
-        C *dst = base + (long long)t * a.axis_stride + b;
-#pragma unroll 4
-        for (int n = t; n < a.n_out; n += rstep, dst += gstep) *dst = S[n * B + b];
-    }
-}
-
-template <typename T, bool INV> __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
-{
-    col_body<T, INV>(a, blockIdx.x, blockIdx.y, blockIdx.z, blockDim.x);
-}
-
-// ---------------------------------------------------------------------------
-// Fused z pass.
-template <typename T>
-__device__ __forceinline__ T wavenumber(int k, int P, T c, bool derivative)
-{
-    // k in [0, P): signed index wrapped at P/2; the derivative drops the
-    // unpaired Nyquist mode (its Hermitian part vanishes in the real output).
-    // Computed in the pass precision (FP64 arithmetic is slow on this GPU).
-    const int m = (2 * k < P) ? k : k - P;
-    if (derivative && 2 * k == P) return (T)0;
-    return (T)m * c;
-}
-
-// OPT: the spectral operation, or -1 to take it from a.op at run time (the
-// batched pass); a fixed OPT folds every test on op away.
-template <typename T, int OPT>
-__device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
-{
-    const int op = OPT >= 0 ? OPT : a.op;
-    using C = typename Cplx<T>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, LB = a.plan.L * B;  // buffers as long as the plan's working length
-    const int nbuf = a.nin > a.nout ? a.nin : a.nout;
-    C *W = a.plan.generic ? S + nbuf * LB : nullptr;
-    const int lb = __ffs(B) - 1;
-    const int x0 = bx * B;
-    const int ky = a.ky0 + by;
-    const int nb = imin(B, a.Mx - x0);
-    const long long off = (long long)ky * a.row_stride + x0;
-    const int tid = threadIdx.x;
-    const int b = tid & (B - 1), t = tid < nt ? tid >> lb : IDLE_T;
-    const FftPlanDev &plan = a.plan;
-    const C *tws = stage_twiddles(plan, S + (nbuf + (a.plan.generic ? 1 : 0)) * LB);
-    __shared__ StageInfo si;
-    load_stages(si, a.plan);
-
-    const int rstep = nt >> lb;
-    const long long gstep = (long long)rstep * a.axis_stride;
-    const int n_in = b < nb ? a.n_in : 0;
-    for (int c = 0; c < a.nin; ++c) {
-        const C *src = reinterpret_cast<const C *>(pick3(a.in, c)) + off + (long long)t * a.axis_stride + b;
-        C *buf = S + c * LB + b;
-#pragma unroll 4
-        for (int n = t; n < L; n += rstep, src += gstep) {
-            C v = C{0, 0};
-            if (n < n_in) v = *src;
-            buf[n * B] = v;
-        }
-    }
-    __syncthreads();
-    fft_lines<false, EMZ<T>>(S, W, B, 1, b, t, plan, tws, si, a.nin, LB);
-
-    if (op != OP_FORWARD) {
-        // the thread's column kx is fixed; it walks kz = t, t + nt/B, ...
-        const int oy = imin(ky, a.Py - ky);
-        const int kx = x0 + b;
-        const T *Kc = reinterpret_cast<const T *>(a.kern) + (long long)oy * a.Mx + kx;
-        const long long kzs = (long long)a.oct_y * a.Mx;
-        const T kyv = wavenumber<T>(ky, a.Py, (T)a.kyc, true);
-        const T kxv = wavenumber<T>(kx, a.Px, (T)a.kxc, true);
-        const T kzc = (T)a.kzc;
-        for (int n = t; n < (b < nb ? L : 0); n += rstep) {
-            const int idx = n * B + b;
-            const int oz = imin(n, a.Pz - n);
-            const T g = Kc[oz * kzs];
-            const T kzv = wavenumber<T>(n, a.Pz, kzc, true);
-            if (op == OP_NONE) {
-                for (int c = 0; c < a.nin; ++c) S[c * LB + idx] = cscale(S[c * LB + idx], g);
-            } else if (op == OP_GRAD) {
-                // out_d = i k_d K in_d; in_d falls back to component x
-                const C i0 = S[idx];
-                const C i1 = a.nin > 1 ? S[LB + idx] : i0;
-                const C i2 = a.nin > 2 ? S[2 * LB + idx] : i0;
-                const T gx = g * kxv, gy = g * kyv, gz = g * kzv;
-                S[idx] = C{-gx * i0.y, gx * i0.x};
-                S[LB + idx] = C{-gy * i1.y, gy * i1.x};
-                S[2 * LB + idx] = C{-gz * i2.y, gz * i2.x};
-            } else if (op == OP_DIV) {
-                const C i0 = S[idx], i1 = S[LB + idx], i2 = S[2 * LB + idx];
-                const C s = C{kxv * i0.x + kyv * i1.x + kzv * i2.x, kxv * i0.y + kyv * i1.y + kzv * i2.y};
-                S[idx] = C{-g * s.y, g * s.x};
-            } else if (op == OP_CURL) {
-                const C i0 = S[idx], i1 = S[LB + idx], i2 = S[2 * LB + idx];
-                const C c0 = C{kyv * i2.x - kzv * i1.x, kyv * i2.y - kzv * i1.y};
-                const C c1 = C{kzv * i0.x - kxv * i2.x, kzv * i0.y - kxv * i2.y};
-                const C c2 = C{kxv * i1.x - kyv * i0.x, kxv * i1.y - kyv * i0.y};
-                S[idx] = C{-g * c0.y, g * c0.x};
-                S[LB + idx] = C{-g * c1.y, g * c1.x};
-                S[2 * LB + idx] = C{-g * c2.y, g * c2.x};
-            } else if (op == OP_FILTER) {
-                const T z = (reinterpret_cast<const T *>(a.zeta) + (long long)oy * a.Mx + kx)[oz * kzs];
-                if (a.reproject && a.nin == 3) {
-                    // r'_c = z r_c - K sum_d k_c k_d r_d. A product k_c k_d is
-                    // even under k -> -k (and survives in the real output)
-                    // unless exactly one of the two axes sits on its Nyquist
-                    // mode, where the unpaired wavenumber makes it odd.
-                    const T kf[3] = {wavenumber<T>(kx, a.Px, (T)a.kxc, false),
-                                     wavenumber<T>(ky, a.Py, (T)a.kyc, false), wavenumber<T>(n, a.Pz, kzc, false)};
-                    const bool nq[3] = {2 * kx == a.Px, 2 * ky == a.Py, 2 * n == a.Pz};
-                    const C in3[3] = {S[idx], S[LB + idx], S[2 * LB + idx]};
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        C acc = C{0, 0};
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            const T kk = nq[c] == nq[d] ? kf[c] * kf[d] : (T)0;
-                            acc.x += kk * in3[d].x;
-                            acc.y += kk * in3[d].y;
-                        }
-                        S[c * LB + idx] = C{z * in3[c].x - g * acc.x, z * in3[c].y - g * acc.y};
-                    }
-                } else {
-                    for (int c = 0; c < a.nin; ++c) S[c * LB + idx] = cscale(S[c * LB + idx], z);
-                }
-            }
-        }
-        __syncthreads();
-        fft_lines<true, EMZ<T>>(S, W, B, 1, b, t, plan, tws, si, a.nout, LB);
-    }
-
-    if (b < nb) {
-        for (int c = 0; c < a.nout; ++c) {
-            C *dst0 = reinterpret_cast<C *>(pick3(a.out, c));
-            if (dst0 == nullptr) continue;
-            C *dst = dst0 + off + (long long)t * a.axis_stride + b;
-            const C *buf = S + c * LB + b;
-#pragma unroll 4
-            for (int n = t; n < a.n_out; n += rstep, dst += gstep) *dst = buf[n * B];
-        }
-    }
-}
-
-template <typename T, int OP> __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
-{
-    z_body<T, OP>(a, blockIdx.x, blockIdx.y, blockDim.x);
-}
-
-// ---------------------------------------------------------------------------
-// x inverse. Line l rebuilds Z = Xa + i Xb over the full length from the two
-// half spectra (Z[L-k] = conj Xa[k] + i conj Xb[k]), transforms back and
-// writes Re -> row 2l, Im -> row 2l+1, first n_out samples only.
-template <typename T>
-__device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, int nt)
-{
-    using C = typename Cplx<T>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *S = reinterpret_cast<C *>(smem_raw);
-    const int B = a.B, L = a.L, ld = a.plan.L + 1, Mx = a.Mx;
-    C *W = a.plan.generic ? S + B * ld : nullptr;
-    const FftPlanDev &plan = a.plan;
-    const C *tws = stage_twiddles(plan, S + B * ld * (a.plan.generic ? 2 : 1));
-    __shared__ StageInfo si;
-    load_stages(si, a.plan);
-    const C *in = reinterpret_cast<const C *>(pick3(a.in, comp));
-    double *out = pick3(a.out, comp);
-    const int tid = threadIdx.x;
-    const bool live = tid < nt;
-    const long long rows = (long long)a.rows_y * a.rows_z;
-    const long long row0 = (long long)bx * 2 * B;
-    __shared__ long long rofs[2 * MAX_LINES];
-    row_offsets(rofs, row0, 2 * B, rows, a.rows_y, a.in_y, a.ld);
-    __syncthreads();
-
-    for (int line = 0; line < B; ++line) {
-        const long long oa = rofs[2 * line], ob = rofs[2 * line + 1];
-        for (int k = live ? tid : Mx; k < Mx; k += nt) {
-            C xa = C{0, 0}, xb = C{0, 0};
-            if (oa >= 0) xa = in[oa + k];
-            if (ob >= 0) xb = in[ob + k];
-            S[line * ld + k] = C{xa.x - xb.y, xa.y + xb.x};
-            if (k >= 1 && k <= L - Mx) S[line * ld + L - k] = C{xa.x + xb.y, xb.x - xa.y};
-        }
-    }
-    __syncthreads();
-    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
-
-    // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
-    const int no = a.n_out;
-    for (int line = 0; line < B; ++line) {
-        const long long ra = row0 + 2 * line;
-        if (ra >= rows) break;
-        const bool vb = ra + 1 < rows;
-        double *oa = out + ra * a.out_stride, *ob = oa + a.out_stride;
-        const C *ln = S + line * ld;
-        for (int n = live ? tid : no; n < no; n += nt) {
-            const C v = ln[n];
-            oa[n] = (double)v.x;
-            if (vb) ob[n] = (double)v.y;
-        }
-    }
-}
-
-template <typename T> __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
-{
-    xinv_body<T>(a, blockIdx.x, blockIdx.y, blockDim.x);
-}
-
-// ---------------------------------------------------------------------------
-// Batched passes: one launch runs a pass of many independent problems. Each
-// persistent CTA walks the tile list (tile i, i + gridDim.x, ...), copies the
-// arguments of its tile's problem into shared memory and runs the pass body
-// with that problem's thread count (the launch's block size is the largest
-// of them). With the arguments in memory rather than in the constant bank the
-// bodies need more registers: up to 255 a thread at 256 threads a CTA keeps
-// them from spilling (at 512 threads ptxas held them to 64 and spilled
-// 0.6-6.6 KB a thread).
-template <typename Args> __device__ __forceinline__ void load_args(Args &dst, const Args *src)
-{
-    static_assert(sizeof(Args) % sizeof(int) == 0, "argument blocks are whole words");
-    const int *s = reinterpret_cast<const int *>(src);
-    int *d = reinterpret_cast<int *>(&dst);
-    for (int i = threadIdx.x; i < (int)(sizeof(Args) / sizeof(int)); i += blockDim.x) d[i] = s[i];
-}
-
-template <typename T>
-__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_xfwd_batch(const XFwdArgs *args, const BatchTile *tiles, int ntiles)
-{
-    __shared__ XFwdArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();  // the previous tile no longer reads a or the shared buffers
-        load_args(a, args + tl.p);
-        __syncthreads();
-        xfwd_body<T>(a, tl.bx, tl.by, a.B * a.plan.tpl);
-    }
-}
-
-template <typename T, bool INV>
-__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_col_batch(const ColArgs *args, const BatchTile *tiles, int ntiles)
-{
-    __shared__ ColArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();
-        load_args(a, args + tl.p);
-        __syncthreads();
-        col_body<T, INV>(a, tl.bx, tl.by, tl.bz, a.B * a.plan.tpl);
-    }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_z_batch(const ZArgs *args, const BatchTile *tiles, int ntiles)
-{
-    __shared__ ZArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();
-        load_args(a, args + tl.p);
-        __syncthreads();
-        z_body<T, -1>(a, tl.bx, tl.by, a.B * a.plan.tpl);
-    }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_xinv_batch(const XInvArgs *args, const BatchTile *tiles, int ntiles)
-{
-    __shared__ XInvArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();
-        load_args(a, args + tl.p);
-        __syncthreads();
-        xinv_body<T>(a, tl.bx, tl.by, a.B * a.plan.tpl);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Launchers
-
 static int threads_for(const FftPlanDev &p, int B) { return B * p.tpl; }
+
+// bytes of a complex element of the pass precision
+static size_t cplx_bytes(int prec) { return prec == PREC_FP32 ? 8 : 16; }
 
 size_t smem_x(int prec, const FftPlanDev &p, int B)
 {
-    const size_t c = prec == PREC_FP64 ? 16 : 8;
-    return c * ((size_t)B * (p.L + 1) * (p.generic ? 2 : 1) + p.ntw);
+    return cplx_bytes(prec) * ((size_t)B * (p.L + 1) * (p.generic ? 2 : 1) + p.ntw);
 }
 size_t smem_col(int prec, const FftPlanDev &p, int B)
 {
-    const size_t c = prec == PREC_FP64 ? 16 : 8;
-    return c * ((size_t)B * p.L * (p.generic ? 2 : 1) + p.ntw);
+    return cplx_bytes(prec) * ((size_t)B * p.L * (p.generic ? 2 : 1) + p.ntw);
 }
 size_t smem_z(int prec, const FftPlanDev &p, int B, int nbuf)
 {
-    const size_t c = prec == PREC_FP64 ? 16 : 8;
-    return c * ((size_t)B * p.L * (nbuf + (p.generic ? 1 : 0)) + p.ntw);
+    return cplx_bytes(prec) * ((size_t)B * p.L * (nbuf + (p.generic ? 1 : 0)) + p.ntw);
 }
 
 int max_smem_per_block()
@@ -448,12 +32,6 @@ int max_smem_per_block()
     return v;
 }
 
-template <typename K> static cudaError_t prep(K kernel, size_t smem)
-{
-    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return cudaSuccess;
-}
-
 cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st)
 {
     if (a.B > MAX_LINES) return cudaErrorInvalidConfiguration;  // row-offset table size
@@ -462,15 +40,10 @@ cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st)
     dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
     const int nt = threads_for(a.plan, a.B);
     const size_t sm = smem_x(prec, a.plan, a.B);
-    cudaError_t e;
-    if (prec == PREC_FP64) {
-        if ((e = prep(k_xfwd<double>, sm)) != cudaSuccess) return e;
-        k_xfwd<double><<<grid, nt, sm, st>>>(a);
-    } else {
-        if ((e = prep(k_xfwd<float>, sm)) != cudaSuccess) return e;
-        k_xfwd<float><<<grid, nt, sm, st>>>(a);
-    }
-    return cudaGetLastError();
+    if (prec == PREC_FP64) return rt::xfwd<double>(a, grid, nt, sm, st);
+    if (prec == PREC_FP32) return rt::xfwd<float>(a, grid, nt, sm, st);
+    if (prec == PREC_DF64) return rt::xfwd_df(a, grid, nt, sm, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaStream_t st)
@@ -478,41 +51,10 @@ cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaS
     dim3 grid((unsigned)((a.Mx + a.B - 1) / a.B), outer, a.ncomp);
     const int nt = threads_for(a.plan, a.B);
     const size_t sm = smem_col(prec, a.plan, a.B);
-    cudaError_t e;
-#define PS_LAUNCH_COL(T, I)                                         \
-    do {                                                            \
-        if ((e = prep(k_col<T, I>, sm)) != cudaSuccess) return e;   \
-        k_col<T, I><<<grid, nt, sm, st>>>(a);                       \
-    } while (0)
-    if (prec == PREC_FP64) {
-        if (inverse) PS_LAUNCH_COL(double, true); else PS_LAUNCH_COL(double, false);
-    } else {
-        if (inverse) PS_LAUNCH_COL(float, true); else PS_LAUNCH_COL(float, false);
-    }
-#undef PS_LAUNCH_COL
-    return cudaGetLastError();
-}
-
-template <typename T>
-static cudaError_t launch_z_t(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
-{
-    cudaError_t e;
-#define PS_LAUNCH_Z(OPV)                                               \
-    case OPV:                                                          \
-        if ((e = prep(k_z<T, OPV>, sm)) != cudaSuccess) return e;      \
-        k_z<T, OPV><<<grid, nt, sm, st>>>(a);                          \
-        break;
-    switch (a.op) {
-        PS_LAUNCH_Z(OP_NONE)
-        PS_LAUNCH_Z(OP_GRAD)
-        PS_LAUNCH_Z(OP_DIV)
-        PS_LAUNCH_Z(OP_CURL)
-        PS_LAUNCH_Z(OP_FILTER)
-        PS_LAUNCH_Z(OP_FORWARD)
-    default: return cudaErrorInvalidValue;
-    }
-#undef PS_LAUNCH_Z
-    return cudaGetLastError();
+    if (prec == PREC_FP64) return rt::col<double>(inverse, a, grid, nt, sm, st);
+    if (prec == PREC_FP32) return rt::col<float>(inverse, a, grid, nt, sm, st);
+    if (prec == PREC_DF64) return rt::col_df(inverse, a, grid, nt, sm, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st)
@@ -521,7 +63,10 @@ cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st)
     const int nt = threads_for(a.plan, a.B);
     const int nbuf = a.nin > a.nout ? a.nin : a.nout;
     const size_t sm = smem_z(prec, a.plan, a.B, nbuf);
-    return prec == PREC_FP64 ? launch_z_t<double>(a, grid, nt, sm, st) : launch_z_t<float>(a, grid, nt, sm, st);
+    if (prec == PREC_FP64) return rt::z<double>(a, grid, nt, sm, st);
+    if (prec == PREC_FP32) return rt::z<float>(a, grid, nt, sm, st);
+    if (prec == PREC_DF64) return rt::z_df(a, grid, nt, sm, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
@@ -532,100 +77,46 @@ cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
     dim3 grid((unsigned)((lines + a.B - 1) / a.B), a.ncomp);
     const int nt = threads_for(a.plan, a.B);
     const size_t sm = smem_x(prec, a.plan, a.B);
-    cudaError_t e;
-    if (prec == PREC_FP64) {
-        if ((e = prep(k_xinv<double>, sm)) != cudaSuccess) return e;
-        k_xinv<double><<<grid, nt, sm, st>>>(a);
-    } else {
-        if ((e = prep(k_xinv<float>, sm)) != cudaSuccess) return e;
-        k_xinv<float><<<grid, nt, sm, st>>>(a);
-    }
-    return cudaGetLastError();
-}
-
-// Batched launchers: nt threads and smem bytes a CTA (the largest over the
-// batch's problems), as many persistent CTAs as fit on the GPU at once.
-template <typename K> static cudaError_t launch_persistent(K kernel, int ntiles, int nt, size_t smem, cudaStream_t st,
-                                                          int &grid)
-{
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0, dev = 0, sms = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, smem)) != cudaSuccess) return e;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    grid = ntiles < per_sm * sms ? ntiles : per_sm * sms;
-    return cudaSuccess;
+    if (prec == PREC_FP64) return rt::xinv<double>(a, grid, nt, sm, st);
+    if (prec == PREC_FP32) return rt::xinv<float>(a, grid, nt, sm, st);
+    if (prec == PREC_DF64) return rt::xinv_df(a, grid, nt, sm, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_xfwd_batch(int prec, const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
                               cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    int grid = 0;
-    cudaError_t e;
-    if (prec == PREC_FP64) {
-        if ((e = launch_persistent(k_xfwd_batch<double>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
-        k_xfwd_batch<double><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    } else {
-        if ((e = launch_persistent(k_xfwd_batch<float>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
-        k_xfwd_batch<float><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    }
-    return cudaGetLastError();
+    if (prec == PREC_FP64) return rt::xfwd_batch<double>(args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP32) return rt::xfwd_batch<float>(args, tiles, ntiles, nt, smem, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_col_batch(int prec, int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt,
                              size_t smem, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    int grid = 0;
-    cudaError_t e;
-#define PS_LAUNCH_COLB(T, I)                                                                            \
-    do {                                                                                                \
-        if ((e = launch_persistent(k_col_batch<T, I>, ntiles, nt, smem, st, grid)) != cudaSuccess)      \
-            return e;                                                                                   \
-        k_col_batch<T, I><<<grid, nt, smem, st>>>(args, tiles, ntiles);                                 \
-    } while (0)
-    if (prec == PREC_FP64) {
-        if (inverse) PS_LAUNCH_COLB(double, true); else PS_LAUNCH_COLB(double, false);
-    } else {
-        if (inverse) PS_LAUNCH_COLB(float, true); else PS_LAUNCH_COLB(float, false);
-    }
-#undef PS_LAUNCH_COLB
-    return cudaGetLastError();
+    if (prec == PREC_FP64) return rt::col_batch<double>(inverse, args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP32) return rt::col_batch<float>(inverse, args, tiles, ntiles, nt, smem, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_z_batch(int prec, const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
                            cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    int grid = 0;
-    cudaError_t e;
-    if (prec == PREC_FP64) {
-        if ((e = launch_persistent(k_z_batch<double>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
-        k_z_batch<double><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    } else {
-        if ((e = launch_persistent(k_z_batch<float>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
-        k_z_batch<float><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    }
-    return cudaGetLastError();
+    if (prec == PREC_FP64) return rt::z_batch<double>(args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP32) return rt::z_batch<float>(args, tiles, ntiles, nt, smem, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_xinv_batch(int prec, const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
                               cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    int grid = 0;
-    cudaError_t e;
-    if (prec == PREC_FP64) {
-        if ((e = launch_persistent(k_xinv_batch<double>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
-        k_xinv_batch<double><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    } else {
-        if ((e = launch_persistent(k_xinv_batch<float>, ntiles, nt, smem, st, grid)) != cudaSuccess) return e;
-        k_xinv_batch<float><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    }
-    return cudaGetLastError();
+    if (prec == PREC_FP64) return rt::xinv_batch<double>(args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP32) return rt::xinv_batch<float>(args, tiles, ntiles, nt, smem, st);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace ps

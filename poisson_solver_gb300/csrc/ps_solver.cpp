@@ -273,6 +273,19 @@ const Plan &Solver::plan(int L, int prec, int emax, int pv)
             for (size_t i = 0; i < tab.size(); ++i) h[i] = make_double2((double)tab[i].real(), (double)tab[i].imag());
             pl->table.ensure(h.size() * sizeof(double2));
             PS_CK(cudaMemcpy(pl->table.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        } else if (prec == PREC_DF64) {
+            // (re hi, re lo, im hi, im lo), each part rounded from the extended-precision value
+            std::vector<float4> h(tab.size());
+            auto split = [](long double v, float &hi, float &lo) {
+                hi = (float)v;
+                lo = (float)(v - (long double)hi);
+            };
+            for (size_t i = 0; i < tab.size(); ++i) {
+                split(tab[i].real(), h[i].x, h[i].y);
+                split(tab[i].imag(), h[i].z, h[i].w);
+            }
+            pl->table.ensure(h.size() * sizeof(float4));
+            PS_CK(cudaMemcpy(pl->table.p, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice));
         } else {
             std::vector<float2> h(tab.size());
             for (size_t i = 0; i < tab.size(); ++i) h[i] = make_float2((float)tab[i].real(), (float)tab[i].imag());
@@ -293,7 +306,7 @@ static int pick_lines(int prec, int tpl, const std::function<size_t(int)> &smem,
                       int pref = 0, int max_threads = MAX_THREADS)
 {
     static const int limit = max_smem_per_block() - 1024;  // room for the static stage table
-    int B = pref > 0 ? pref : (prec == PREC_FP64 ? 8 : 16);
+    int B = pref > 0 ? pref : (prec == PREC_FP32 ? 16 : 8);
     if (const char *v = env ? getenv(env) : nullptr) {
         const int want = atoi(v);
         if (want >= 1 && want <= 64 && (want & (want - 1)) == 0) B = want;
@@ -385,11 +398,14 @@ void Solver::finish_setup()
     kzp = ((dims == 2 ? oy : oz) + 3) & ~3;
     pushed = produced = rhs_ready = 0;
     kern32.release();
+    kern_df.release();
     kernzf32.release();
     zeta64.release();
     zeta32.release();
+    zeta_df.release();
     smooth64.release();
     smooth32.release();
+    smooth_df.release();
     smooth_s = -1.0;
     stage.release();
     for (int c = 0; c < 3; ++c) {
@@ -416,8 +432,9 @@ void Solver::set_option(int option, int value)
     case PS_OPT_REPROJECT: opt_reproject = value != 0; rhs_ready = 0; break;
     case PS_OPT_PASS_TIMING: opt_timing = value != 0; break;
     case PS_OPT_PRECISION:
-        if (value != PS_PREC_FP64 && value != PS_PREC_FP32) throw Error(PS_ERR_ARGUMENT, "unknown precision");
-        precision = value == PS_PREC_FP64 ? PREC_FP64 : PREC_FP32;
+        if (value != PS_PREC_FP64 && value != PS_PREC_FP32 && value != PS_PREC_DF64)
+            throw Error(PS_ERR_ARGUMENT, "unknown precision");
+        precision = value == PS_PREC_FP64 ? PREC_FP64 : value == PS_PREC_FP32 ? PREC_FP32 : PREC_DF64;
         rhs_ready = 0;
         break;
     default: throw Error(PS_ERR_ARGUMENT, "unknown option");
@@ -453,7 +470,8 @@ int Solver::get_option(int option) const
     case PS_OPT_DIV: return opt_div;
     case PS_OPT_CURL: return opt_curl;
     case PS_OPT_REPROJECT: return opt_reproject;
-    case PS_OPT_PRECISION: return precision == PREC_FP64 ? PS_PREC_FP64 : PS_PREC_FP32;
+    case PS_OPT_PRECISION:
+        return precision == PREC_FP64 ? PS_PREC_FP64 : precision == PREC_FP32 ? PS_PREC_FP32 : PS_PREC_DF64;
     case PS_OPT_PASS_TIMING: return opt_timing;
     default: throw Error(PS_ERR_ARGUMENT, "unknown option");
     }
@@ -570,6 +588,13 @@ void Solver::ensure_kernel(int prec)
 {
     if (prec == PREC_FP64) return;
     const size_t nk = (size_t)Mx * oy * oz;
+    if (prec == PREC_DF64) {
+        if (!kern_df.p) {
+            kern_df.ensure(nk * sizeof(float2));
+            PS_CK(launch_to_df((const double *)kern64.p, (float2 *)kern_df.p, nk, stream));
+        }
+        return;
+    }
     if (!kern32.p) {
         kern32.ensure(nk * sizeof(float));
         PS_CK(launch_to_fp32((const double *)kern64.p, (float *)kern32.p, nk, stream));
@@ -607,6 +632,10 @@ void Solver::ensure_zeta(int prec)
     if (prec == PREC_FP32 && !zeta32.p) {
         zeta32.ensure(nk * sizeof(float));
         PS_CK(launch_to_fp32((const double *)zeta64.p, (float *)zeta32.p, nk, stream));
+    }
+    if (prec == PREC_DF64 && !zeta_df.p) {
+        zeta_df.ensure(nk * sizeof(float2));
+        PS_CK(launch_to_df((const double *)zeta64.p, (float2 *)zeta_df.p, nk, stream));
     }
 }
 
@@ -665,12 +694,16 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
         if ((out_mask >> c & 1) && Aout[c]) write_mask |= 1 << c;
 
     const int prec = precision;
-    const size_t csz = prec == PREC_FP64 ? sizeof(double2) : sizeof(float2);
+    const size_t csz = prec == PREC_FP32 ? sizeof(float2) : sizeof(double2);  // double-float complex: 16 bytes
     ensure_kernel(prec);
     if (op == OP_FILTER && filter_source == 0) ensure_zeta(prec);
     if (op == OP_FILTER && filter_source == 1 && prec == PREC_FP32 && !smooth32.p) {
         smooth32.ensure((size_t)Mx * oy * oz * sizeof(float));
         PS_CK(launch_to_fp32((const double *)smooth64.p, (float *)smooth32.p, (size_t)Mx * oy * oz, stream));
+    }
+    if (op == OP_FILTER && filter_source == 1 && prec == PREC_DF64 && !smooth_df.p) {
+        smooth_df.ensure((size_t)Mx * oy * oz * sizeof(float2));
+        PS_CK(launch_to_df((const double *)smooth64.p, (float2 *)smooth_df.p, (size_t)Mx * oy * oz, stream));
     }
     for (int c = 0; c < 3; ++c)
         if ((in_mask | out_mask) >> c & 1) work[c].ensure(work_elems() * csz);
@@ -739,11 +772,11 @@ int Solver::prepare(const double *const Bin[3], double *const Aout[3], bool filt
     za.row_stride = ldx;
     za.op = op;
     za.reproject = op == OP_FILTER && filter_source == 0 && opt_reproject && in_mask == 7;
-    za.kern = prec == PREC_FP64 ? kern64.p : kern32.p;
+    za.kern = prec == PREC_FP64 ? kern64.p : prec == PREC_FP32 ? kern32.p : kern_df.p;
     za.zeta = nullptr;
     if (op == OP_FILTER)
-        za.zeta = filter_source == 1 ? (prec == PREC_FP64 ? smooth64.p : smooth32.p)
-                                     : (prec == PREC_FP64 ? zeta64.p : zeta32.p);
+        za.zeta = filter_source == 1 ? (prec == PREC_FP64 ? smooth64.p : prec == PREC_FP32 ? smooth32.p : smooth_df.p)
+                                     : (prec == PREC_FP64 ? zeta64.p : prec == PREC_FP32 ? zeta32.p : zeta_df.p);
     za.oct_y = oy;
     za.kern_zf = prec == PREC_FP32 ? static_cast<const float *>(kernzf32.p) : nullptr;
     za.kzp = kzp;
@@ -944,7 +977,7 @@ PassChoice Solver::default_choice(int pass, const PassArgs &pa)
     else if (axis > 0 && family_ok(pass, 'w', pa)) fam = 'w';
     else fam = family_ok(pass, 'p', pa) ? 'p' : 'r';
 
-    int pref = precision == PREC_FP64 ? 8 : 16;
+    int pref = precision == PREC_FP32 ? 16 : 8;
     if (fam == 'w') pref = pass == 0 || pass == 4 ? 4 : 8;
     if (fam == 't') pref = 8;  // 64-byte rows: 8.7 against 10.0 ms with 4 for the 512^3 curl pass
     if (fam == 'p' && pass == 0) pref = 2;
@@ -1110,7 +1143,7 @@ std::string Solver::tune_key(int pass, const PassArgs &pa)
         device_tag = d.str();
     }
     std::ostringstream k;
-    k << device_tag << ":" << (precision == PREC_FP64 ? "fp64" : "fp32") << ":" << dims << "d:N" << n[0] << 'x'
+    k << device_tag << ":" << (precision == PREC_FP64 ? "fp64" : precision == PREC_FP32 ? "fp32" : "df64") << ":" << dims << "d:N" << n[0] << 'x'
       << n[1] << 'x' << n[2] << ":P" << P[0] << 'x' << P[1] << 'x' << P[2] << ":op" << pa.z.op << ":in" << pa.x.ncomp
       << ":out" << pa.xi.ncomp << ":z" << pa.z.nin << pa.z.nout << ":pass" << pass;
     return k.str();
@@ -1447,6 +1480,7 @@ void Solver::smooth3d(double s)
     if (smooth_s != s) {
         smooth64.ensure(nk * sizeof(double));
         smooth32.release();
+        smooth_df.release();
         KernelFillArgs fa{};
         fa.zeta_out = (double *)smooth64.p;
         fa.Mx = Mx;
@@ -1500,7 +1534,8 @@ void Solver::check_status()
 
 size_t Solver::device_bytes() const
 {
-    size_t s = kern64.bytes + kern32.bytes + kernzf32.bytes + zeta64.bytes + zeta32.bytes;
+    size_t s = kern64.bytes + kern32.bytes + kern_df.bytes + kernzf32.bytes + zeta64.bytes + zeta32.bytes +
+               zeta_df.bytes + smooth64.bytes + smooth32.bytes + smooth_df.bytes;
     for (int c = 0; c < 3; ++c) s += work[c].bytes + fb[c].bytes + fa[c].bytes + fr[c].bytes;
     for (auto &kv : plans) s += kv.second->table.bytes;
     return s;

@@ -113,10 +113,10 @@ struct Solver {
     int opt_grad = 0, opt_div = 0, opt_curl = 0, opt_reproject = 0;
     int precision = PREC_FP64;
 
-    DevBuf kern64, kern32;  // octant K = G zeta / (Px Py Pz)
+    DevBuf kern64, kern32, kern_df;  // octant K = G zeta / (Px Py Pz); kern_df: double-float pairs
     DevBuf kernzf32;        // FP32 K with z fastest, [oy][Mx][kzp] (unbounded z of 256..1024 points)
-    DevBuf zeta64, zeta32;  // octant zeta / (Px Py Pz), built on first use
-    DevBuf smooth64, smooth32;  // octant exp(-s^2 |k|^2 / 2) / (Px Py Pz) of smooth3d(s)
+    DevBuf zeta64, zeta32, zeta_df;  // octant zeta / (Px Py Pz), built on first use
+    DevBuf smooth64, smooth32, smooth_df;  // octant exp(-s^2 |k|^2 / 2) / (Px Py Pz) of smooth3d(s)
     double smooth_s = -1.0;     // s the smooth octants hold (-1: none)
     int filter_source = 0;      // the filter pass multiplies by zeta (0) or the smooth octant (1)
     DevBuf stage;               // packed interleaved fields for push/pull_interleaved

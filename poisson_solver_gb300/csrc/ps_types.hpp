@@ -9,13 +9,16 @@ constexpr int MAX_STAGES = 16;
 constexpr int MAX_THREADS = 512;  // CTA size bound of the pass kernels (<= 128 registers a thread)
 constexpr int MAX_LINES = 64;     // lines a CTA of any pass kernel (the x passes keep 2 row offsets a line)
 
-enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
+// Pass precision: FP64, FP32, or double-float (pairs of FP32 numbers, about
+// 48 significant bits: ps_dfloat.cuh).
+enum Precision { PREC_FP64 = 0, PREC_FP32 = 1, PREC_DF64 = 2 };
 
 // Register elements a thread holds per FFT stage, which also caps the radix:
-// 8 complex doubles (radix <= 8) or 16 complex floats (radix <= 16). The
-// fused z pass holds three components in shared memory, so its FP32 variant
-// uses 8 to double the threads per line at the same footprint.
-__host__ __device__ constexpr int e_max(int prec) { return prec == PREC_FP64 ? 8 : 16; }
+// 8 complex doubles or double-floats (radix <= 8) or 16 complex floats
+// (radix <= 16). The fused z pass holds three components in shared memory,
+// so its FP32 variant uses 8 to double the threads per line at the same
+// footprint.
+__host__ __device__ constexpr int e_max(int prec) { return prec == PREC_FP32 ? 16 : 8; }
 __host__ __device__ constexpr int e_max_z(int /*prec*/) { return 8; }
 
 // One 1D transform length as the kernels see it (see ps_fft.cuh).
@@ -260,6 +263,7 @@ cudaError_t launch_kernel_fill(const KernelFillArgs &a, cudaStream_t st);
 cudaError_t launch_deinterleave(const double *packed, int ncomp, long long n, double *const out[3], cudaStream_t st);
 cudaError_t launch_interleave(const double *const in[3], int ncomp, long long n, double *packed, cudaStream_t st);
 cudaError_t launch_to_fp32(const double *in, float *out, size_t n, cudaStream_t st);
+cudaError_t launch_to_df(const double *in, float2 *out, size_t n, cudaStream_t st);  // (hi, lo) pairs
 // FP32 copy of the octant [oz][oy][Mx] with z fastest: out[(y Mx + x) kzp + z],
 // zero for oz <= z < kzp (each column a whole number of 16-byte units).
 cudaError_t launch_kernel_zfast(const double *kern, float *out, int Mx, int oy, int oz, int kzp, cudaStream_t st);

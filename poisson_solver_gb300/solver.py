@@ -121,8 +121,10 @@ class PoissonSolver:
         self._call("ps_set_option", L.PS_OPT_REPROJECT, int(bool(toggle)))
 
     def set_precision(self, precision: str):
-        """'fp64' (default) or 'fp32' transforms; the kernel is always built in FP64."""
-        v = {"fp64": L.PS_PREC_FP64, "fp32": L.PS_PREC_FP32}[precision]
+        """'fp64' (default), 'fp32' or 'df64' (double-float: pairs of FP32
+        numbers, FP64-class accuracy) transforms; the kernel is always built
+        in FP64."""
+        v = {"fp64": L.PS_PREC_FP64, "fp32": L.PS_PREC_FP32, "df64": L.PS_PREC_DF64}[precision]
         self._call("ps_set_option", L.PS_OPT_PRECISION, v)
 
     def set_stream(self, stream_handle: int):
@@ -256,7 +258,7 @@ class PoissonBatch:
 
     def __init__(self, precision: str = "fp64"):
         self._lib = L.load()
-        prec = {"fp64": L.PS_PREC_FP64, "fp32": L.PS_PREC_FP32}[precision]
+        prec = {"fp64": L.PS_PREC_FP64, "fp32": L.PS_PREC_FP32, "df64": L.PS_PREC_DF64}[precision]
         h = ctypes.c_void_p()
         st = self._lib.ps_batch_create(ctypes.byref(h), prec)
         if st != L.PS_OK:
