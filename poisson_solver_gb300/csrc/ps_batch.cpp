@@ -1,6 +1,6 @@
 // Batched solves: many independent problems (any grid, boundary conditions,
 // components and output option each) run as five launches, one per pass,
-// each launch covering the tiles of every problem (ps_kernels.cu, k_*_batch).
+// each launch covering the tiles of every problem (k_*_batch in ps_kernels_body.cuh).
 // The five launches are captured once into a CUDA graph and replayed by every
 // solve until the set of problems, their options or their pushed components
 // change.

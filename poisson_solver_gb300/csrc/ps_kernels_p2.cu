@@ -1,5 +1,5 @@
 // Pass kernels specialised on power-of-two transform lengths (FP32 hot path):
-// the same five passes as ps_kernels.cu, built on the compile-time FFT core of
+// the same five passes as ps_kernels_body.cuh, built on the compile-time FFT core of
 // ps_fft_p2.cuh. The host uses them for FP32 and 64 <= L <= 2048 and falls
 // back to the run-time kernels otherwise (p2::supported).
 #include <cuda_runtime.h>

@@ -125,13 +125,14 @@ struct XInvArgs {
     FftPlanDev plan;
 };
 
-// Launchers (ps_kernels.cu). They return the launch status.
+// Launchers of the run-time kernels (ps_kernels.cu; bodies in
+// ps_kernels_body.cuh). They return the launch status.
 cudaError_t launch_xfwd(int prec, const XFwdArgs &a, cudaStream_t st);
 cudaError_t launch_col(int prec, int inverse, const ColArgs &a, int outer, cudaStream_t st);
 cudaError_t launch_z(int prec, const ZArgs &a, int ny, cudaStream_t st);
 cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st);
 
-// Batched passes (ps_kernels.cu): one launch runs the tiles of many problems.
+// Batched passes (ps_kernels.cu; FP64 and FP32): one launch runs the tiles of many problems.
 // Tile = (problem, bx, by, bz): x passes (line block, component); y passes
 // (column block, z slab, component); z pass (column block, ky row).
 struct BatchTile {
