@@ -10,11 +10,12 @@
 // straight from registers along the rows (a warp instruction covers 32
 // consecutive elements of a row, 256 contiguous bytes):
 //   forward: the first stage loads its 32 (HALF: 16, the rest is the zero
-//     padding) FP64 samples of each row, the last stage's line is split into
-//     the two half spectra on the way out;
-//   inverse: the two half spectra are combined into the line on the way in,
-//     the last stage stores Re and Im of its outputs (HALF: the kept half)
-//     to the two FP64 rows.
+//     padding) FP64 samples of each row, the last stage's outputs are split
+//     into the two half spectra on the way out, each beside its mirror
+//     fetched from another lane by a warp shuffle;
+//   inverse: the two half spectra are combined into the first stage's
+//     inputs in registers (mirrors by warp shuffles), the last stage stores
+//     Re and Im of its outputs (HALF: the kept half) to the two FP64 rows.
 // Against the length-specialised kernels (16 elements a thread, three stages
 // through shared memory, CTA barriers) this halves the shared-memory passes.
 #include "ps_wide.cuh"
@@ -83,25 +84,34 @@ __global__ void __launch_bounds__(XQ_THREADS, 3) k_xfq(const XFwdArgs a)
         write_line<L, 0>(line, t, v);
     }
     __syncwarp();
-    {
-        C v[TL::U][TL::R];
-        read_line<L, LAST>(line, t, v);
-        twiddle_dft<L, LAST, false>(v, TW, t);
-        write_line<L, LAST>(line, t, v);  // the positions this thread read
-    }
-    __syncwarp();
-    // separate the half spectra of rows a and b
+    C v[TL::U][TL::R];
+    read_line<L, LAST>(line, t, v);
+    twiddle_dft<L, LAST, false>(v, TW, t);
+    // Separate the half spectra of rows a and b straight from the registers:
+    // this thread holds Z[k], k = t + TPL u + 32 r, and the mirror Z[L - k]
+    // sits in lane TPL - t of the line at (U - 1 - u, R - 1 - r), or for
+    // t = 0 in this thread ((0, R - r mod R) for u = 0, else (U - u, R - 1 - r));
+    // one warp shuffle a value, for the k < L/2 this thread stores.
+    constexpr int U = TL::U, R = TL::R;
     const long long oa = spec_row(ra, rows, a.rows_y, a.out_y, a.ld), ob = spec_row(rb, rows, a.rows_y, a.out_y, a.ld);
-    if (oa < 0) return;
-    C *outa = out + oa + t, *outb = out + ob + t;
+    C *outa = out + (oa >= 0 ? oa : 0), *outb = out + (ob >= 0 ? ob : 0);
+    const int lane = threadIdx.x & 31;
+    const int src = (lane & ~(Q::TPL - 1)) | ((Q::TPL - t) & (Q::TPL - 1));
 #pragma unroll
-    for (int j = 0; j < Q::KPER; ++j) {
-        const int k = t + j * Q::TPL;
-        if (k < Q::Mx) {
-            const C z = line[skw(k)], w = line[skw((L - k) & (L - 1))];
-            outa[j * Q::TPL] = C{0.5f * (z.x + w.x), 0.5f * (z.y - w.y)};
-            if (ob >= 0) outb[j * Q::TPL] = C{0.5f * (z.y + w.y), 0.5f * (w.x - z.x)};
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int r = 0; r < R / 2; ++r) {
+            const C z = v[u][r], p = v[U - 1 - u][R - 1 - r];
+            C w = C{__shfl_sync(0xffffffffu, p.x, src), __shfl_sync(0xffffffffu, p.y, src)};
+            if (t == 0) w = v[u == 0 ? 0 : U - u][u == 0 ? (R - r) % R : R - 1 - r];
+            const int k = t + Q::TPL * u + 32 * r;
+            if (oa >= 0) outa[k] = C{0.5f * (z.x + w.x), 0.5f * (z.y - w.y)};
+            if (ob >= 0) outb[k] = C{0.5f * (z.y + w.y), 0.5f * (w.x - z.x)};
         }
+    if (t == 0) {  // k = L/2 is its own mirror
+        const C z = v[0][R / 2];
+        if (oa >= 0) outa[L / 2] = C{0.5f * (z.x + z.x), 0.5f * (z.y - z.y)};
+        if (ob >= 0) outb[L / 2] = C{0.5f * (z.y + z.y), 0.5f * (z.x - z.x)};
     }
 }
 
@@ -138,22 +148,27 @@ __global__ void __launch_bounds__(XQ_THREADS, 2) k_xiq(const XInvArgs a)
             xa[j] = (live && ia >= 0) ? pa[j * Q::TPL] : C{0.f, 0.f};
             xb[j] = (live && ib >= 0) ? pb[j * Q::TPL] : C{0.f, 0.f};
         }
+        // The first stage's inputs Z[t + TPL r], r < 32, from the registers:
+        // Z[k] = Xa[k] + i Xb[k] for r < 16 (k < L/2); above, the mirror
+        // conj(Xa[k']) + i conj(Xb[k']) of k' = L - k, loaded by lane TPL - t
+        // of the line at j = 31 - r (one warp shuffle), or for t = 0 by this
+        // thread (Z[L/2] directly at j = 16, then the mirrors of j = 32 - r).
+        // j runs down so the loaded values die as they are used.
+        static_assert(Q::KPER == 17, "16 values below L/2 a thread, and L/2 itself");
+        const int lane = threadIdx.x & 31;
+        const int src = (lane & ~(Q::TPL - 1)) | ((Q::TPL - t) & (Q::TPL - 1));
+        C v0[1][32];
+        C own = C{xa[16].x - xb[16].y, xa[16].y + xb[16].x};  // t = 0: Z[L/2]
 #pragma unroll
-        for (int j = 0; j < Q::KPER; ++j) {
-            const int k = t + j * Q::TPL;
-            if (k < Q::Mx) {
-                line[skw(k)] = C{xa[j].x - xb[j].y, xa[j].y + xb[j].x};
-                if (k >= 1 && k <= L - Q::Mx) line[skw(L - k)] = C{xa[j].x + xb[j].y, xb[j].x - xa[j].y};
-            }
+        for (int j = 15; j >= 0; --j) {
+            v0[0][j] = C{xa[j].x - xb[j].y, xa[j].y + xb[j].x};
+            const C m = C{xa[j].x + xb[j].y, xb[j].x - xa[j].y};
+            const C got = C{__shfl_sync(0xffffffffu, m.x, src), __shfl_sync(0xffffffffu, m.y, src)};
+            v0[0][31 - j] = t == 0 ? own : got;
+            own = m;
         }
-    }
-    __syncwarp();
-    {
-        C v[1][32];
-        read_line<L, 0>(line, t, v);
-        dft<32, true>(v[0]);  // the first stage has no twiddles (m = 1)
-        __syncwarp();
-        write_line<L, 0>(line, t, v);
+        dft<32, true>(v0[0]);  // the first stage has no twiddles (m = 1)
+        write_line<L, 0>(line, t, v0);
     }
     __syncwarp();
     C v[TL::U][TL::R];
