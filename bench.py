@@ -58,6 +58,11 @@ WORKLOADS = {
                     desc="64 independent problems in one batched solve: sizes uniform in [32, 192] per axis, "
                          "boundary conditions uniform over {000, 111, 110, 001}, 1-3 components, "
                          "Gaussian-blob sources (random centres, sigma in [0.05, 0.2]), output A, reg 2"),
+    "batch64p2": dict(kind="batch", problems=64, seed=5, reg=2, sizes=(32, 64, 128),
+                      desc="64 independent problems in one batched solve: sides drawn from {32, 64, 128} per axis "
+                           "(power-of-two padded lengths: FP32 passes the compiled families cover run with them), "
+                           "boundary conditions uniform over {000, 111, 110, 001}, 1-3 components, "
+                           "Gaussian-blob sources, output A, reg 2"),
 }
 
 BATCH_BCS = [(0, 0, 0), (1, 1, 1), (1, 1, 0), (0, 0, 1)]
@@ -123,7 +128,10 @@ def batch_problems(w):
     rng = np.random.default_rng(w["seed"])
     probs = []
     for _ in range(w["problems"]):
-        nc = tuple(int(v) for v in rng.integers(32, 193, 3))
+        if "sizes" in w:
+            nc = tuple(int(v) for v in rng.choice(w["sizes"], 3))
+        else:
+            nc = tuple(int(v) for v in rng.integers(32, 193, 3))
         bc = BATCH_BCS[int(rng.integers(0, 4))]
         ncomp = int(rng.integers(1, 4))
         blobs = [(rng.uniform(-0.6, 0.6, 3), rng.uniform(0.05, 0.2), rng.standard_normal()) for _ in range(ncomp)]

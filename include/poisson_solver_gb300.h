@@ -299,7 +299,9 @@ int ps_batch_pull_device(ps_batch *b, int index, double *ax, double *ay, double 
 int ps_batch_set_stream(ps_batch *b, void *stream);
 int ps_batch_synchronize(ps_batch *b);
 enum {
-    PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0, /* kernels one batched solve launches (5) */
+    PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0, /* kernels one batched solve launches: the batched launches with
+                                             tiles, plus the passes of FP32 problems routed to their own
+                                             kernel family (power-of-two lengths the compiled families cover) */
     PS_BATCH_INFO_TILES_PER_SOLVE = 1,    /* CTA tiles of the last captured solve, all passes */
     PS_BATCH_INFO_POINTS = 2              /* grid points over all problems */
 };

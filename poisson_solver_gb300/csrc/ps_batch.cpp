@@ -53,6 +53,13 @@ struct Batch {
     // transforms; ps_batch_autotune times them too.
     int pv[3] = {0, 0, 0};
     std::vector<int> write_masks;  // outputs of each problem in the captured solve
+    // Passes that a problem runs with its own kernel family instead of the
+    // batched run-time launch (its usual choice, when that is not the
+    // run-time family: power-of-two lengths in FP32), launched after the
+    // batched launch of the pass with the problem's own arguments.
+    std::vector<PassArgs> own_args;
+    std::vector<std::array<PassChoice, 5>> own_choice;
+    std::vector<int> routed[5];
     bool dirty = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -166,26 +173,45 @@ struct Batch {
         PS_BCK(cudaMemcpy(e.tiles.p, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice));
     }
 
-    // Pass k of every problem as one launch on stream st.
-    cudaError_t launch(int k, cudaStream_t st) const
+    // Pass k of every problem on stream st: one batched launch over the
+    // problems it covers, then the routed problems' own launches.
+    cudaError_t launch(int k, cudaStream_t st)
     {
         const int prec = precision;
         const PassExec &e = ex[k];
+        cudaError_t r;
         switch (k) {
         case 0:
-            return launch_xfwd_batch(prec, (const XFwdArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
-                                     e.smem, st);
+            r = launch_xfwd_batch(prec, (const XFwdArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
+                                  e.smem, st);
+            break;
         case 1:
         case 3:
-            return launch_col_batch(prec, k == 3, (const ColArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles,
-                                    e.nt, e.smem, st);
+            r = launch_col_batch(prec, k == 3, (const ColArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
+                                 e.smem, st);
+            break;
         case 2:
-            return launch_z_batch(prec, (const ZArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt, e.smem,
-                                  st);
+            r = launch_z_batch(prec, (const ZArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt, e.smem, st);
+            break;
         default:
-            return launch_xinv_batch(prec, (const XInvArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
-                                     e.smem, st);
+            r = launch_xinv_batch(prec, (const XInvArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
+                                  e.smem, st);
         }
+        if (r != cudaSuccess) return r;
+        try {
+            for (int p : routed[k]) items[p]->launch_on(k, own_choice[p][k], own_args[p], st);
+        } catch (const Error &err) {
+            throw Error(err.status, std::string("routed pass: ") + err.what());
+        }
+        return cudaSuccess;
+    }
+
+    // launches of one solve: the batched launches with tiles and the routed ones
+    int launches_per_solve() const
+    {
+        int n = 0;
+        for (int k = 0; k < 5; ++k) n += (ex[k].ntiles > 0) + (int)routed[k].size();
+        return n;
     }
 
     void build()
@@ -203,6 +229,8 @@ struct Batch {
         std::vector<PassArgs> pa(n);
         std::vector<const Plan *> plx(n), ply(n), plz(n);
         write_masks.assign(n, 0);
+        own_choice.assign(n, {});
+        for (auto &r : routed) r.clear();
         for (int p = 0; p < n; ++p) {
             Solver &s = *items[p];
             if (!s.pushed) throw Error(PS_ERR_STATE, "problem " + std::to_string(p) + ": solve called before push");
@@ -218,24 +246,46 @@ struct Batch {
                 }
             }
             write_masks[p] = s.prepare(Bin, Aout, false, pa[p]);
+            for (int k = 0; k < 5; ++k) {
+                own_choice[p][k] = PassChoice{'r', 1};
+                if (k >= 3 && !write_masks[p]) continue;
+                const PassChoice c = s.pass_choice(k, pa[p]);
+                if (c.fam != 'r') {
+                    own_choice[p][k] = c;
+                    routed[k].push_back(p);
+                }
+            }
             plx[p] = &s.plan(s.P[0], prec, 0, pv[0]);
             ply[p] = &s.plan(s.P[1], prec, 0, pv[1]);
             plz[p] = &s.plan(s.P[2], prec, e_max_z(prec), pv[2]);  // the z body's element budget
         }
-        std::vector<int> tx(n), ty(n), tz(n), Bx, By, Bz;
+        // launch shapes over the problems each batched launch covers (x: passes
+        // 0 and 4, y: 1 and 3, z: 2)
+        auto batched = [&](int p, int k) { return own_choice[p][k].fam == 'r'; };
+        std::vector<int> gx, gy, gz;  // problems in the batched x, y and z launches
         for (int p = 0; p < n; ++p) {
-            tx[p] = plx[p]->dev.tpl;
-            ty[p] = ply[p]->dev.tpl;
-            tz[p] = plz[p]->dev.tpl;
+            if (batched(p, 0) || (write_masks[p] && batched(p, 4))) gx.push_back(p);
+            if (batched(p, 1) || (write_masks[p] && batched(p, 3))) gy.push_back(p);
+            if (batched(p, 2)) gz.push_back(p);
         }
-        choose_lines(tx, [&](int p, int B) { return smem_x(prec, plx[p]->dev, B); }, MAX_LINES, cap[0], start[0], Bx,
-                     ex[0].nt, ex[0].smem);
-        choose_lines(ty, [&](int p, int B) { return smem_col(prec, ply[p]->dev, B); }, MAX_LINES, cap[1], start[1], By,
-                     ex[1].nt, ex[1].smem);
+        std::vector<int> tx, ty, tz, Bgx, Bgy, Bgz, Bx(n, 1), By(n, 1), Bz(n, 1);
+        for (int p : gx) tx.push_back(plx[p]->dev.tpl);
+        for (int p : gy) ty.push_back(ply[p]->dev.tpl);
+        for (int p : gz) tz.push_back(plz[p]->dev.tpl);
+        choose_lines(tx, [&](int i, int B) { return smem_x(prec, plx[gx[i]]->dev, B); }, MAX_LINES, cap[0], start[0],
+                     Bgx, ex[0].nt, ex[0].smem);
+        choose_lines(ty, [&](int i, int B) { return smem_col(prec, ply[gy[i]]->dev, B); }, MAX_LINES, cap[1], start[1],
+                     Bgy, ex[1].nt, ex[1].smem);
         choose_lines(
             tz,
-            [&](int p, int B) { return smem_z(prec, plz[p]->dev, B, std::max(pa[p].z.nin, pa[p].z.nout)); },
-            MAX_LINES, cap[2], start[2], Bz, ex[2].nt, ex[2].smem);
+            [&](int i, int B) {
+                const int p = gz[i];
+                return smem_z(prec, plz[p]->dev, B, std::max(pa[p].z.nin, pa[p].z.nout));
+            },
+            MAX_LINES, cap[2], start[2], Bgz, ex[2].nt, ex[2].smem);
+        for (size_t i = 0; i < gx.size(); ++i) Bx[gx[i]] = Bgx[i];
+        for (size_t i = 0; i < gy.size(); ++i) By[gy[i]] = Bgy[i];
+        for (size_t i = 0; i < gz.size(); ++i) Bz[gz[i]] = Bgz[i];
         ex[3].nt = ex[1].nt;
         ex[3].smem = ex[1].smem;
         ex[4].nt = ex[0].nt;
@@ -265,24 +315,30 @@ struct Batch {
             axi[p].B = Bx[p];
 
             const long long lines = ((long long)s.n[1] * s.n[2] + 1) / 2;
-            const int gx = (int)((lines + Bx[p] - 1) / Bx[p]);
-            for (int c = 0; c < ax[p].ncomp; ++c)
-                for (int b = 0; b < gx; ++b) t0.push_back({p, b, c, 0});
-            const int gy = (s.Mx + By[p] - 1) / By[p];
-            for (int c = 0; c < ay[p].ncomp; ++c)
-                for (int z = 0; z < s.n[2]; ++z)
-                    for (int b = 0; b < gy; ++b) t1.push_back({p, b, z, c});
-            const int gz = (s.Mx + Bz[p] - 1) / Bz[p];
-            for (int ky = 0; ky < s.P[1]; ++ky)
-                for (int b = 0; b < gz; ++b) t2.push_back({p, b, ky, 0});
-            if (write_masks[p]) {
-                for (int c = 0; c < ayi[p].ncomp; ++c)
+            const int nbx = (int)((lines + Bx[p] - 1) / Bx[p]);
+            if (batched(p, 0))
+                for (int c = 0; c < ax[p].ncomp; ++c)
+                    for (int b = 0; b < nbx; ++b) t0.push_back({p, b, c, 0});
+            const int nby = (s.Mx + By[p] - 1) / By[p];
+            if (batched(p, 1))
+                for (int c = 0; c < ay[p].ncomp; ++c)
                     for (int z = 0; z < s.n[2]; ++z)
-                        for (int b = 0; b < gy; ++b) t3.push_back({p, b, z, c});
-                for (int c = 0; c < axi[p].ncomp; ++c)
-                    for (int b = 0; b < gx; ++b) t4.push_back({p, b, c, 0});
+                        for (int b = 0; b < nby; ++b) t1.push_back({p, b, z, c});
+            const int nbz = (s.Mx + Bz[p] - 1) / Bz[p];
+            if (batched(p, 2))
+                for (int ky = 0; ky < s.P[1]; ++ky)
+                    for (int b = 0; b < nbz; ++b) t2.push_back({p, b, ky, 0});
+            if (write_masks[p]) {
+                if (batched(p, 3))
+                    for (int c = 0; c < ayi[p].ncomp; ++c)
+                        for (int z = 0; z < s.n[2]; ++z)
+                            for (int b = 0; b < nby; ++b) t3.push_back({p, b, z, c});
+                if (batched(p, 4))
+                    for (int c = 0; c < axi[p].ncomp; ++c)
+                        for (int b = 0; b < nbx; ++b) t4.push_back({p, b, c, 0});
             }
         }
+        own_args = pa;
         PS_BCK(cudaStreamSynchronize(stream));  // kernel builds done before the arguments change hands
         upload(ex[0], ax, t0);
         upload(ex[1], ay, t1);
@@ -575,7 +631,7 @@ int ps_batch_get_info(const ps_batch *h, int what, double *value)
     if (!h || !h->b || !value) return PS_ERR_ARGUMENT;
     const ps::Batch &b = *h->b;
     switch (what) {
-    case PS_BATCH_INFO_LAUNCHES_PER_SOLVE: *value = 5; break;
+    case PS_BATCH_INFO_LAUNCHES_PER_SOLVE: *value = (double)b.launches_per_solve(); break;
     case PS_BATCH_INFO_TILES_PER_SOLVE: *value = (double)b.tiles_per_solve(); break;
     case PS_BATCH_INFO_POINTS: {
         double pts = 0;

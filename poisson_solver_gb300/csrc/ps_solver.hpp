@@ -192,6 +192,21 @@ struct Solver {
     // transform plan it runs with.
     PassChoice current_choice(int pass, int in_mask);
     const FftPlanDev &current_plan(int pass, int in_mask);
+    // For the batched solve: the choice for prepared pass arguments, and one
+    // pass launched on another stream (the batch's capture stream).
+    PassChoice pass_choice(int pass, const PassArgs &pa) { return choice(pass, pa); }
+    void launch_on(int pass, const PassChoice &c, PassArgs &pa, cudaStream_t st)
+    {
+        cudaStream_t saved = stream;
+        stream = st;
+        try {
+            launch_pass(pass, c, pa);
+        } catch (...) {
+            stream = saved;
+            throw;
+        }
+        stream = saved;
+    }
 
     size_t device_bytes() const;
     void copy_kernel(double *host, long long capacity) const;

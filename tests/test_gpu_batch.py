@@ -235,3 +235,41 @@ def test_autotuned_batch_gives_the_same_results(native, precision):
         ref, _ = native.solve(nc, bc, _dx(nc), data[i], (0, 2, 6)[i % 3], precision=precision, **opts)
         got = _pull(b, i)
         assert rel_l2(got, ref) < tol
+
+
+# FP32 problems whose padded lengths the compiled families cover run their
+# passes with those kernels (routed), beside the batched run-time launch
+ROUTED = [
+    ((128, 128, 128), (0, 0, 0), (0, 1, 2), dict(curl=True)),  # padded 256^3: the bulk-copy kernels
+    ((64, 64, 64), (1, 1, 1), (0,), dict(grad=True)),          # 64^3 periodic: the length-specialised kernels
+    ((32, 64, 32), (0, 0, 1), (0, 1, 2), dict()),              # 64 x 128 x 32: specialised x, y; run-time z
+    ((17, 12, 10), (0, 0, 0), (0, 1, 2), dict(curl=True)),     # Bluestein lengths: the batched launch
+]
+
+
+def test_fp32_batch_routes_power_of_two_problems(native, oracle):
+    from poisson_solver_gb300 import _lib as L
+    b = native.PoissonBatch("fp32")
+    for rnd in range(2):  # a second solve with new data goes through a rebuilt graph
+        data = []
+        for i, (nc, bc, comps, opts) in enumerate(ROUTED):
+            if rnd == 0:
+                assert b.add(nc, bc, _dx(nc), 2) == i
+                for k, v in opts.items():
+                    getattr(b, f"set_return_{k}")(i, v)
+            B = _fields(nc, comps, 900 + 10 * rnd + i, zero_mean=bc == (1, 1, 1))
+            b.push(i, *B)
+            data.append(B)
+        b.solve()
+        assert b.info(L.PS_BATCH_INFO_LAUNCHES_PER_SOLVE) > 5  # routed launches beside the batched ones
+        for i, (nc, bc, comps, opts) in enumerate(ROUTED):
+            shape = (nc[2], nc[1], nc[0])
+            A = [np.full(shape, np.nan) for _ in range(3)]
+            b.pull(i, *A)
+            single, _ = native.solve(nc, bc, _dx(nc), data[i], 2, precision="fp32", **opts)
+            ref, _ = oracle.solve3d(nc, bc, _dx(nc), data[i], 2, **opts)
+            for a, s in zip(A, single):
+                if s is not None:
+                    assert np.array_equal(a, s), f"problem {i}: batched and single solves differ"
+            assert rel_l2([a for a, s in zip(A, single) if s is not None], [r for r in ref if r is not None]) < FP32_TOL
+    b.close()
