@@ -361,9 +361,21 @@ struct Batch {
         }
         PS_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
         cudaError_t e = cudaSuccess;
-        for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = launch(k, cs);
+        std::string thrown;  // a routed launch's error: the capture still ends before it is reported
+        int thrown_status = PS_OK;
+        try {
+            for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = launch(k, cs);
+        } catch (const Error &err) {
+            thrown = err.what();
+            thrown_status = err.status;
+        }
         cudaGraph_t g = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+        if (!thrown.empty()) {
+            if (own) cudaStreamDestroy(cs);
+            if (g) cudaGraphDestroy(g);
+            throw Error(thrown_status, thrown);
+        }
         if (own) cudaStreamDestroy(cs);
         if (e != cudaSuccess || ec != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
