@@ -80,7 +80,11 @@ int main(int argc, char** argv) {
   poisson.push(B[0], B[1], B[2]);
   poisson.solve3d();
   poisson.pull(A[0], A[1], A[2], B[0], B[1], B[2]);
-  // the extensions: kernel family, interleaved ghost-offset arrays, smoothing
+  // the extensions: double-float transforms, kernel family, interleaved
+  // ghost-offset arrays, smoothing
+  poisson.set_precision(PS_PREC_DF64);
+  poisson.solve3d();
+  poisson.pull(A[0], A[1], A[2], nullptr, nullptr, nullptr);
   int ext[3] = {20, 18, 16}, off[3] = {2, 1, 0};
   double *I = new double[3 * 20 * 18 * 16]();
   poisson.set_kernel(PS_KERNEL_GAUSSIAN);
