@@ -431,8 +431,9 @@ namespace rt {
 
 template <typename K> inline cudaError_t prep(K kernel, size_t smem)
 {
-    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return cudaSuccess;
+    // Always: the 48 KB a launch gets without it includes the kernel's static
+    // shared memory, so a request just under 48 KB can already be too large.
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 template <typename T> inline cudaError_t xfwd(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)

@@ -364,8 +364,9 @@ __global__ void __launch_bounds__(BL *(L / EM)) k_xinv(const XInvArgs a)
 
 template <typename K> cudaError_t prep(K kernel, size_t smem)
 {
-    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return cudaSuccess;
+    // Always: the 48 KB a launch gets without it includes the kernel's static
+    // shared memory, so a request just under 48 KB can already be too large.
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 template <int L, int EM> constexpr size_t ntw() { return Plan<L, EM>::NTW; }

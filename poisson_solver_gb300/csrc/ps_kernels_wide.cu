@@ -344,8 +344,9 @@ __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
 // ---------------------------------------------------------------------------
 template <typename K> cudaError_t prep(K kernel, size_t smem)
 {
-    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return cudaSuccess;
+    // Always: the 48 KB a launch gets without it includes the kernel's static
+    // shared memory, so a request just under 48 KB can already be too large.
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 #define PS_WIDE_LENGTHS(X) X(256) X(512) X(1024) X(2048)

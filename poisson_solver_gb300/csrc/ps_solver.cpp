@@ -1255,7 +1255,13 @@ void Solver::autotune(int in_mask)
             float best_ms = 0.f;
             for (const PassChoice &c : cands) {
                 PassArgs run = pa;
-                launch_pass(pass, c, run);  // warm-up (and the one-time attribute setup)
+                try {
+                    launch_pass(pass, c, run);  // warm-up (and the one-time attribute setup)
+                } catch (const Error &err) {
+                    throw Error(err.status, std::string(err.what()) + " (tuning pass " + std::to_string(pass) +
+                                                ", family " + c.fam + ", " + std::to_string(c.B) + " lines, plan variant " +
+                                                std::to_string(c.pv) + ")");
+                }
                 PS_CK(cudaEventRecord(e0, stream));
                 const int reps = 3;
                 for (int r = 0; r < reps; ++r) launch_pass(pass, c, run);

@@ -153,3 +153,29 @@ def test_linearity_and_fp32_at_256(native):
     assert rel_l2(A3, [a * x + y for x, y in zip(A1, A2)]) < 1e-13
     A1f, _ = native.solve(nc, (0, 0, 0), (dx,) * 3, B1, 6, curl=True, precision="fp32")
     assert rel_l2(A1f, A1) < 1e-6
+
+
+def test_fp64_y_pass_just_under_48kb_in_a_fresh_process(oracle):
+    """A y transform of 1024 points in FP64 at 2 lines a CTA asks for 49 136
+    bytes of dynamic shared memory: under 48 KB, but over it with the
+    kernel's static shared memory, so the launch must raise the kernel's
+    limit itself (in a fresh process nothing else has raised it)."""
+    import os
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+    nc, bc = (6, 512, 4), (0, 0, 0)
+    code = ("import numpy as np, poisson_solver_gb300 as ps; "
+            f"rng = np.random.default_rng(3); B = rng.standard_normal(({nc[2]}, {nc[1]}, {nc[0]})); "
+            f"A, _ = ps.solve({nc}, {bc}, (0.1, 0.01, 0.1), [B, None, None], 2, precision='fp64'); "
+            "np.save('out.npy', A[0])")
+    env = dict(os.environ, PS_LINES_Y="2", PS_TUNE_CACHE="", PYTHONPATH=ROOT)
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([sys.executable, "-c", code], env=env, cwd=d, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        got = np.load(os.path.join(d, "out.npy"))
+    B = np.random.default_rng(3).standard_normal((nc[2], nc[1], nc[0]))
+    ref, _ = oracle.solve3d(nc, bc, (0.1, 0.01, 0.1), [B, None, None], 2)
+    assert rel_l2([got], [ref[0]]) < 1e-12
