@@ -45,7 +45,7 @@ __device__ __forceinline__ long long spec_row(long long r, long long rows, int r
 }
 
 template <int L, bool HALF>
-__global__ void __launch_bounds__(XQ_THREADS, 3) k_xfq(const XFwdArgs a)
+__global__ void __launch_bounds__(XQ_THREADS, 2) k_xfq(const XFwdArgs a)
 {
     using C = float2;
     using PL = WP<L>;
