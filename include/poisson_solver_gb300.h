@@ -234,11 +234,15 @@ int ps_get_pass_config(ps_solver *h, int pass, int component_mask, int *family, 
  * length transformed by Bluestein's algorithm, the convolution length the
  * stages run on (*conv_length; 0 otherwise). With FP32 transforms the
  * run-time kernels have plan variants that ps_autotune times beside the
- * families and lines: the power-of-two part in radix 16 or radix 8, and
+ * families and lines: the power-of-two part in radix 16 or radix 8,
  * Bluestein's convolution length as the least power of two or the least
- * 2^a 3^b 5^c >= 2 L - 1. PS_PLAN_X/_Y/_Z (bit 0: radix 8, bit 1: smooth
- * length) set them for the run-time family and bypass tuned choices. FP64
- * transforms always take the default plan. No reference counterpart. */
+ * 2^a 3^b 5^c >= 2 L - 1, and, for a length whose largest prime p divides it
+ * once with p - 1 and the cofactor free of primes above 13, Rader's algorithm
+ * in place of Bluestein's: the first stage has radix p and runs each p-point
+ * DFT as a cyclic convolution of p - 1 points (then *conv_length is p - 1).
+ * PS_PLAN_X/_Y/_Z (bit 0: radix 8, bit 1: smooth length, bit 2: Rader) set
+ * them for the run-time family and bypass tuned choices. FP64 transforms
+ * always take the default plan. No reference counterpart. */
 int ps_get_pass_plan(ps_solver *h, int pass, int component_mask, int *radices, int capacity, int *nstages,
                      int *conv_length);
 
@@ -291,9 +295,14 @@ int ps_batch_solve(ps_batch *b);
  * are overwritten. Later solves, and rebuilds after adds, options or pushes,
  * use the tuned settings. ps_batch_get_tuning reports them for axis 0..2
  * (x, y, z): the CTA thread bound, the starting lines and the plan variant
- * (bit 0: radix 8, bit 1: smooth Bluestein length). */
+ * (bit 0: radix 8, bit 1: smooth Bluestein length, bit 2: Rader's algorithm;
+ * see ps_get_pass_plan). ps_batch_set_tuning sets them (a thread bound that
+ * is a multiple of 32 up to 256, starting lines a power of two up to 64, a
+ * variant 0..7; bits a length does not use are ignored), for instance to
+ * reuse settings tuned earlier; the next solve rebuilds the batch. */
 int ps_batch_autotune(ps_batch *b);
 int ps_batch_get_tuning(const ps_batch *b, int axis, int *max_threads, int *start_lines, int *plan_variant);
+int ps_batch_set_tuning(ps_batch *b, int axis, int max_threads, int start_lines, int plan_variant);
 int ps_batch_pull(ps_batch *b, int index, double *ax, double *ay, double *az);
 int ps_batch_pull_device(ps_batch *b, int index, double *ax, double *ay, double *az);
 int ps_batch_set_stream(ps_batch *b, void *stream);

@@ -100,6 +100,7 @@ SIGNATURES = {
     "ps_batch_solve": (_i, [_vp]),
     "ps_batch_autotune": (_i, [_vp]),
     "ps_batch_get_tuning": (_i, [_vp, _i, _ip, _ip, _ip]),
+    "ps_batch_set_tuning": (_i, [_vp, _i, _i, _i, _i]),
     "ps_batch_pull": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_pull_device": (_i, [_vp, _i, _dp, _dp, _dp]),
     "ps_batch_set_stream": (_i, [_vp, _vp]),

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libps_gb300.so")
-SOURCES = ["ps_kernels.cu", "ps_kernels_df.cu", "ps_kernels_p2.cu", "ps_kernels_wide.cu", "ps_kernels_ztm.cu", "ps_kernels_zq.cu", "ps_kernels_yq.cu", "ps_kernels_xq.cu", "ps_kernels_ztc.cu", "ps_greens.cu", "ps_fields.cu", "ps_solver.cpp", "ps_api.cpp", "ps_batch.cpp", "ps_noalloc.cu"]
+SOURCES = ["ps_kernels.cu", "ps_kernels_df.cu", "ps_kernels_rader.cu", "ps_kernels_p2.cu", "ps_kernels_wide.cu", "ps_kernels_ztm.cu", "ps_kernels_zq.cu", "ps_kernels_yq.cu", "ps_kernels_xq.cu", "ps_kernels_ztc.cu", "ps_greens.cu", "ps_fields.cu", "ps_solver.cpp", "ps_api.cpp", "ps_batch.cpp", "ps_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

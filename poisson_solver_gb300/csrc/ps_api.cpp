@@ -262,7 +262,7 @@ int ps_get_pass_plan(ps_solver *h, int pass, int component_mask, int *radices, i
         const ps::FftPlanDev &d = s.current_plan(pass, component_mask);
         *nstages = d.nstages;
         for (int i = 0; i < d.nstages && i < capacity; ++i) radices[i] = d.radix[i];
-        *conv_length = d.blue ? d.L : 0;
+        *conv_length = d.blue ? d.L : d.rader ? d.rq : 0;
     });
 }
 

@@ -41,6 +41,7 @@ struct Batch {
         DevBuf args, tiles;
         int ntiles = 0, nt = 0;
         size_t smem = 0;
+        bool rader = false;  // a problem of the launch has a Rader plan
     };
     PassExec ex[5];
     // Launch shape of the x (passes 0 and 4), y (1 and 3) and z (2)
@@ -166,6 +167,8 @@ struct Batch {
     template <typename Args> static void upload(PassExec &e, const std::vector<Args> &args, const std::vector<BatchTile> &tiles)
     {
         e.ntiles = (int)tiles.size();
+        e.rader = false;
+        for (const BatchTile &t : tiles) e.rader = e.rader || args[t.p].plan.rader;
         if (args.empty() || tiles.empty()) return;
         e.args.ensure(args.size() * sizeof(Args));
         e.tiles.ensure(tiles.size() * sizeof(BatchTile));
@@ -183,19 +186,20 @@ struct Batch {
         switch (k) {
         case 0:
             r = launch_xfwd_batch(prec, (const XFwdArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
-                                  e.smem, st);
+                                  e.smem, e.rader, st);
             break;
         case 1:
         case 3:
             r = launch_col_batch(prec, k == 3, (const ColArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
-                                 e.smem, st);
+                                 e.smem, e.rader, st);
             break;
         case 2:
-            r = launch_z_batch(prec, (const ZArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt, e.smem, st);
+            r = launch_z_batch(prec, (const ZArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt, e.smem,
+                               e.rader, st);
             break;
         default:
             r = launch_xinv_batch(prec, (const XInvArgs *)e.args.p, (const BatchTile *)e.tiles.p, e.ntiles, e.nt,
-                                  e.smem, st);
+                                  e.smem, e.rader, st);
         }
         if (r != cudaSuccess) return r;
         try {
@@ -431,9 +435,9 @@ struct Batch {
                 float best_ms = -1.f;
                 if (precision == PREC_FP32) {
                     // z bodies hold 8 elements a thread: no radix-cap variant
-                    const int vmask = ax == 2 ? PV_SMOOTH_M : (PV_HALF_RADIX | PV_SMOOTH_M);
+                    const int vmask = ax == 2 ? (PV_SMOOTH_M | PV_RADER) : (PV_HALF_RADIX | PV_SMOOTH_M | PV_RADER);
                     int best_pv = pv[ax];
-                    for (int v = 0; v <= 3; ++v) {
+                    for (int v = 0; v <= 7; ++v) {
                         if ((v & ~vmask) != 0) continue;
                         pv[ax] = v;
                         const float ms = time_axis();
@@ -609,6 +613,20 @@ int ps_batch_get_tuning(const ps_batch *h, int axis, int *max_threads, int *star
     *max_threads = b.cap[axis];
     *start_lines = b.start[axis];
     *plan_variant = b.pv[axis];
+    return PS_OK;
+}
+
+int ps_batch_set_tuning(ps_batch *h, int axis, int max_threads, int start_lines, int plan_variant)
+{
+    if (!h || !h->b || axis < 0 || axis > 2) return PS_ERR_ARGUMENT;
+    if (max_threads < 32 || max_threads > ps::BATCH_MAX_THREADS || max_threads % 32 != 0) return PS_ERR_ARGUMENT;
+    if (start_lines < 1 || start_lines > 64 || (start_lines & (start_lines - 1)) != 0) return PS_ERR_ARGUMENT;
+    if (plan_variant < 0 || plan_variant > 7) return PS_ERR_ARGUMENT;
+    ps::Batch &b = *h->b;
+    b.cap[axis] = max_threads;
+    b.start[axis] = start_lines;
+    b.pv[axis] = plan_variant;
+    b.dirty = true;  // the next solve rebuilds and recaptures
     return PS_OK;
 }
 

@@ -370,9 +370,8 @@ __device__ __forceinline__ void split_index(int bf, int m, int lm, int &j, int &
 }
 
 // One in-place Stockham stage with a compile-time radix.
-template <int EM, int R, bool INV, typename C>
-__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws, int4 sd,
-                                      int lm)
+template <int EM, int R, bool INV, typename C, typename PL>
+__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const PL &P, const C *tws, int4 sd, int lm)
 {
     constexpr int U = EM / R;
     const int L = P.L, m = sd.y, nbf = L / R, tpl = P.tpl;
@@ -422,8 +421,8 @@ __device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const 
 // tpl threads however few butterflies it has (a length-194 line has 2).
 // Twiddles are applied to the inputs in place first; each output then sums
 // R twiddled inputs in the order r = 0 .. R-1.
-template <bool INV, typename C>
-__device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws, int4 sd)
+template <bool INV, typename C, typename PL>
+__device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const PL &P, const C *tws, int4 sd)
 {
     const int L = P.L, R = sd.x, m = sd.y, nbf = L / R, tpl = P.tpl;
     const C *tw = tws + sd.z;
@@ -458,9 +457,11 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
     __syncthreads();
 }
 
-// Full transform of the CTA's lines, for ncomp line sets cstride elements
-// apart. EM is the register elements a thread holds per stage (and the
-// largest radix); the plan's threads-per-line was computed for the same EM.
+// Stages s .. ns-1 of the stage table over lines of P.L elements with P.tpl
+// threads a line (P the plan for its own stages, a LineGeom for the
+// sub-transforms of a Rader plan), for ncomp line sets cstride elements apart. EM is the register
+// elements a thread holds per stage (and the largest radix); the plan's
+// threads-per-line was computed for the same EM.
 // Thread t of a line takes butterflies t, t + tpl, ...: a caller passes t = L
 // for a thread that must only join the barriers (every butterfly index it
 // would take is then past the stage's count).
@@ -473,12 +474,10 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const Ff
 // Radices without an unrolled butterfly: primes above 7 (11 and 13 included).
 __device__ __forceinline__ bool is_generic_radix(int R) { return R > 8 && R != 16; }
 
-template <bool INV, int EM, typename C>
-__device__ __forceinline__ void fft_stages(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+template <bool INV, int EM, typename C, typename PL>
+__device__ __forceinline__ void run_stages(C *S, C *W, int sn, int sb, int b, int t, const PL &P, int s, int ns,
                                            const C *tws, const StageInfo &si, int ncomp, int cstride)
 {
-    const int ns = P.nstages;
-    int s = 0;
     for (; s < ns && is_generic_radix(si.st[s].x); ++s)
         for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, tws, si.st[s]);
     for (; s < ns && si.st[s].x == 7; ++s)
@@ -500,6 +499,13 @@ __device__ __forceinline__ void fft_stages(C *S, C *W, int sn, int sb, int b, in
         for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
         ++s;
     }
+}
+
+template <bool INV, int EM, typename C>
+__device__ __forceinline__ void fft_stages(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+                                           const C *tws, const StageInfo &si, int ncomp, int cstride)
+{
+    run_stages<INV, EM>(S, W, sn, sb, b, t, P, 0, P.nstages, tws, si, ncomp, cstride);
 }
 
 // Line-thread index of a thread that must only join the barriers: past every
@@ -548,12 +554,136 @@ __device__ __forceinline__ void bluestein_lines(C *S, C *W, int sn, int sb, int 
     __syncthreads();
 }
 
+// The line geometry the stage functions read (a plan's, or a Rader plan's
+// sub-transforms').
+struct LineGeom {
+    int L, tpl;
+};
+
+// What a Rader stage reads of its plan, gathered once.
+template <typename C> struct RaderGeom {
+    int L, tpl, ns;            // line length, threads a line, stages of the plan
+    int q1, rtpl, rs0, rns;    // sub-transform length p - 1, its threads, its stages
+    float ip, iq;              // 1 / p and 1 / (p - 1)
+    const int *itab;           // g^-j mod p (j < p - 1), then log_g k at k - 1
+    const C *bh;               // FFT(beta) / (p - 1): forward, then inverse
+};
+
+template <typename C> __device__ __forceinline__ RaderGeom<C> rader_geom(const FftPlanDev &P)
+{
+    return RaderGeom<C>{P.L, P.tpl, P.nstages, P.rq, P.rtpl, P.rs0, P.rns, P.rinv_p, P.rinv_q, P.itab,
+                        reinterpret_cast<const C *>(P.table) + P.rbh};
+}
+
+// The sub-transforms of a Rader stage: the L / p sub-lines of p - 1 points of
+// every line set at once, sub-line bf on line threads [bf rtpl, (bf + 1) rtpl)
+// (the plan's threads a line cover them all). No loop over sub-lines: with
+// the stages inside one, ptxas spilled.
 template <bool INV, int EM, typename C>
+__device__ __forceinline__ void rader_sub(C *S, C *W, int sn, int sb, int b, int t, const RaderGeom<C> &g,
+                                          const C *tws, const StageInfo &si, int ncomp, int cstride)
+{
+    const int q1 = g.q1, nbf = g.L / (q1 + 1), tps = g.rtpl;
+    const int bf = t < g.tpl ? t / tps : nbf;
+    const bool on = bf < nbf;
+    const int off = on ? bf * q1 * sn : 0;
+    run_stages<INV, EM>(S + off, W + off, sn, sb, b, on ? t - bf * tps : IDLE_T, LineGeom{q1, tps}, g.rs0,
+                        g.rs0 + g.rns, tws, si, ncomp, cstride);
+}
+
+// Rader's algorithm for stage 0 of a Rader plan, then the plan's other
+// stages. Stage 0 has a prime radix p and m = 1: butterfly bf < nbf = L / p
+// is the p-point DFT of x[bf + r nbf], written to y[bf p + k]. With g a
+// primitive root mod p, a[j] = x[bf + g^-j nbf] (j < p - 1) and
+// beta[m] = w^(g^m), w = e^{-+2 pi i / p}:
+//   y[bf p + g^q] = x[bf] + (a (*) beta)[q],  y[bf p] = x[bf] + sum_j a[j],
+// a cyclic convolution of p - 1 points, computed as the sub-transform of a,
+// times the precomputed spectrum FFT(beta) / (p - 1), and the unnormalised
+// inverse sub-transform. In each line the sub-line of butterfly bf takes
+// elements [bf (p - 1), (bf + 1)(p - 1)) and x[bf] the spare element
+// nbf (p - 1) + bf; sum_j a[j] (the sub-transform's DC term) is kept in a
+// register by line thread bf (nbf <= tpl, since tpl EM >= L). The scratch
+// line W (one for all line sets) stages the gather and the outputs, and is
+// the scratch of direct-DFT sub-stages (radix 11 or 13) in between.
+// Index division by p and p - 1 runs in FP32: (e + 1/2) / q lies at least
+// 1 / (2 q) from an integer, far above the rounding error for any line length.
+template <bool INV, int EM, typename C>
+__device__ __forceinline__ void rader_lines(C *S, C *W, int sn, int sb, int b, int t, const RaderGeom<C> &g,
+                                            const C *tws, const StageInfo &si, int ncomp, int cstride)
+{
+    const int L = g.L, tpl = g.tpl, q1 = g.q1, p = q1 + 1, nbf = L / p, nq = nbf * q1;
+    const int *perm = g.itab, *qlog = g.itab + q1;
+    const C *bh = g.bh + (INV ? q1 : 0);
+    C *Wb = W + b * sb;
+    // gather: sub-line entries a[j] and x[bf] at the spare elements
+    for (int c = 0; c < ncomp; ++c) {
+        C *Sb = S + c * cstride + b * sb;
+        for (int e = t; e < L; e += tpl) Wb[e * sn] = Sb[e * sn];
+        __syncthreads();
+        for (int e = t; e < L; e += tpl) {
+            int src = e - nq;
+            if (e < nq) {
+                const int bf = (int)(((float)e + 0.5f) * g.iq), j = e - bf * q1;
+                src = bf + __ldg(&perm[j]) * nbf;
+            }
+            Sb[e * sn] = Wb[src * sn];
+        }
+        __syncthreads();
+    }
+    rader_sub<false, EM>(S, W, sn, sb, b, t, g, tws, si, ncomp, cstride);
+    // keep the DC terms, then multiply by the convolution spectrum
+    C a0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        a0[c] = C{0, 0};
+        if (c < ncomp && t < nbf) a0[c] = S[c * cstride + b * sb + t * q1 * sn];
+    }
+    __syncthreads();
+    for (int c = 0; c < ncomp; ++c) {
+        C *Sb = S + c * cstride + b * sb;
+        for (int e = t; e < nq; e += tpl) {
+            const int bf = (int)(((float)e + 0.5f) * g.iq), j = e - bf * q1;
+            Sb[e * sn] = cmul(Sb[e * sn], bh[j]);
+        }
+    }
+    __syncthreads();
+    rader_sub<true, EM>(S, W, sn, sb, b, t, g, tws, si, ncomp, cstride);
+    // outputs into W (k > 0 from the convolution, k = 0 by line thread bf), then back
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (c >= ncomp) break;  // ncomp is the same on every thread
+        C *Sb = S + c * cstride + b * sb;
+        for (int e = t; e < L; e += tpl) {
+            const int bf = (int)(((float)e + 0.5f) * g.ip), k = e - bf * p;
+            if (k > 0) Wb[e * sn] = cadd(Sb[(nq + bf) * sn], Sb[(bf * q1 + __ldg(&qlog[k - 1])) * sn]);
+        }
+        if (t < nbf) Wb[t * p * sn] = cadd(Sb[(nq + t) * sn], a0[c]);
+        __syncthreads();
+        for (int e = t; e < L; e += tpl) Sb[e * sn] = Wb[e * sn];
+        __syncthreads();
+    }
+    run_stages<INV, EM>(S, W, sn, sb, b, t, LineGeom{L, tpl}, 1, g.ns, tws, si, ncomp, cstride);
+}
+
+// The transform of a plan. RAD: the kernel runs Rader plans too (separate
+// instantiations, so that the registers of the Rader path do not count
+// against the kernels of the other plans).
+template <bool INV, int EM, bool RAD = false, typename C>
 __device__ __forceinline__ void fft_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P, const C *tws,
                                           const StageInfo &si, int ncomp = 1, int cstride = 0)
 {
-    if (P.blue) bluestein_lines<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
-    else fft_stages<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    if (P.blue) {
+        bluestein_lines<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+        return;
+    }
+    if constexpr (RAD) {
+        if (P.rader) {
+            const RaderGeom<C> g = rader_geom<C>(P);
+            rader_lines<INV, EM>(S, W, sn, sb, b, t, g, tws, si, ncomp, cstride);
+            return;
+        }
+    }
+    fft_stages<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
 }
 
 // Component c of a three-entry parameter array, read with constant indices.

@@ -84,38 +84,38 @@ cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st)
 }
 
 cudaError_t launch_xfwd_batch(int prec, const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                              cudaStream_t st)
+                              bool rader, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (prec == PREC_FP64) return rt::xfwd_batch<double>(args, tiles, ntiles, nt, smem, st);
-    if (prec == PREC_FP32) return rt::xfwd_batch<float>(args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP64) return rt::xfwd_batch<double>(args, tiles, ntiles, nt, smem, rader, st);
+    if (prec == PREC_FP32) return rt::xfwd_batch<float>(args, tiles, ntiles, nt, smem, rader, st);
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_col_batch(int prec, int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt,
-                             size_t smem, cudaStream_t st)
+                             size_t smem, bool rader, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (prec == PREC_FP64) return rt::col_batch<double>(inverse, args, tiles, ntiles, nt, smem, st);
-    if (prec == PREC_FP32) return rt::col_batch<float>(inverse, args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP64) return rt::col_batch<double>(inverse, args, tiles, ntiles, nt, smem, rader, st);
+    if (prec == PREC_FP32) return rt::col_batch<float>(inverse, args, tiles, ntiles, nt, smem, rader, st);
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_z_batch(int prec, const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                           cudaStream_t st)
+                           bool rader, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (prec == PREC_FP64) return rt::z_batch<double>(args, tiles, ntiles, nt, smem, st);
-    if (prec == PREC_FP32) return rt::z_batch<float>(args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP64) return rt::z_batch<double>(args, tiles, ntiles, nt, smem, rader, st);
+    if (prec == PREC_FP32) return rt::z_batch<float>(args, tiles, ntiles, nt, smem, rader, st);
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_xinv_batch(int prec, const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                              cudaStream_t st)
+                              bool rader, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (prec == PREC_FP64) return rt::xinv_batch<double>(args, tiles, ntiles, nt, smem, st);
-    if (prec == PREC_FP32) return rt::xinv_batch<float>(args, tiles, ntiles, nt, smem, st);
+    if (prec == PREC_FP64) return rt::xinv_batch<double>(args, tiles, ntiles, nt, smem, rader, st);
+    if (prec == PREC_FP32) return rt::xinv_batch<float>(args, tiles, ntiles, nt, smem, rader, st);
     return cudaErrorInvalidValue;
 }
 

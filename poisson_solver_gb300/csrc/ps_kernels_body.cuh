@@ -10,6 +10,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "ps_fft.cuh"
 #include "ps_types.hpp"
 
@@ -38,7 +40,7 @@ template <typename T> constexpr int EMZ = e_max_z(sizeof(T) == 8 ? PREC_FP64 : P
 // have more threads than the problem of its tile uses). Threads tid >= nt only
 // join the barriers: their line-thread index is set to L, past every
 // butterfly, and the load/store loops skip them.
-template <typename T>
+template <typename T, bool RAD = false>
 __device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, int nt)
 {
     using C = typename Cplx<T>::type;
@@ -88,7 +90,7 @@ __device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, i
         }
     }
     __syncthreads();
-    fft_lines<false, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
+    fft_lines<false, EMX<T>, RAD>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
 
     // separate the two half spectra and store
     const int Mx = a.Mx;
@@ -104,15 +106,15 @@ __device__ __forceinline__ void xfwd_body(const XFwdArgs &a, int bx, int comp, i
     }
 }
 
-template <typename T> __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
+template <typename T, bool RAD = false> __global__ void __launch_bounds__(MAX_THREADS) k_xfwd(const XFwdArgs a)
 {
-    xfwd_body<T>(a, blockIdx.x, blockIdx.y, blockDim.x);
+    xfwd_body<T, RAD>(a, blockIdx.x, blockIdx.y, blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
 // Column transforms along a strided axis, in place: the CTA takes B adjacent
 // columns (one 128-byte row segment per sample for the default B) of one slab.
-template <typename T, bool INV>
+template <typename T, bool INV, bool RAD = false>
 __device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int comp, int nt)
 {
     using C = typename Cplx<T>::type;
@@ -144,7 +146,7 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int
         }
     }
     __syncthreads();
-    fft_lines<INV, EMX<T>>(S, W, B, 1, b, t, plan, tws, si);
+    fft_lines<INV, EMX<T>, RAD>(S, W, B, 1, b, t, plan, tws, si);
     if (b < nb) {
         C *dst = base + (long long)t * a.axis_stride + b;
 #pragma unroll 4
@@ -152,9 +154,9 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int bx, int slab, int
     }
 }
 
-template <typename T, bool INV> __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
+template <typename T, bool INV, bool RAD = false> __global__ void __launch_bounds__(MAX_THREADS) k_col(const ColArgs a)
 {
-    col_body<T, INV>(a, blockIdx.x, blockIdx.y, blockIdx.z, blockDim.x);
+    col_body<T, INV, RAD>(a, blockIdx.x, blockIdx.y, blockIdx.z, blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -172,7 +174,7 @@ __device__ __forceinline__ T wavenumber(int k, int P, T c, bool derivative)
 
 // OPT: the spectral operation, or -1 to take it from a.op at run time (the
 // batched pass); a fixed OPT folds every test on op away.
-template <typename T, int OPT>
+template <typename T, int OPT, bool RAD = false>
 __device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
 {
     const int op = OPT >= 0 ? OPT : a.op;
@@ -208,7 +210,7 @@ __device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
         }
     }
     __syncthreads();
-    fft_lines<false, EMZ<T>>(S, W, B, 1, b, t, plan, tws, si, a.nin, LB);
+    fft_lines<false, EMZ<T>, RAD>(S, W, B, 1, b, t, plan, tws, si, a.nin, LB);
 
     if (op != OP_FORWARD) {
         // the thread's column kx is fixed; it walks kz = t, t + nt/B, ...
@@ -275,7 +277,7 @@ __device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
             }
         }
         __syncthreads();
-        fft_lines<true, EMZ<T>>(S, W, B, 1, b, t, plan, tws, si, a.nout, LB);
+        fft_lines<true, EMZ<T>, RAD>(S, W, B, 1, b, t, plan, tws, si, a.nout, LB);
     }
 
     if (b < nb) {
@@ -290,16 +292,16 @@ __device__ __forceinline__ void z_body(const ZArgs &a, int bx, int by, int nt)
     }
 }
 
-template <typename T, int OP> __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
+template <typename T, int OP, bool RAD = false> __global__ void __launch_bounds__(MAX_THREADS) k_z(const ZArgs a)
 {
-    z_body<T, OP>(a, blockIdx.x, blockIdx.y, blockDim.x);
+    z_body<T, OP, RAD>(a, blockIdx.x, blockIdx.y, blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
 // x inverse. Line l rebuilds Z = Xa + i Xb over the full length from the two
 // half spectra (Z[L-k] = conj Xa[k] + i conj Xb[k]), transforms back and
 // writes Re -> row 2l, Im -> row 2l+1, first n_out samples only.
-template <typename T>
+template <typename T, bool RAD = false>
 __device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, int nt)
 {
     using C = typename Cplx<T>::type;
@@ -332,7 +334,7 @@ __device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, i
         }
     }
     __syncthreads();
-    fft_lines<true, EMX<T>>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
+    fft_lines<true, EMX<T>, RAD>(S, W, 1, ld, tid % B, live ? tid / B : IDLE_T, plan, tws, si);
 
     // line l -> rows 2l (real parts) and 2l+1 (imaginary parts), n < n_out
     const int no = a.n_out;
@@ -350,20 +352,20 @@ __device__ __forceinline__ void xinv_body(const XInvArgs &a, int bx, int comp, i
     }
 }
 
-template <typename T> __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
+template <typename T, bool RAD = false> __global__ void __launch_bounds__(MAX_THREADS) k_xinv(const XInvArgs a)
 {
-    xinv_body<T>(a, blockIdx.x, blockIdx.y, blockDim.x);
+    xinv_body<T, RAD>(a, blockIdx.x, blockIdx.y, blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
-// Batched passes: one launch runs a pass of many independent problems. Each
-// persistent CTA walks the tile list (tile i, i + gridDim.x, ...), copies the
-// arguments of its tile's problem into shared memory and runs the pass body
-// with that problem's thread count (the launch's block size is the largest
-// of them). With the arguments in memory rather than in the constant bank the
-// bodies need more registers: up to 255 a thread at 256 threads a CTA keeps
-// them from spilling (at 512 threads ptxas held them to 64 and spilled
-// 0.6-6.6 KB a thread).
+// Batched passes: one launch runs a pass of many independent problems. CTA i
+// takes tile i of the tile list, copies the arguments of its tile's problem
+// into shared memory and runs the pass body with that problem's thread count
+// (the launch's block size is the largest of them). One tile a CTA, not a
+// persistent CTA walking the list: with the pass body inside a tile loop
+// ptxas kept these kernels at 128 registers and spilled 1.7-3.7 KB a thread
+// (255 registers still spilled 1.1-1.8 KB), where one tile a CTA compiles to
+// 48-76 registers without spills.
 template <typename Args> __device__ __forceinline__ void load_args(Args &dst, const Args *src)
 {
     static_assert(sizeof(Args) % sizeof(int) == 0, "argument blocks are whole words");
@@ -372,55 +374,51 @@ template <typename Args> __device__ __forceinline__ void load_args(Args &dst, co
     for (int i = threadIdx.x; i < (int)(sizeof(Args) / sizeof(int)); i += blockDim.x) d[i] = s[i];
 }
 
-template <typename T>
+template <typename T, bool RAD = false>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_xfwd_batch(const XFwdArgs *args, const BatchTile *tiles, int ntiles)
 {
     __shared__ XFwdArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();  // the previous tile no longer reads a or the shared buffers
+    if ((int)blockIdx.x < ntiles) {
+        const BatchTile tl = tiles[blockIdx.x];
         load_args(a, args + tl.p);
         __syncthreads();
-        xfwd_body<T>(a, tl.bx, tl.by, a.B * a.plan.tpl);
+        xfwd_body<T, RAD>(a, tl.bx, tl.by, a.B * a.plan.tpl);
     }
 }
 
-template <typename T, bool INV>
+template <typename T, bool INV, bool RAD = false>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_col_batch(const ColArgs *args, const BatchTile *tiles, int ntiles)
 {
     __shared__ ColArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();
+    if ((int)blockIdx.x < ntiles) {
+        const BatchTile tl = tiles[blockIdx.x];
         load_args(a, args + tl.p);
         __syncthreads();
-        col_body<T, INV>(a, tl.bx, tl.by, tl.bz, a.B * a.plan.tpl);
+        col_body<T, INV, RAD>(a, tl.bx, tl.by, tl.bz, a.B * a.plan.tpl);
     }
 }
 
-template <typename T>
+template <typename T, bool RAD = false>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_z_batch(const ZArgs *args, const BatchTile *tiles, int ntiles)
 {
     __shared__ ZArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();
+    if ((int)blockIdx.x < ntiles) {
+        const BatchTile tl = tiles[blockIdx.x];
         load_args(a, args + tl.p);
         __syncthreads();
-        z_body<T, -1>(a, tl.bx, tl.by, a.B * a.plan.tpl);
+        z_body<T, -1, RAD>(a, tl.bx, tl.by, a.B * a.plan.tpl);
     }
 }
 
-template <typename T>
+template <typename T, bool RAD = false>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_xinv_batch(const XInvArgs *args, const BatchTile *tiles, int ntiles)
 {
     __shared__ XInvArgs a;
-    for (int i = blockIdx.x; i < ntiles; i += gridDim.x) {
-        const BatchTile tl = tiles[i];
-        __syncthreads();
+    if ((int)blockIdx.x < ntiles) {
+        const BatchTile tl = tiles[blockIdx.x];
         load_args(a, args + tl.p);
         __syncthreads();
-        xinv_body<T>(a, tl.bx, tl.by, a.B * a.plan.tpl);
+        xinv_body<T, RAD>(a, tl.bx, tl.by, a.B * a.plan.tpl);
     }
 }
 
@@ -436,125 +434,132 @@ template <typename K> inline cudaError_t prep(K kernel, size_t smem)
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+template <typename K, typename A> inline cudaError_t run(K kernel, dim3 grid, int nt, size_t sm, cudaStream_t st, const A &a)
+{
+    cudaError_t e = prep(kernel, sm);
+    if (e != cudaSuccess) return e;
+    kernel<<<grid, nt, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Rader plans (an FP32 plan variant) run on their own instantiations, in
+// ps_kernels_rader.cu (a translation unit of its own, compiled in parallel).
+template <typename T> constexpr bool HAS_RAD = std::is_same<T, float>::value;
+cudaError_t xfwd_rader(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st);
+cudaError_t col_rader(int inverse, const ColArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st);
+cudaError_t z_rader(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st);
+cudaError_t xinv_rader(const XInvArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st);
+cudaError_t xfwd_batch_rader(const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                             cudaStream_t st);
+cudaError_t col_batch_rader(int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                            cudaStream_t st);
+cudaError_t z_batch_rader(const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, cudaStream_t st);
+cudaError_t xinv_batch_rader(const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
+                             cudaStream_t st);
+
 template <typename T> inline cudaError_t xfwd(const XFwdArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    cudaError_t e = prep(k_xfwd<T>, sm);
-    if (e != cudaSuccess) return e;
-    k_xfwd<T><<<grid, nt, sm, st>>>(a);
-    return cudaGetLastError();
+    if constexpr (HAS_RAD<T>)
+        if (a.plan.rader) return xfwd_rader(a, grid, nt, sm, st);
+    return run(k_xfwd<T>, grid, nt, sm, st, a);
 }
 
 template <typename T>
 inline cudaError_t col(int inverse, const ColArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    cudaError_t e;
-    if (inverse) {
-        if ((e = prep(k_col<T, true>, sm)) != cudaSuccess) return e;
-        k_col<T, true><<<grid, nt, sm, st>>>(a);
-    } else {
-        if ((e = prep(k_col<T, false>, sm)) != cudaSuccess) return e;
-        k_col<T, false><<<grid, nt, sm, st>>>(a);
-    }
-    return cudaGetLastError();
+    if constexpr (HAS_RAD<T>)
+        if (a.plan.rader) return col_rader(inverse, a, grid, nt, sm, st);
+    return inverse ? run(k_col<T, true>, grid, nt, sm, st, a) : run(k_col<T, false>, grid, nt, sm, st, a);
 }
 
 template <typename T> inline cudaError_t z(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    cudaError_t e;
-#define PS_LAUNCH_Z(OPV)                                               \
-    case OPV:                                                          \
-        if ((e = prep(k_z<T, OPV>, sm)) != cudaSuccess) return e;      \
-        k_z<T, OPV><<<grid, nt, sm, st>>>(a);                          \
-        break;
+    if constexpr (HAS_RAD<T>)
+        if (a.plan.rader) return z_rader(a, grid, nt, sm, st);
     switch (a.op) {
-        PS_LAUNCH_Z(OP_NONE)
-        PS_LAUNCH_Z(OP_GRAD)
-        PS_LAUNCH_Z(OP_DIV)
-        PS_LAUNCH_Z(OP_CURL)
-        PS_LAUNCH_Z(OP_FILTER)
-        PS_LAUNCH_Z(OP_FORWARD)
+    case OP_NONE: return run(k_z<T, OP_NONE>, grid, nt, sm, st, a);
+    case OP_GRAD: return run(k_z<T, OP_GRAD>, grid, nt, sm, st, a);
+    case OP_DIV: return run(k_z<T, OP_DIV>, grid, nt, sm, st, a);
+    case OP_CURL: return run(k_z<T, OP_CURL>, grid, nt, sm, st, a);
+    case OP_FILTER: return run(k_z<T, OP_FILTER>, grid, nt, sm, st, a);
+    case OP_FORWARD: return run(k_z<T, OP_FORWARD>, grid, nt, sm, st, a);
     default: return cudaErrorInvalidValue;
     }
-#undef PS_LAUNCH_Z
-    return cudaGetLastError();
 }
 
 // one kernel for every spectral operation, read from a.op at run time
 template <typename T> inline cudaError_t z_any_op(const ZArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    cudaError_t e = prep(k_z<T, -1>, sm);
-    if (e != cudaSuccess) return e;
-    k_z<T, -1><<<grid, nt, sm, st>>>(a);
-    return cudaGetLastError();
+    return run(k_z<T, -1>, grid, nt, sm, st, a);
 }
 
 template <typename T> inline cudaError_t xinv(const XInvArgs &a, dim3 grid, int nt, size_t sm, cudaStream_t st)
 {
-    cudaError_t e = prep(k_xinv<T>, sm);
-    if (e != cudaSuccess) return e;
-    k_xinv<T><<<grid, nt, sm, st>>>(a);
-    return cudaGetLastError();
+    if constexpr (HAS_RAD<T>)
+        if (a.plan.rader) return xinv_rader(a, grid, nt, sm, st);
+    return run(k_xinv<T>, grid, nt, sm, st, a);
 }
 
 // Batched launches: nt threads and smem bytes a CTA (the largest over the
-// batch's problems), as many persistent CTAs as fit on the GPU at once.
-template <typename K> inline cudaError_t persistent_grid(K kernel, int ntiles, int nt, size_t smem, int &grid)
+// batch's problems), one CTA a tile; a configuration no SM can hold is an
+// error here rather than at the launch.
+template <typename K> inline cudaError_t tile_grid(K kernel, int ntiles, int nt, size_t smem, int &grid)
 {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int per_sm = 0, dev = 0, sms = 0;
+    int per_sm = 0;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, smem)) != cudaSuccess) return e;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    grid = ntiles < per_sm * sms ? ntiles : per_sm * sms;
+    grid = ntiles;
     return cudaSuccess;
 }
 
-template <typename T>
-inline cudaError_t xfwd_batch(const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, cudaStream_t st)
+template <typename K, typename A>
+inline cudaError_t run_tiles(K kernel, const A *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, cudaStream_t st)
 {
     int grid = 0;
-    cudaError_t e = persistent_grid(k_xfwd_batch<T>, ntiles, nt, smem, grid);
+    cudaError_t e = tile_grid(kernel, ntiles, nt, smem, grid);
     if (e != cudaSuccess) return e;
-    k_xfwd_batch<T><<<grid, nt, smem, st>>>(args, tiles, ntiles);
+    kernel<<<grid, nt, smem, st>>>(args, tiles, ntiles);
     return cudaGetLastError();
+}
+
+// rader: some problem of the launch has a Rader plan on this pass (FP32)
+template <typename T>
+inline cudaError_t xfwd_batch(const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, bool rader,
+                              cudaStream_t st)
+{
+    if constexpr (HAS_RAD<T>)
+        if (rader) return xfwd_batch_rader(args, tiles, ntiles, nt, smem, st);
+    return run_tiles(k_xfwd_batch<T>, args, tiles, ntiles, nt, smem, st);
 }
 
 template <typename T>
 inline cudaError_t col_batch(int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                             cudaStream_t st)
+                             bool rader, cudaStream_t st)
 {
-    int grid = 0;
-    cudaError_t e;
-    if (inverse) {
-        if ((e = persistent_grid(k_col_batch<T, true>, ntiles, nt, smem, grid)) != cudaSuccess) return e;
-        k_col_batch<T, true><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    } else {
-        if ((e = persistent_grid(k_col_batch<T, false>, ntiles, nt, smem, grid)) != cudaSuccess) return e;
-        k_col_batch<T, false><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    }
-    return cudaGetLastError();
+    if constexpr (HAS_RAD<T>)
+        if (rader) return col_batch_rader(inverse, args, tiles, ntiles, nt, smem, st);
+    return inverse ? run_tiles(k_col_batch<T, true>, args, tiles, ntiles, nt, smem, st)
+                   : run_tiles(k_col_batch<T, false>, args, tiles, ntiles, nt, smem, st);
 }
 
 template <typename T>
-inline cudaError_t z_batch(const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, cudaStream_t st)
+inline cudaError_t z_batch(const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, bool rader,
+                           cudaStream_t st)
 {
-    int grid = 0;
-    cudaError_t e = persistent_grid(k_z_batch<T>, ntiles, nt, smem, grid);
-    if (e != cudaSuccess) return e;
-    k_z_batch<T><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    return cudaGetLastError();
+    if constexpr (HAS_RAD<T>)
+        if (rader) return z_batch_rader(args, tiles, ntiles, nt, smem, st);
+    return run_tiles(k_z_batch<T>, args, tiles, ntiles, nt, smem, st);
 }
 
 template <typename T>
-inline cudaError_t xinv_batch(const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, cudaStream_t st)
+inline cudaError_t xinv_batch(const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem, bool rader,
+                              cudaStream_t st)
 {
-    int grid = 0;
-    cudaError_t e = persistent_grid(k_xinv_batch<T>, ntiles, nt, smem, grid);
-    if (e != cudaSuccess) return e;
-    k_xinv_batch<T><<<grid, nt, smem, st>>>(args, tiles, ntiles);
-    return cudaGetLastError();
+    if constexpr (HAS_RAD<T>)
+        if (rader) return xinv_batch_rader(args, tiles, ntiles, nt, smem, st);
+    return run_tiles(k_xinv_batch<T>, args, tiles, ntiles, nt, smem, st);
 }
 
 // the double-float instantiations (ps_kernels_df.cu): single problems only,

@@ -153,14 +153,16 @@ static void host_fft_pow2(std::vector<std::complex<long double>> &a)
     }
 }
 
-// In-place DFT (e^{-2 pi i nk / M}) of a length M = 2^a 3^b 5^c in extended
-// precision, by recursive decimation in time: the spectrum of a Bluestein
-// kernel on a smooth convolution length.
+// In-place DFT (e^{-2 pi i nk / M}) in extended precision, by recursive
+// decimation in time over the smallest prime factor (O(M * sum of the prime
+// factors)): the spectrum of a Bluestein kernel on a smooth convolution
+// length, and the convolution spectrum of a Rader stage.
 static void host_fft_smooth(std::vector<std::complex<long double>> &a)
 {
     const size_t M = a.size();
     if (M <= 1) return;
-    const size_t R = M % 2 == 0 ? 2 : M % 3 == 0 ? 3 : 5;
+    size_t R = 2;
+    while (M % R != 0) ++R;
     const size_t m = M / R;
     std::vector<std::vector<std::complex<long double>>> sub(R, std::vector<std::complex<long double>>(m));
     for (size_t n = 0; n < m; ++n)
@@ -201,14 +203,64 @@ static bool bluestein_length(int L)
     return L > 16 && largest_prime_factor(L) >= BLUESTEIN_MIN_PRIME && !getenv("PS_NO_BLUESTEIN");
 }
 
+// Threads a line of length Ls needs for the stages rs with emax register
+// elements a thread: a fixed radix R takes emax / R butterflies a thread, a
+// direct-DFT stage spreads the line's outputs over up to 64 threads.
+static int stage_threads(const std::vector<int> &rs, int Ls, int emax)
+{
+    int tp = 1;
+    for (int R : rs) tp = std::max(tp, fixed_radix(R) ? (Ls / R + emax / R - 1) / (emax / R) : std::min(Ls, 64));
+    return tp;
+}
+
+// Rader's algorithm applies to a Bluestein length L whose largest prime p
+// divides it once, whose cofactor L / p and p - 1 have no prime factor above
+// 13 (their stages are the fixed radices and the direct radix-11/13 stages),
+// whose sub-transforms all run at once on at most 256 threads a line, and
+// whose stage count (the Rader stage, the cofactor's stages and those of
+// p - 1) fits the stage table.
+static bool rader_length(int L, int max_radix, int emax)
+{
+    if (!bluestein_length(L)) return false;
+    const int p = largest_prime_factor(L), c = L / p;
+    if (c % p == 0 || largest_prime_factor(c) > 13 || largest_prime_factor(p - 1) > 13) return false;
+    const std::vector<int> sub = factorize(p - 1, max_radix);
+    if (stage_threads(sub, p - 1, emax) * c > 256) return false;
+    return 1 + (int)factorize(c, max_radix).size() + (int)sub.size() <= MAX_STAGES;
+}
+
+// smallest primitive root of the prime p
+static int primitive_root(int p)
+{
+    std::vector<int> f;
+    for (int x = p - 1, q = 2; x > 1; ++q)
+        if (x % q == 0) {
+            f.push_back(q);
+            while (x % q == 0) x /= q;
+        }
+    for (int g = 2;; ++g) {
+        bool ok = true;
+        for (int q : f) {
+            long long r = 1, b = g;
+            for (int e = (p - 1) / q; e > 0; e >>= 1, b = b * b % p)
+                if (e & 1) r = r * b % p;
+            if (r == 1) ok = false;
+        }
+        if (ok) return g;
+    }
+}
+
 const Plan &Solver::plan(int L, int prec, int emax, int pv)
 {
     if (emax <= 0) emax = e_max(prec);
     if (prec != PREC_FP32) pv = 0;  // FP64 results do not depend on tuning
     const int Lt = L;  // the transform length
-    const bool blue = bluestein_length(Lt);
-    if (!blue) pv &= ~PV_SMOOTH_M;
     if (emax < 16) pv &= ~PV_HALF_RADIX;
+    const int rmax = (pv & PV_HALF_RADIX) ? emax / 2 : emax;  // the radix cap of the stages
+    if (!rader_length(Lt, rmax, emax)) pv &= ~PV_RADER;
+    const bool rader = (pv & PV_RADER) != 0;
+    const bool blue = bluestein_length(Lt) && !rader;
+    if (!blue) pv &= ~PV_SMOOTH_M;
     const auto key = std::make_tuple(L, prec, emax, pv);
     auto it = plans.find(key);
     if (it != plans.end()) return *it->second;
@@ -221,35 +273,82 @@ const Plan &Solver::plan(int L, int prec, int emax, int pv)
     d.L = L;
     d.blue = blue ? 1 : 0;
     d.lb = Lt;
-    std::vector<int> rad = L > 1 ? factorize(L, (pv & PV_HALF_RADIX) ? emax / 2 : emax) : std::vector<int>{};
+    const int rp = rader ? largest_prime_factor(Lt) : 0;  // the Rader stage's prime
+    std::vector<int> rad = L > 1 ? factorize(rader ? L / rp : L, rmax) : std::vector<int>{};
+    if (rader) rad.insert(rad.begin(), rp);
     if ((int)rad.size() > MAX_STAGES) throw Error(PS_ERR_UNSUPPORTED, "transform length has too many factors");
     d.nstages = (int)rad.size();
     std::vector<std::complex<long double>> tab;
-    int m = 1, tpl = 1;
-    for (int s = 0; s < d.nstages; ++s) {
-        const int R = rad[s];
-        d.radix[s] = R;
-        d.m[s] = m;
-        d.lm[s] = (m & (m - 1)) == 0 ? __builtin_ctz((unsigned)m) : -1;
-        d.tw[s] = (int)tab.size();
-        for (int j = 0; j < m; ++j)
-            for (int r = 1; r < R; ++r) tab.push_back(root((long long)j * r, (long long)m * R));
-        const int nbf = L / R;
-        if (fixed_radix(R)) {
-            const int U = emax / R;
-            tpl = std::max(tpl, (nbf + U - 1) / U);
-            d.gw[s] = 0;
-        } else {
-            d.generic = 1;
-            d.gw[s] = (int)tab.size();
-            for (int q = 0; q < R; ++q) tab.push_back(root(q, R));
-            // the direct DFT spreads a line's L outputs over its threads
-            tpl = std::max(tpl, std::min(L, 64));
+    // stages s0.. of a transform of length Ls from table slot `slot`: radices,
+    // sub-transform sizes, twiddles (the table entries) and the threads a line
+    // they need; a Rader stage (slot 0 of a Rader plan) has no table entries
+    auto add_stages = [&](const std::vector<int> &rs, int Ls, int slot, bool skip_first) {
+        int m = 1, tp = 1;
+        for (size_t i = 0; i < rs.size(); ++i, ++slot) {
+            const int R = rs[i];
+            d.radix[slot] = R;
+            d.m[slot] = m;
+            d.lm[slot] = (m & (m - 1)) == 0 ? __builtin_ctz((unsigned)m) : -1;
+            d.tw[slot] = (int)tab.size();
+            d.gw[slot] = 0;
+            if (!(skip_first && i == 0)) {
+                for (int j = 0; j < m; ++j)
+                    for (int r = 1; r < R; ++r) tab.push_back(root((long long)j * r, (long long)m * R));
+                const int nbf = Ls / R;
+                if (fixed_radix(R)) {
+                    const int U = emax / R;
+                    tp = std::max(tp, (nbf + U - 1) / U);
+                } else {
+                    d.generic = 1;
+                    d.gw[slot] = (int)tab.size();
+                    for (int q = 0; q < R; ++q) tab.push_back(root(q, R));
+                    // the direct DFT spreads a line's L outputs over its threads
+                    tp = std::max(tp, std::min(Ls, 64));
+                }
+            }
+            m *= R;
         }
-        m *= R;
+        return tp;
+    };
+    int tpl = add_stages(rad, L, 0, rader);
+    if (rader) {
+        // sub-transforms of p - 1 points in the stage slots after the plan's
+        const std::vector<int> sub = factorize(rp - 1, rmax);
+        d.rader = 1;
+        d.generic = 1;  // the scratch line stages the gather and the outputs
+        d.rq = rp - 1;
+        d.rs0 = d.nstages;
+        d.rns = (int)sub.size();
+        d.rtpl = add_stages(sub, rp - 1, d.rs0, false);
+        // every sub-line at once (rader_length keeps this within 256 threads);
+        // the DC terms of the sub-transforms are held by line threads 0 .. L / p - 1
+        const int nbf = L / rp;
+        tpl = std::max({tpl, d.rtpl * nbf, nbf});
+        d.rinv_p = (float)(1.0 / rp);
+        d.rinv_q = (float)(1.0 / (rp - 1));
     }
     d.tpl = tpl;
     d.ntw = (int)tab.size();  // the part copied to shared memory
+    std::vector<int> itab;
+    if (rader) {
+        // the convolution spectra FFT(beta) / (p - 1), beta[m] = w^(g^m),
+        // forward (w = e^{-2 pi i / p}) then inverse (its conjugate), and the
+        // index tables: g^-j mod p, then log_g k at k - 1
+        const int p = rp, q1 = p - 1, g = primitive_root(p);
+        std::vector<long long> gp(q1);
+        gp[0] = 1;
+        for (int j = 1; j < q1; ++j) gp[j] = gp[j - 1] * g % p;
+        for (int inv = 0; inv < 2; ++inv) {
+            std::vector<std::complex<long double>> bt(q1);
+            for (int j = 0; j < q1; ++j) bt[j] = inv ? std::conj(root(gp[j], p)) : root(gp[j], p);
+            host_fft_smooth(bt);
+            if (inv == 0) d.rbh = (int)tab.size();
+            for (int j = 0; j < q1; ++j) tab.push_back(bt[j] / (long double)q1);
+        }
+        itab.resize(2 * q1);
+        for (int j = 0; j < q1; ++j) itab[j] = (int)gp[(q1 - j) % q1];  // g^-j
+        for (int q = 0; q < q1; ++q) itab[q1 + gp[q] - 1] = q;          // log_g (g^q)
+    }
     if (blue) {
         // chirp c[n] = e^{-i pi n^2 / Lt} and the spectrum of its conjugate
         // wrapped onto M = L points, scaled by 1/M (read through the cache)
@@ -294,6 +393,11 @@ const Plan &Solver::plan(int L, int prec, int emax, int pv)
         }
     }
     d.table = pl->table.p;
+    if (!itab.empty()) {
+        pl->itable.ensure(itab.size() * sizeof(int));
+        PS_CK(cudaMemcpy(pl->itable.p, itab.data(), itab.size() * sizeof(int), cudaMemcpyHostToDevice));
+        d.itab = static_cast<const int *>(pl->itable.p);
+    }
     Plan &ref = *pl;
     plans[key] = std::move(pl);
     return ref;
@@ -1009,8 +1113,9 @@ const Plan &Solver::pass_plan(int pass, const PassChoice &c)
 }
 
 // The plan variants that change the run-time family's plan of a pass (FP32
-// only): a radix cap below an element budget of 16, and a smooth Bluestein
-// length that is shorter than the power of two.
+// only): a radix cap below an element budget of 16, a smooth Bluestein
+// length that is shorter than the power of two, and a Rader stage in place of
+// Bluestein's algorithm.
 int Solver::plan_variants(int pass) const
 {
     if (precision != PREC_FP32) return 0;
@@ -1018,6 +1123,7 @@ int Solver::plan_variants(int pass) const
     int v = 0;
     if (family_emax(pass, 'r') >= 16 && L > 1) v |= PV_HALF_RADIX;
     if (bluestein_length(L) && next_smooth(2 * L - 1) < next_pow2(2 * L - 1)) v |= PV_SMOOTH_M;
+    if (rader_length(L, family_emax(pass, 'r'), family_emax(pass, 'r'))) v |= PV_RADER;
     return v;
 }
 
@@ -1111,7 +1217,7 @@ void tune_load_locked()
         int B = 0, pv = 0;
         if (!(in >> key >> fam >> B)) continue;
         if (!(in >> pv)) pv = 0;
-        if (fam.size() == 1 && B >= 1 && B <= 64 && pv >= 0 && pv <= 3) tune_table[key] = PassChoice{fam[0], B, pv};
+        if (fam.size() == 1 && B >= 1 && B <= 64 && pv >= 0 && pv <= 7) tune_table[key] = PassChoice{fam[0], B, pv};
     }
 }
 
@@ -1244,7 +1350,7 @@ void Solver::autotune(int in_mask)
             for (char fam : {'q', 't', 'w', 'p', 'r'}) {
                 if (!family_ok(pass, fam, pa)) continue;
                 const int pvs = fam == 'r' ? plan_variants(pass) : 0;
-                for (int pv = 0; pv <= 3; ++pv) {
+                for (int pv = 0; pv <= 7; ++pv) {
                     if ((pv & ~pvs) != 0) continue;
                     const Plan &pl = pass_plan(pass, PassChoice{fam, 1, pv});
                     for (int B = 1; B <= 64; B *= 2)

@@ -58,6 +58,7 @@ struct DevBuf {
 struct Plan {
     FftPlanDev dev{};
     DevBuf table;
+    DevBuf itable;  // index tables of a Rader plan
 };
 
 // Plan variants of the run-time family, tuned for FP32 transforms (FP64
@@ -65,8 +66,11 @@ struct Plan {
 // PV_HALF_RADIX runs the power-of-two part of a length in radices of half the
 // element budget (radix 8 instead of 16: one stage more, two butterflies a
 // thread); PV_SMOOTH_M takes Bluestein's convolution length as the least
-// 2^a 3^b 5^c >= 2 lb - 1 instead of the least power of two.
-enum { PV_HALF_RADIX = 1, PV_SMOOTH_M = 2 };
+// 2^a 3^b 5^c >= 2 lb - 1 instead of the least power of two; PV_RADER
+// replaces Bluestein's algorithm by a Rader stage for the largest prime p
+// where p - 1 and the cofactor are 13-smooth (a cyclic convolution of p - 1
+// points in place of two transforms of at least 2 L - 1).
+enum { PV_HALF_RADIX = 1, PV_SMOOTH_M = 2, PV_RADER = 4 };
 
 // Kernel family and lines per CTA of one pass: 'r' run-time, 'p' length-
 // specialised, 'w' wide, 't' tensor-memory fused z, 'q' a warp per line or

@@ -41,6 +41,19 @@ struct FftPlanDev {
     int lb;     // the transform length (L for other plans)
     int chirp;  // table offset of c[n] = e^{-i pi n^2 / lb}, n < lb
     int kspec;  // table offset of K[k] = FFT_M(conj c, wrapped)[k] / M, k < M
+    // Rader plans (FP32 plan variant): stage 0 has a prime radix p >= 17 and
+    // m = 1, and each of its L / p butterflies is computed by Rader's
+    // algorithm, a cyclic convolution of p - 1 points run by the sub-transform
+    // stages rs0 .. rs0 + rns - 1 of the stage table (their twiddles in the
+    // shared table, like the plan's own).
+    int rader;   // 1 for a Rader plan
+    int rq;      // p - 1, the sub-transform length
+    int rtpl;    // threads a sub-transform
+    int rs0;     // first sub-transform stage in the stage table
+    int rns;     // sub-transform stages
+    int rbh;     // table offset of the convolution spectra: forward (p - 1 entries), then inverse
+    const int *itab;  // g^-j mod p for j < p - 1, then log_g k for k = 1 .. p - 1 (g a primitive root)
+    float rinv_p, rinv_q;  // 1 / p and 1 / (p - 1), for exact index division in FP32
 };
 
 // Spectral operation of the fused z pass.
@@ -138,15 +151,17 @@ cudaError_t launch_xinv(int prec, const XInvArgs &a, cudaStream_t st);
 struct BatchTile {
     int p, bx, by, bz;
 };
+// rader: some problem of the launch has a Rader plan on the pass (the
+// launch then runs the kernels instantiated for them).
 constexpr int BATCH_MAX_THREADS = 256;  // CTA size bound of the batched passes
 cudaError_t launch_xfwd_batch(int prec, const XFwdArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                              cudaStream_t st);
+                              bool rader, cudaStream_t st);
 cudaError_t launch_col_batch(int prec, int inverse, const ColArgs *args, const BatchTile *tiles, int ntiles, int nt,
-                             size_t smem, cudaStream_t st);
+                             size_t smem, bool rader, cudaStream_t st);
 cudaError_t launch_z_batch(int prec, const ZArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                           cudaStream_t st);
+                           bool rader, cudaStream_t st);
 cudaError_t launch_xinv_batch(int prec, const XInvArgs *args, const BatchTile *tiles, int ntiles, int nt, size_t smem,
-                              cudaStream_t st);
+                              bool rader, cudaStream_t st);
 
 // Shared-memory bytes each pass needs for a given line count (data, scratch
 // for direct-DFT stages, twiddle table).

@@ -333,6 +333,11 @@ class PoissonBatch:
         the pushed problems and keep the fastest."""
         self._call("ps_batch_autotune")
 
+    def set_tuning(self, axis: int, max_threads: int, start_lines: int, plan_variant: int):
+        """Set the CTA thread bound, starting lines and plan variant of the x
+        (0), y (1) or z (2) launches; the next solve rebuilds the batch."""
+        self._call("ps_batch_set_tuning", int(axis), int(max_threads), int(start_lines), int(plan_variant))
+
     def tuning(self):
         """[(CTA thread bound, starting lines, plan variant)] of the x, y and
         z launches."""

@@ -212,7 +212,7 @@ def test_autotuned_batch_gives_the_same_results(native, precision):
     before = [_pull(b, i) for i in range(len(PROBLEMS))]
     b.autotune()
     for t, s, v in b.tuning():
-        assert t in (64, 128, 256) and s in (2, 4, 8, 16, 32) and v in (0, 1, 2, 3)
+        assert t in (64, 128, 256) and s in (2, 4, 8, 16, 32) and 0 <= v <= 7
         assert precision == "fp32" or v == 0  # FP64 batches keep the default plans
     b.solve()
     after = [_pull(b, i) for i in range(len(PROBLEMS))]

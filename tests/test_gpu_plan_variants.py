@@ -133,6 +133,6 @@ def test_autotune_considers_plan_variants(native, tmp_path, monkeypatch):
         s.pull(*A1)
         assert rel_l2(A1, A0) < 1e-6
         xs, xm = s.pass_plan(7)[0]
-        assert (xs, xm) in [EXPECTED[v][:2] for v in range(4)]
+        assert (xs, xm) in [EXPECTED[v][:2] for v in range(4)] + [([97, 2], 96)]  # or Rader's (bit 2)
     lines = (tmp_path / "tune.txt").read_text().split("\n")
-    assert all(int(l.split()[3]) in (0, 1, 2, 3) for l in lines if l)
+    assert all(0 <= int(l.split()[3]) <= 7 for l in lines if l)
