@@ -518,14 +518,15 @@ constexpr int IDLE_T = 1 << 28;
 // circular convolution of length M done by the plan's stages (forward, times the precomputed
 // spectrum K of the wrapped conj(c) scaled by 1/M, unnormalised inverse). The
 // inverse DFT conjugates the chirp and reads K at -k, which is the spectrum of
-// the wrapped c. The chirp and K are read from the plan's global table (each
-// entry once a line), the stage twiddles from shared memory.
+// the wrapped c. The chirp and K are read from the shared copy of the table
+// when the plan stages them there (bsh), else from the plan's global table
+// (each entry once a line); the stage twiddles always from shared memory.
 template <bool INV, int EM, typename C>
 __device__ __forceinline__ void bluestein_lines(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
                                                 const C *tws, const StageInfo &si, int ncomp, int cstride)
 {
     const int M = P.L, Lb = P.lb, tpl = P.tpl;
-    const C *g = reinterpret_cast<const C *>(P.table);  // global table: chirp and K are not staged
+    const C *g = P.bsh ? tws : reinterpret_cast<const C *>(P.table);
     const C *ch = g + P.chirp, *K = g + P.kspec;
     for (int c = 0; c < ncomp; ++c) {
         C *Sb = S + c * cstride + b * sb;

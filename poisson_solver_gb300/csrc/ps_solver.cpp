@@ -351,7 +351,9 @@ const Plan &Solver::plan(int L, int prec, int emax, int pv)
     }
     if (blue) {
         // chirp c[n] = e^{-i pi n^2 / Lt} and the spectrum of its conjugate
-        // wrapped onto M = L points, scaled by 1/M (read through the cache)
+        // wrapped onto M = L points, scaled by 1/M; staged in shared memory
+        // with the twiddles when the two take at most 16 KB (the kernels read
+        // each entry once a line), else read through the cache
         d.chirp = (int)tab.size();
         for (long long k = 0; k < Lt; ++k) tab.push_back(root((k * k) % (2LL * Lt), 2LL * Lt));
         std::vector<std::complex<long double>> b(L, {0.0L, 0.0L});
@@ -364,6 +366,11 @@ const Plan &Solver::plan(int L, int prec, int emax, int pv)
         else host_fft_smooth(b);
         d.kspec = (int)tab.size();
         for (int k = 0; k < L; ++k) tab.push_back(b[k] / (long double)L);
+        const size_t elem = prec == PREC_FP32 ? 8 : 16;
+        if ((size_t)(Lt + L) * elem <= 16384) {
+            d.ntw = (int)tab.size();
+            d.bsh = 1;
+        }
     }
     if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length " + std::to_string(Lt) + " too large");
     if (!tab.empty()) {
