@@ -512,6 +512,51 @@ __device__ __forceinline__ void fft_stages(C *S, C *W, int sn, int sb, int b, in
 // butterfly and every element of any plan.
 constexpr int IDLE_T = 1 << 28;
 
+// Compile-time stage sequence of a power-of-two length M with EM elements a
+// thread: radix-EM stages, then one radix 2^rem stage (the order the host's
+// factorisation gives such a length), with M / EM threads a line. Every
+// radix, sub-transform size, twiddle offset and loop bound is a constant, so
+// the index arithmetic of the run-time stage loop folds away. The host marks
+// the Bluestein plans whose convolution stages are exactly these (ctm = M).
+__host__ __device__ constexpr int ct_log2(int x) { return x <= 1 ? 0 : 1 + ct_log2(x >> 1); }
+
+template <int M, int EM> struct CtPlan {
+    static constexpr int LM = ct_log2(M), LE = ct_log2(EM);
+    static constexpr int NFULL = LM / LE, REM = LM - NFULL * LE, NST = NFULL + (REM ? 1 : 0);
+    static constexpr int L = M, tpl = M / EM;
+    __host__ __device__ static constexpr int radix(int s) { return s < NFULL ? EM : (1 << REM); }
+    __host__ __device__ static constexpr int mm(int s) { return s == 0 ? 1 : mm(s - 1) * radix(s - 1); }
+    __host__ __device__ static constexpr int tw(int s) { return s == 0 ? 0 : tw(s - 1) + mm(s - 1) * (radix(s - 1) - 1); }
+};
+
+template <bool INV, int EM, int M, int S = 0, typename C>
+__device__ __forceinline__ void ct_stages(C *Sl, int sn, int sb, int b, int t, const C *tws, int ncomp, int cstride)
+{
+    using PL = CtPlan<M, EM>;
+    if constexpr (S < PL::NST) {
+        constexpr int R = PL::radix(S), m = PL::mm(S);
+        for (int c = 0; c < ncomp; ++c)
+            stage<EM, R, INV>(Sl + c * cstride, sn, sb, b, t, PL{}, tws, make_int4(R, m, PL::tw(S), 0), ct_log2(m));
+        ct_stages<INV, EM, M, S + 1>(Sl, sn, sb, b, t, tws, ncomp, cstride);
+    }
+}
+
+// The convolution transforms of a Bluestein plan: compile-time stages for
+// the marked power-of-two lengths, the run-time stage loop otherwise.
+template <bool INV, int EM, typename C>
+__device__ __forceinline__ void blue_stages(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
+                                            const C *tws, const StageInfo &si, int ncomp, int cstride)
+{
+    switch (P.ctm) {
+    case 64: ct_stages<INV, EM, 64>(S, sn, sb, b, t, tws, ncomp, cstride); break;
+    case 128: ct_stages<INV, EM, 128>(S, sn, sb, b, t, tws, ncomp, cstride); break;
+    case 256: ct_stages<INV, EM, 256>(S, sn, sb, b, t, tws, ncomp, cstride); break;
+    case 512: ct_stages<INV, EM, 512>(S, sn, sb, b, t, tws, ncomp, cstride); break;
+    case 1024: ct_stages<INV, EM, 1024>(S, sn, sb, b, t, tws, ncomp, cstride); break;
+    default: fft_stages<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    }
+}
+
 // Bluestein's algorithm for a length lb with a large prime factor, on lines
 // of M = P.L >= 2 lb - 1 elements (a power of two, or 2^a 3^b 5^c): with
 // c[n] = e^{-i pi n^2 / lb}, X[k] = c[k] sum_n (x[n] c[n]) conj(c[k - n]), a
@@ -537,7 +582,7 @@ __device__ __forceinline__ void bluestein_lines(C *S, C *W, int sn, int sb, int 
         }
     }
     __syncthreads();
-    fft_stages<false, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    blue_stages<false, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
     for (int c = 0; c < ncomp; ++c) {
         C *Sb = S + c * cstride + b * sb;
         for (int k = t; k < M; k += tpl) {
@@ -547,7 +592,7 @@ __device__ __forceinline__ void bluestein_lines(C *S, C *W, int sn, int sb, int 
         }
     }
     __syncthreads();
-    fft_stages<true, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    blue_stages<true, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
     for (int c = 0; c < ncomp; ++c) {
         C *Sb = S + c * cstride + b * sb;
         for (int k = t; k < Lb; k += tpl) Sb[k * sn] = INV ? cmulc(Sb[k * sn], ch[k]) : cmul(Sb[k * sn], ch[k]);

@@ -371,6 +371,13 @@ const Plan &Solver::plan(int L, int prec, int emax, int pv)
             d.ntw = (int)tab.size();
             d.bsh = 1;
         }
+        // the kernels' compile-time stage sequence of a power-of-two M (64 ..
+        // 1024): radix-emax stages, then one stage of the remaining power of
+        // two, M / emax threads a line
+        bool ct = (L & (L - 1)) == 0 && L >= 64 && L <= 1024 && d.tpl == L / emax;
+        for (int s = 0, lg = __builtin_ctz((unsigned)L), le = __builtin_ctz((unsigned)emax); ct && s < d.nstages; ++s)
+            ct = d.radix[s] == (s < lg / le ? emax : 1 << (lg % le)) && d.nstages == lg / le + (lg % le ? 1 : 0);
+        if (ct) d.ctm = L;
     }
     if (tpl > MAX_THREADS) throw Error(PS_ERR_UNSUPPORTED, "transform length " + std::to_string(Lt) + " too large");
     if (!tab.empty()) {

@@ -42,6 +42,7 @@ struct FftPlanDev {
     int chirp;  // table offset of c[n] = e^{-i pi n^2 / lb}, n < lb
     int kspec;  // table offset of K[k] = FFT_M(conj c, wrapped)[k] / M, k < M
     int bsh;    // 1: chirp and K lie in the part of the table staged in shared memory
+    int ctm;    // M when the convolution stages are the compile-time sequence of M (64..1024), else 0
     // Rader plans (FP32 plan variant): stage 0 has a prime radix p >= 17 and
     // m = 1, and each of its L / p butterflies is computed by Rader's
     // algorithm, a cyclic convolution of p - 1 points run by the sub-transform
