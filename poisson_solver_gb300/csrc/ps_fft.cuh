@@ -334,8 +334,9 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *x)
 // start (indexing the plan's arrays in the kernel parameters at run time
 // would force a local-memory copy of the whole parameter block).
 struct StageInfo {
-    int4 st[MAX_STAGES];  // radix, m, twiddle offset, generic-table offset
-    int lm[MAX_STAGES];   // log2(m) or -1
+    int4 st[MAX_STAGES];       // radix, m, twiddle offset, generic-table offset
+    int lm[MAX_STAGES];        // log2(m) or -1
+    unsigned mg[MAX_STAGES];   // floor(2^32 / m) + 1 when m is not a power of two (split_index)
 };
 
 // One stage a thread (the caller synchronises before the first use).
@@ -345,6 +346,7 @@ __device__ __forceinline__ void load_stages(StageInfo &si, const FftPlanDev &P)
     if (i < MAX_STAGES) {
         si.st[i] = make_int4(P.radix[i], P.m[i], P.tw[i], P.gw[i]);
         si.lm[i] = P.lm[i];
+        si.mg[i] = P.lm[i] < 0 && P.m[i] > 1 ? 0xFFFFFFFFu / (unsigned)P.m[i] + 1u : 0u;
     }
 }
 
@@ -357,21 +359,31 @@ template <typename C> __device__ __forceinline__ const C *stage_twiddles(const F
     return TW;
 }
 
-// j = bf mod m and q = bf / m, by shifts when m is a power of two
-__device__ __forceinline__ void split_index(int bf, int m, int lm, int &j, int &q)
+// Division of n < 2^16 by a run-time d < 2^16 without a divide: q = n / d is
+// the high word of n * div_magic(d) (the multiplier argument of split_index
+// below); d = 1 gives n.
+__device__ __forceinline__ unsigned div_magic(int d) { return d > 1 ? 0xFFFFFFFFu / (unsigned)d + 1u : 0u; }
+__device__ __forceinline__ int div_by(int n, int d, unsigned mg) { return d > 1 ? (int)__umulhi((unsigned)n, mg) : n; }
+
+// j = bf mod m and q = bf / m, by shifts when m is a power of two, else by
+// the multiplier mg = floor(2^32 / m) + 1: with mg m = 2^32 + e, 0 < e <= m,
+// floor(bf mg / 2^32) = floor(bf / m) whenever bf e < 2^32, which bf, m < 2^16
+// (butterfly counts and sub-transform sizes of any plan) guarantee.
+__device__ __forceinline__ void split_index(int bf, int m, int lm, unsigned mg, int &j, int &q)
 {
     if (lm >= 0) {
         j = bf & (m - 1);
         q = bf >> lm;
     } else {
-        q = bf / m;
+        q = (int)__umulhi((unsigned)bf, mg);
         j = bf - q * m;
     }
 }
 
 // One in-place Stockham stage with a compile-time radix.
 template <int EM, int R, bool INV, typename C, typename PL>
-__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const PL &P, const C *tws, int4 sd, int lm)
+__device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const PL &P, const C *tws, int4 sd, int lm,
+                                      unsigned mg = 0u)
 {
     constexpr int U = EM / R;
     const int L = P.L, m = sd.y, nbf = L / R, tpl = P.tpl;
@@ -384,7 +396,7 @@ __device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const 
         const int bf = t + u * tpl;
         if (bf < nbf) {
             int j, q;
-            split_index(bf, m, lm, j, q);
+            split_index(bf, m, lm, mg, j, q);
             const C *src = Sb + bf * sn;
 #pragma unroll
             for (int r = 0; r < R; ++r) v[u][r] = src[r * rstride];
@@ -404,7 +416,7 @@ __device__ __forceinline__ void stage(C *S, int sn, int sb, int b, int t, const 
         const int bf = t + u * tpl;
         if (bf < nbf) {
             int j, q;
-            split_index(bf, m, lm, j, q);
+            split_index(bf, m, lm, mg, j, q);
             C *dst = Sb + (q * R * m + j) * sn;
             const int mstride = m * sn;
 #pragma unroll
@@ -428,19 +440,20 @@ __device__ void stage_generic(C *S, C *W, int sn, int sb, int b, int t, const PL
     const C *tw = tws + sd.z;
     const C *gw = tws + sd.w;
     C *Sb = S + b * sb, *Wb = W + b * sb;
+    const unsigned mgn = div_magic(nbf), mgm = div_magic(m);  // index divisions by nbf and m
     if (m > 1) {
         for (int e = t; e < L; e += tpl) {
-            const int r = e / nbf, bf = e - r * nbf;
+            const int r = div_by(e, nbf, mgn), bf = e - r * nbf;
             if (r > 0) {
-                const C w = tw[(bf % m) * (R - 1) + r - 1];
+                const C w = tw[(bf - div_by(bf, m, mgm) * m) * (R - 1) + r - 1];
                 Sb[e * sn] = INV ? cmulc(Sb[e * sn], w) : cmul(Sb[e * sn], w);
             }
         }
         __syncthreads();
     }
     for (int o = t; o < L; o += tpl) {
-        const int k = o / nbf, bf = o - k * nbf;
-        const int j = bf % m, q = bf / m;
+        const int k = div_by(o, nbf, mgn), bf = o - k * nbf;
+        const int q = div_by(bf, m, mgm), j = bf - q * m;
         C acc = C{0, 0};
         int idx = 0;  // (r k) mod R
         for (int r = 0; r < R; ++r) {
@@ -481,22 +494,22 @@ __device__ __forceinline__ void run_stages(C *S, C *W, int sn, int sb, int b, in
     for (; s < ns && is_generic_radix(si.st[s].x); ++s)
         for (int c = 0; c < ncomp; ++c) stage_generic<INV>(S + c * cstride, W, sn, sb, b, t, P, tws, si.st[s]);
     for (; s < ns && si.st[s].x == 7; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 7, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 7, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
     for (; s < ns && si.st[s].x == 5; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 5, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 5, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
     for (; s < ns && si.st[s].x == 3; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 3, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 3, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
     if constexpr (EM >= 16)
         for (; s < ns && si.st[s].x == 16; ++s)
-            for (int c = 0; c < ncomp; ++c) stage<EM, 16, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+            for (int c = 0; c < ncomp; ++c) stage<EM, 16, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
     for (; s < ns && si.st[s].x == 8; ++s)
-        for (int c = 0; c < ncomp; ++c) stage<EM, 8, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 8, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
     if (s < ns && si.st[s].x == 4) {
-        for (int c = 0; c < ncomp; ++c) stage<EM, 4, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 4, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
         ++s;
     }
     if (s < ns && si.st[s].x == 2) {
-        for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s]);
+        for (int c = 0; c < ncomp; ++c) stage<EM, 2, INV>(S + c * cstride, sn, sb, b, t, P, tws, si.st[s], si.lm[s], si.mg[s]);
         ++s;
     }
 }
