@@ -269,8 +269,11 @@ int ps_get_kernel(const ps_solver *h, double *out, long long capacity);
  *   ps_batch_pull(b, i, ax, ay, az)                     pull of problem i's A
  *
  * Same field layout, components and errors as the single-problem calls; a
- * solve fails with PS_ERR_STATE if a problem has nothing pushed. Every
- * problem is solved with the run-time transform kernels (any length).
+ * solve fails with PS_ERR_STATE if a problem has nothing pushed. The batched
+ * launches run the run-time transform kernels (any length); FP32 passes over
+ * power-of-two lengths that a compiled family covers run as the problem's
+ * own launch right after them. Many right-hand sides of one problem are
+ * problems added with the same setup: they share its kernel build.
  * ps_batch_solve runs asynchronously on the batch's stream; pulls wait. */
 typedef struct ps_batch ps_batch;
 int ps_batch_create(ps_batch **out, int precision);
@@ -312,7 +315,11 @@ enum {
                                              tiles, plus the passes of FP32 problems routed to their own
                                              kernel family (power-of-two lengths the compiled families cover) */
     PS_BATCH_INFO_TILES_PER_SOLVE = 1,    /* CTA tiles of the last captured solve, all passes */
-    PS_BATCH_INFO_POINTS = 2              /* grid points over all problems */
+    PS_BATCH_INFO_POINTS = 2,             /* grid points over all problems */
+    PS_BATCH_INFO_KERNEL_BUILDS = 3       /* Green's-kernel octants computed for the batch's problems: a
+                                             problem added with the grid, boundary conditions, spacing and
+                                             regularisation of an earlier one (another right-hand side)
+                                             copies that one's octant instead */
 };
 int ps_batch_get_info(const ps_batch *b, int what, double *value);
 const char *ps_batch_last_error(const ps_batch *b);

@@ -52,6 +52,7 @@ FAMILY_NAMES = {0: "runtime", 1: "p2", 2: "wide", 3: "tmem", 4: "tma", 5: "tc"}
 PS_BATCH_INFO_LAUNCHES_PER_SOLVE = 0
 PS_BATCH_INFO_TILES_PER_SOLVE = 1
 PS_BATCH_INFO_POINTS = 2
+PS_BATCH_INFO_KERNEL_BUILDS = 3
 
 # Every symbol the header declares, with (restype, argtypes).
 _vp = ctypes.c_void_p

@@ -79,12 +79,24 @@ struct Batch {
         return *items[i];
     }
 
+    // A problem with the setup of an earlier one (another right-hand side of
+    // the same problem) copies that problem's kernel octant instead of
+    // building its own.
     int add(const int ncell[3], const int bc[3], const double dx[3], int reg)
     {
         auto s = std::make_unique<Solver>();
         s->stream = stream;
         s->precision = precision;
+        for (const auto &o : items) {
+            bool same = o->dims == 3 && o->reg == reg && o->kernel_family == s->kernel_family;
+            for (int d = 0; d < 3 && same; ++d) same = o->n[d] == ncell[d] && o->bc[d] == bc[d] && o->dx[d] == dx[d];
+            if (same) {
+                s->kernel_from = o.get();
+                break;
+            }
+        }
         s->setup3d(ncell, bc, dx, reg);
+        s->kernel_from = nullptr;
         items.push_back(std::move(s));
         dirty = true;
         return (int)items.size() - 1;
@@ -667,6 +679,12 @@ int ps_batch_get_info(const ps_batch *h, int what, double *value)
         double pts = 0;
         for (const auto &s : b.items) pts += (double)s->n[0] * s->n[1] * s->n[2];
         *value = pts;
+        break;
+    }
+    case PS_BATCH_INFO_KERNEL_BUILDS: {
+        int k = 0;
+        for (const auto &s : b.items) k += s->kernel_builds;
+        *value = (double)k;
         break;
     }
     default: return PS_ERR_ARGUMENT;

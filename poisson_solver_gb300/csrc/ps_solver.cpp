@@ -602,6 +602,17 @@ void Solver::build_kernel()
     const int prec = PREC_FP64;
     const size_t nk = (size_t)Mx * oy * oz;
     kern64.ensure(nk * sizeof(double));
+    if (const Solver *k = kernel_from) {
+        bool same = k->is_setup && k->kern64.p && k->dims == dims && k->reg == reg &&
+                    k->kernel_family == kernel_family && k->gauss_width == gauss_width;
+        for (int d = 0; d < 3 && same; ++d) same = k->P[d] == P[d] && k->bc[d] == bc[d] && k->dx[d] == dx[d];
+        if (same) {
+            PS_CK(cudaMemcpyAsync(kern64.p, k->kern64.p, nk * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+            PS_CK(cudaStreamSynchronize(stream));
+            return;
+        }
+    }
+    ++kernel_builds;
     KernelFillArgs fa{};
     fa.kern = (double *)kern64.p;
     fa.Mx = Mx;

@@ -118,6 +118,12 @@ struct Solver {
     int precision = PREC_FP64;
 
     DevBuf kern64, kern32, kern_df;  // octant K = G zeta / (Px Py Pz); kern_df: double-float pairs
+    // A handle whose FP64 kernel octant the next build copies instead of
+    // computing, when it was built from the same inputs (the batch sets it
+    // for a problem added with the setup of an earlier one); kernel_builds
+    // counts the octants computed, not copied.
+    const Solver *kernel_from = nullptr;
+    int kernel_builds = 0;
     DevBuf kernzf32;        // FP32 K with z fastest, [oy][Mx][kzp] (unbounded z of 256..1024 points)
     DevBuf zeta64, zeta32, zeta_df;  // octant zeta / (Px Py Pz), built on first use
     DevBuf smooth64, smooth32, smooth_df;  // octant exp(-s^2 |k|^2 / 2) / (Px Py Pz) of smooth3d(s)

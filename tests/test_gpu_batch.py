@@ -273,3 +273,41 @@ def test_fp32_batch_routes_power_of_two_problems(native, oracle):
                     assert np.array_equal(a, s), f"problem {i}: batched and single solves differ"
             assert rel_l2([a for a, s in zip(A, single) if s is not None], [r for r in ref if r is not None]) < FP32_TOL
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_many_right_hand_sides_share_one_kernel_build(native, oracle, precision):
+    """Right-hand sides of one problem are problems added with the same setup:
+    they copy the first one's kernel octant instead of building their own
+    (PS_BATCH_INFO_KERNEL_BUILDS), and every solution still matches the
+    oracle and, in FP64, the single-problem solve bit for bit."""
+    psg = native
+    nc, bc, reg = (24, 18, 14), (0, 0, 0), 2
+    other = ((12, 10, 9), (1, 1, 0))
+    b = psg.PoissonBatch(precision)
+    setups = [(nc, bc)] * 4 + [other] + [(nc, bc)]
+    data = []
+    for i, (n, c) in enumerate(setups):
+        b.add(n, c, _dx(n), reg)
+        b.set_return_curl(i, True)
+        B = _fields(n, (0, 1, 2), 500 + i, zero_mean=c == (1, 1, 0))
+        b.push(i, *B)
+        data.append(B)
+    assert b.info(psg._lib.PS_BATCH_INFO_KERNEL_BUILDS) == 2
+    b.solve()
+    tol = FP64_TOL if precision == "fp64" else FP32_TOL
+    for i, (n, c) in enumerate(setups):
+        shape = (n[2], n[1], n[0])
+        A = [np.empty(shape) for _ in range(3)]
+        b.pull(i, *A)
+        ref, _ = oracle.solve3d(n, c, _dx(n), data[i], reg, curl=True)
+        assert rel_l2(A, ref) < tol, i
+        if precision == "fp64":
+            single, _ = psg.solve(n, c, _dx(n), data[i], reg, precision="fp64", curl=True)
+            for x, y in zip(A, single):
+                assert np.array_equal(x, y), i
+    # a changed kernel family is built anew and is not shared by later adds
+    b.set_kernel(0, "gaussian", 0.0)
+    b.add(nc, bc, _dx(nc), reg)
+    assert b.info(psg._lib.PS_BATCH_INFO_KERNEL_BUILDS) == 3
+    b.close()
