@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "ps_dfloat.cuh"
 #include "ps_types.hpp"
 
@@ -555,19 +557,24 @@ __device__ __forceinline__ void ct_stages(C *Sl, int sn, int sb, int b, int t, c
 }
 
 // The convolution transforms of a Bluestein plan: compile-time stages for
-// the marked power-of-two lengths, the run-time stage loop otherwise.
+// the marked power-of-two lengths in FP32 and FP64, the run-time stage loop
+// otherwise (double-float transforms included: unrolled, their arithmetic
+// made the compile of their instantiations several times longer).
 template <bool INV, int EM, typename C>
 __device__ __forceinline__ void blue_stages(C *S, C *W, int sn, int sb, int b, int t, const FftPlanDev &P,
                                             const C *tws, const StageInfo &si, int ncomp, int cstride)
 {
-    switch (P.ctm) {
-    case 64: ct_stages<INV, EM, 64>(S, sn, sb, b, t, tws, ncomp, cstride); break;
-    case 128: ct_stages<INV, EM, 128>(S, sn, sb, b, t, tws, ncomp, cstride); break;
-    case 256: ct_stages<INV, EM, 256>(S, sn, sb, b, t, tws, ncomp, cstride); break;
-    case 512: ct_stages<INV, EM, 512>(S, sn, sb, b, t, tws, ncomp, cstride); break;
-    case 1024: ct_stages<INV, EM, 1024>(S, sn, sb, b, t, tws, ncomp, cstride); break;
-    default: fft_stages<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
+    if constexpr (std::is_same<C, float2>::value || std::is_same<C, double2>::value) {
+        switch (P.ctm) {
+        case 64: ct_stages<INV, EM, 64>(S, sn, sb, b, t, tws, ncomp, cstride); return;
+        case 128: ct_stages<INV, EM, 128>(S, sn, sb, b, t, tws, ncomp, cstride); return;
+        case 256: ct_stages<INV, EM, 256>(S, sn, sb, b, t, tws, ncomp, cstride); return;
+        case 512: ct_stages<INV, EM, 512>(S, sn, sb, b, t, tws, ncomp, cstride); return;
+        case 1024: ct_stages<INV, EM, 1024>(S, sn, sb, b, t, tws, ncomp, cstride); return;
+        default: break;
+        }
     }
+    fft_stages<INV, EM>(S, W, sn, sb, b, t, P, tws, si, ncomp, cstride);
 }
 
 // Bluestein's algorithm for a length lb with a large prime factor, on lines
